@@ -1,0 +1,185 @@
+/*
+ * sphx.h -- C ABI of the GB300 (sm_103a) execution policy for SPHinXsys'
+ * weakly-compressible fluid step.
+ *
+ * Every entry point returns an int status (SPHX_OK or an SPHX_ERR_* code), never
+ * calls exit(), and records a message readable with sphx_last_error().  Work is
+ * enqueued on the stream of the context; entry points that return a value to the
+ * host (time steps, reductions, capacities) synchronise that stream, like the
+ * reference's ReduceDynamics::exec.  A context is used from one host thread at a
+ * time, as the reference drives its single in-order device queue
+ * (src/src_sycl/shared/particle_dynamics/implementation_sycl.h:43-94).
+ *
+ * Data layout: every particle variable lives on the device as structure-of-arrays
+ * (component c of particle i at base[c * n + i]); sphx_body_upload/download do the
+ * AoS <-> SoA transpose of the reference's Eigen Vecd arrays at the boundary.
+ * Reference paths below are relative to the SPHinXsys source tree.
+ */
+#ifndef SPHX_H
+#define SPHX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status codes */
+#define SPHX_OK 0
+#define SPHX_ERR_INVALID_ARG 1  /* bad handle, size, name or parameter */
+#define SPHX_ERR_CUDA 2         /* a CUDA runtime call failed */
+#define SPHX_ERR_CAPACITY 3     /* neighbour or cell storage too small (after retry) */
+#define SPHX_ERR_OUT_OF_MEMORY 4
+#define SPHX_ERR_NOT_FOUND 5    /* unknown variable name */
+#define SPHX_ERR_TIMEOUT 6      /* a bounded device wait gave up */
+#define SPHX_ERR_NUMERIC 7      /* non-finite value detected by a checked entry point */
+#define SPHX_ERR_NO_DEVICE 8
+
+typedef struct sphx_ctx_s *sphx_ctx;
+typedef struct sphx_body_s *sphx_body;
+typedef struct sphx_cell_list_s *sphx_cell_list;
+typedef struct sphx_relation_s *sphx_relation;
+
+typedef enum { SPHX_F64 = 0, SPHX_U32 = 1, SPHX_F32 = 2, SPHX_I32 = 3 } sphx_dtype;
+
+/* Message of the last failing call on this host thread (static storage). */
+const char *sphx_last_error(void);
+/* Library version string. */
+const char *sphx_version(void);
+
+/* ------------------------------------------------------------------ context
+ * Replaces the SYCL device queue singleton and USM helpers
+ * (src/src_sycl/shared/particle_dynamics/implementation_sycl.h:43-139).  `stream`
+ * may be 0 to let the context create its own non-blocking stream; otherwise it is a
+ * cudaStream_t owned by the caller. */
+int sphx_ctx_create(int device, void *stream, sphx_ctx *out);
+int sphx_ctx_destroy(sphx_ctx ctx);
+int sphx_ctx_synchronize(sphx_ctx ctx);
+/* Number of kernels this context has launched so far. */
+int sphx_ctx_launch_count(sphx_ctx ctx, uint64_t *count);
+/* The cudaStream_t the context enqueues on. */
+int sphx_ctx_stream(sphx_ctx ctx, void **stream);
+
+/* ------------------------------------------------------------------ particles
+ * A body's particle variables, the device mirror of BaseParticles' DiscreteVariable
+ * registry (src/shared/common/sphinxsys_variable.h:119-378; DelegatedData at :282-289,
+ * prepareForOutput/finalizeLoadIn at :350-356).  `dim` is 2 or 3.  Variables used by
+ * the fluid step: Position, Velocity, Force, ForcePrior (dim components); Density,
+ * Pressure, DensityChangeRate, Mass, VolumetricMeasure, DensitySummation (scalars);
+ * OriginalID, SortedID (u32).  Wall bodies add NormalDirection, Velocity and
+ * Acceleration (the Solid averages, src/shared/materials/base_material.cpp:57-72). */
+int sphx_body_create(sphx_ctx ctx, int dim, size_t n, sphx_body *out);
+int sphx_body_destroy(sphx_body body);
+int sphx_body_size(sphx_body body, size_t *n);
+/* registerStateVariable: creates (zero-filled) a variable if absent. */
+int sphx_body_register(sphx_body body, const char *name, sphx_dtype dtype, int ncomp);
+/* Host AoS (n x ncomp) -> device SoA; registers the variable if needed. */
+int sphx_body_upload(sphx_body body, const char *name, sphx_dtype dtype, int ncomp, const void *host, size_t n);
+/* Device SoA -> host AoS (n x ncomp); synchronises the stream. */
+int sphx_body_download(sphx_body body, const char *name, void *host, size_t n);
+/* DelegatedData(CudaDevicePolicy): device base pointer of a variable (SoA). */
+int sphx_body_device_ptr(sphx_body body, const char *name, void **dev, sphx_dtype *dtype, int *ncomp);
+
+/* ------------------------------------------------------------------ mesh + cell list */
+typedef struct
+{
+    int dim;
+    int all_cells[3];   /* cells per axis (all_grid_points - 1) */
+    double lower[3];    /* mesh_lower_bound_ */
+    double grid_spacing;
+} sphx_mesh_desc;
+
+/* Mesh::Mesh(tentative_bounds, grid_spacing, buffer_width)
+ * (src/shared/meshes/base_mesh.cpp:6-16). */
+int sphx_mesh_from_bounds(int dim, const double *lower, const double *upper, double grid_spacing, int buffer_width,
+                          sphx_mesh_desc *out);
+
+/* CellLinkedList<SPHAdaptation> storage: CellOffset[ncells+1] and ParticleIndex
+ * (src/shared/meshes/cell_linked_list.cpp:160-175). */
+int sphx_cell_list_create(sphx_ctx ctx, const sphx_mesh_desc *mesh, size_t particle_capacity, sphx_cell_list *out);
+int sphx_cell_list_destroy(sphx_cell_list cl);
+/* UpdateCellLinkedList::exec / BaseCellLinkedList::UpdateCellLists
+ * (update_cell_linked_list.hpp:40-106, cell_linked_list.cpp:84-101): hash by
+ * CellIndexFromPosition (base_mesh.hxx:9-15), count, exclusive scan, scatter.  Inside a
+ * cell the particles ascend by index, a canonical form of the reference's
+ * unordered atomic / concurrent_vector fill. */
+int sphx_cell_list_update(sphx_cell_list cl, sphx_body body);
+int sphx_cell_list_num_cells(sphx_cell_list cl, size_t *ncells);
+/* Copies CellOffset (ncells+1) and ParticleIndex (n) to the host. */
+int sphx_cell_list_download(sphx_cell_list cl, uint32_t *cell_offset, uint32_t *particle_index, size_t n);
+
+/* exclusive_scan(ParallelDevicePolicy, ...) (src/src_sycl/shared/common/
+ * algorithm_primitive_sycl.h:96-122): device u32 exclusive prefix sum of n entries,
+ * returns the total through *total (synchronises). */
+int sphx_exclusive_scan_u32(sphx_ctx ctx, const uint32_t *d_in, uint32_t *d_out, size_t n, uint32_t *total);
+
+/* ------------------------------------------------------------------ relations
+ * InnerRelation (src/shared/body_relations/inner_body_relation.cpp:10-20) and
+ * ContactRelation (contact_body_relation.cpp:11-32).  The Wendland C2 kernel of
+ * smoothing length h (kernel_wendland_c2.cpp:8-45) is evaluated once per
+ * configuration update, as NeighborBuilderInner/Contact do (neighborhood.cpp:26-160).
+ * Contact `search_depth` is SearchDepthContact (base_body_relation.cpp:10-16). */
+int sphx_inner_relation_create(sphx_body body, sphx_cell_list cl, double h, sphx_relation *out);
+int sphx_contact_relation_create(sphx_body body, sphx_body target, sphx_cell_list target_cl, double h,
+                                 int search_depth, double target_rho0, sphx_relation *out);
+int sphx_relation_destroy(sphx_relation rel);
+/* updateConfiguration(): neighbour search on the current positions.  Grows its
+ * storage and searches again when a list overflows (synchronises once). */
+int sphx_relation_update(sphx_relation rel);
+/* Neighbour lists as CSR on the host: counts[n_src] and, when non-null, j/W/dW/r of
+ * total = sum(counts) entries and e (total x dim); lists follow cell scan order. */
+int sphx_relation_download(sphx_relation rel, uint32_t *counts, uint32_t *j, double *W, double *dW, double *r,
+                           double *e, size_t *total);
+
+/* ------------------------------------------------------------------ fluid dynamics */
+typedef struct
+{
+    double rho0, c0;        /* WeaklyCompressibleFluid (weakly_compressible_fluid.cpp:8-30) */
+    double h;               /* smoothing length (adaptation.h:71, h = 1.3 dp) */
+    double sigma0;          /* SPHAdaptation::LatticeNumberDensity (adaptation.cpp:25-58) */
+    double limiter_slope;   /* TruncatedLinear slope of AcousticRiemannSolver (riemann_solver.h:87), 3 */
+    double acoustic_cfl;    /* AcousticTimeStep default 0.6 (fluid_time_step.h) */
+    double advection_cfl;   /* AdvectionTimeStep default 0.25 */
+    double U_ref;           /* AdvectionTimeStep reference speed */
+} sphx_fluid_params;
+
+/* SPHAdaptation::computeLatticeNumberDensity for Wendland C2 (adaptation.cpp:25-58). */
+int sphx_lattice_number_density(int dim, double h, double dp, double *sigma0);
+
+/* InteractionWithUpdate<DensitySummationComplexFreeSurface>::exec
+ * (density_summation.cpp:74-82,124-144; density_summation.hpp:28-32). */
+int sphx_density_summation_complex_free_surface(sphx_relation inner, sphx_relation wall_contact,
+                                                const sphx_fluid_params *p);
+/* Dynamics1Level<Integration1stHalfWithWallRiemann>::exec(dt)
+ * (dynamics_algorithms.h:336-352; fluid_integration.hpp:49-113). */
+int sphx_integration_1st_half_with_wall_riemann(sphx_relation inner, sphx_relation wall_contact,
+                                                const sphx_fluid_params *p, double dt);
+/* Dynamics1Level<Integration2ndHalfWithWallRiemann>::exec(dt) (fluid_integration.hpp:166-231). */
+int sphx_integration_2nd_half_with_wall_riemann(sphx_relation inner, sphx_relation wall_contact,
+                                                const sphx_fluid_params *p, double dt);
+/* ReduceDynamics<AcousticTimeStep>::exec (fluid_time_step.cpp:21-31). */
+int sphx_acoustic_time_step(sphx_body fluid, const sphx_fluid_params *p, double *dt);
+/* ReduceDynamics<AdvectionTimeStep>::exec (fluid_time_step.cpp:54-65). */
+int sphx_advection_time_step(sphx_body fluid, const sphx_fluid_params *p, double *dt);
+/* SimpleDynamics<GravityForce<Gravity>>::exec (force_prior.hpp:20-41). */
+int sphx_gravity_force(sphx_body fluid, const double *gravity);
+/* ParticleSorting::exec (particle_sorting.cpp:25-58): Morton order of the cell of
+ * `mesh` (base_mesh.hxx:80-99), stable in the current index; permutes every variable
+ * of the body and refreshes SortedID. */
+int sphx_particle_sorting(sphx_body body, const sphx_mesh_desc *mesh);
+
+/* ------------------------------------------------------------------ observation */
+/* ObservingAQuantity<Real> over a contact relation from observer points
+ * (general_interpolation.h:58-78): out[i] = sum W V q / (sum W V + TinyReal). */
+int sphx_observe_quantity(sphx_relation observer_contact, const char *name, double *out);
+/* ReduceDynamics<TotalMechanicalEnergy> (general_reduce.cpp:75-79). */
+int sphx_total_mechanical_energy(sphx_body fluid, const double *gravity, double *energy);
+/* UpperFrontInAxisDirection over an axis-aligned box region (general_reduce.h:82-99). */
+int sphx_upper_front_in_axis_direction(sphx_body fluid, int axis, const double *region_lower,
+                                       const double *region_upper, double *front);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPHX_H */

@@ -10,7 +10,7 @@ observer points.
   (y vertical, dp = 0.05; used for the regression-series check).
 * ``dambreak_3d`` is the benchmark tank: 3.2 x 1.0 x 1.8 (x, y, z) with a 1.2 x 1.0 x 0.6
   water block at x = 0, z vertical, rho0 = 1, g = 1, U_ref = 2 sqrt(g H), c0 = 10 U_ref,
-  4 wall layers.  dp = 0.0075 gives 1,702,400 fluid particles, dp = 0.006 gives 3,320,000.
+  4 wall layers.  dp = 0.0075 gives 1,702,400 fluid particles, dp = 0.006 gives 3,340,000.
 """
 from __future__ import annotations
 

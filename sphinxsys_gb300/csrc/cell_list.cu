@@ -1,0 +1,548 @@
+// Cell linked list (counting sort of particles into cells), device exclusive scan and
+// the Morton particle sort.
+//
+// Reference: UpdateCellLinkedList (src/shared/shared_ck/particle_dynamics/
+// configuration_dynamics/update_cell_linked_list.hpp:40-106), BaseCellLinkedList::
+// UpdateCellLists (src/shared/meshes/cell_linked_list.cpp:84-101), Mesh cell hashing
+// (src/shared/meshes/base_mesh.hxx:9-26,68-99), ParticleSorting
+// (src/shared/particle_dynamics/configuration_dynamics/particle_sorting.cpp:25-58).
+#include <algorithm>
+
+#include "sphx_device.cuh"
+#include "sphx_internal.cuh"
+
+using namespace sphx;
+
+namespace
+{
+constexpr unsigned kBlock = 256;
+constexpr unsigned kScanItems = 8;                  // items per thread in the scan
+constexpr unsigned kScanTile = kBlock * kScanItems; // items per block
+
+// Hash every particle into its cell and take its arrival rank in that cell.
+template <int D>
+__global__ void k_hash_count(size_t n, const double *__restrict__ pos, MeshDev m, uint32_t *__restrict__ cell_of,
+                             uint32_t *__restrict__ rank, uint32_t *__restrict__ count)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    double x[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+        x[a] = pos[a * n + i];
+    int c[3];
+    cell_index<D>(m, x, c);
+    uint32_t lc = linear_cell<D>(m, c);
+    cell_of[i] = lc;
+    rank[i] = atomicAdd(&count[lc], 1u);
+}
+
+// Block-local exclusive scan helper: each thread owns kScanItems consecutive items.
+__device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *smem_warp, uint32_t &block_total)
+{
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= unsigned(o))
+            x += y;
+    }
+    if (lane == 31)
+        smem_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0)
+    {
+        uint32_t w = lane < (blockDim.x >> 5) ? smem_warp[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= unsigned(o))
+                w += y;
+        }
+        smem_warp[lane] = w;
+    }
+    __syncthreads();
+    uint32_t warp_prefix = warp > 0 ? smem_warp[warp - 1] : 0u;
+    block_total = smem_warp[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return warp_prefix + x - v;
+}
+
+// Pass 1: per-tile sums.
+__global__ void k_scan_tile_sums(const uint32_t *__restrict__ in, size_t n, uint32_t *__restrict__ tile_sums)
+{
+    __shared__ uint32_t sw[32];
+    size_t base = size_t(blockIdx.x) * kScanTile + size_t(threadIdx.x) * kScanItems;
+    uint32_t s = 0;
+#pragma unroll
+    for (unsigned k = 0; k < kScanItems; ++k)
+        if (base + k < n)
+            s += in[base + k];
+    uint32_t total;
+    block_exclusive_scan(s, sw, total);
+    if (threadIdx.x == 0)
+        tile_sums[blockIdx.x] = total;
+}
+
+// Pass 2: exclusive scan of the tile sums by one block (loops over chunks).
+__global__ void k_scan_tile_prefix(uint32_t *__restrict__ tile_sums, size_t ntiles, uint32_t *__restrict__ total_out)
+{
+    __shared__ uint32_t sw[32];
+    uint32_t carry = 0;
+    for (size_t base = 0; base < ntiles; base += blockDim.x)
+    {
+        size_t i = base + threadIdx.x;
+        uint32_t v = i < ntiles ? tile_sums[i] : 0u;
+        uint32_t tot;
+        uint32_t ex = block_exclusive_scan(v, sw, tot);
+        if (i < ntiles)
+            tile_sums[i] = carry + ex;
+        carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && total_out)
+        *total_out = carry;
+}
+
+// Pass 3: scan inside each tile, offset by the tile prefix.
+__global__ void k_scan_apply(const uint32_t *__restrict__ in, uint32_t *__restrict__ out, size_t n,
+                             const uint32_t *__restrict__ tile_prefix)
+{
+    __shared__ uint32_t sw[32];
+    size_t base = size_t(blockIdx.x) * kScanTile + size_t(threadIdx.x) * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t s = 0;
+#pragma unroll
+    for (unsigned k = 0; k < kScanItems; ++k)
+    {
+        v[k] = base + k < n ? in[base + k] : 0u;
+        s += v[k];
+    }
+    uint32_t total;
+    uint32_t run = tile_prefix[blockIdx.x] + block_exclusive_scan(s, sw, total);
+#pragma unroll
+    for (unsigned k = 0; k < kScanItems; ++k)
+        if (base + k < n)
+        {
+            out[base + k] = run;
+            run += v[k];
+        }
+}
+
+__global__ void k_count_keys(size_t n, const uint32_t *__restrict__ key, uint32_t *__restrict__ rank,
+                             uint32_t *__restrict__ count)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n)
+        rank[i] = atomicAdd(&count[key[i]], 1u);
+}
+
+// offset[nkeys] = total, closing the CellOffset array (cell_linked_list.cpp:171-174).
+__global__ void k_set_total(uint32_t *offset, uint32_t nkeys, uint32_t total) { offset[nkeys] = total; }
+
+__global__ void k_scatter(size_t n, const uint32_t *__restrict__ cell_of, const uint32_t *__restrict__ rank,
+                          const uint32_t *__restrict__ offset, uint32_t *__restrict__ particle_index)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n)
+        particle_index[offset[cell_of[i]] + rank[i]] = uint32_t(i);
+}
+
+// Puts each cell's particles in ascending index order (insertion sort of a short segment).
+__global__ void k_sort_segments(size_t nseg, const uint32_t *__restrict__ offset, uint32_t *__restrict__ idx)
+{
+    size_t c = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= nseg)
+        return;
+    uint32_t b = offset[c], e = offset[c + 1];
+    for (uint32_t k = b + 1; k < e; ++k)
+    {
+        uint32_t v = idx[k];
+        uint32_t m = k;
+        while (m > b && idx[m - 1] > v)
+        {
+            idx[m] = idx[m - 1];
+            --m;
+        }
+        idx[m] = v;
+    }
+}
+
+// Cell-ordered copies of the positions: exact FP64 and the FP32 offset from the lower
+// corner of the particle's cell (for the neighbour-search pre-filter).
+template <int D>
+__global__ void k_gather_sorted(size_t n, const uint32_t *__restrict__ idx, const uint32_t *__restrict__ cell_of,
+                                const double *__restrict__ pos, MeshDev m, double *__restrict__ spos,
+                                float *__restrict__ soff)
+{
+    size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= n)
+        return;
+    uint32_t i = idx[k];
+    int c[3];
+    cell_from_linear<D>(m, cell_of[i], c);
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+    {
+        double x = pos[a * n + i];
+        spos[a * n + k] = x;
+        soff[a * n + k] = float(x - cell_corner(m, a, c[a]));
+    }
+}
+
+template <int D>
+__global__ void k_morton_key(size_t n, const double *__restrict__ pos, MeshDev m, uint32_t *__restrict__ key)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    double x[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+        x[a] = pos[a * n + i];
+    int c[3];
+    cell_index<D>(m, x, c);
+    key[i] = morton_key<D>(c);
+}
+
+template <typename T>
+__global__ void k_permute(size_t n, int ncomp, const uint32_t *__restrict__ perm, const T *__restrict__ src,
+                          T *__restrict__ dst)
+{
+    size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= n)
+        return;
+    uint32_t i = perm[k];
+    for (int c = 0; c < ncomp; ++c)
+        dst[c * n + k] = src[c * n + i];
+}
+
+__global__ void k_sorted_id(size_t n, const uint32_t *__restrict__ original_id, uint32_t *__restrict__ sorted_id)
+{
+    size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k < n)
+        sorted_id[original_id[k]] = uint32_t(k);
+}
+
+__global__ void k_morton_rank_key(size_t n, const double *__restrict__ pos, MeshDev m, int dim,
+                                  const uint32_t *__restrict__ morton_rank, uint32_t *__restrict__ key)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    double x[3] = {0, 0, 0};
+    for (int a = 0; a < dim; ++a)
+        x[a] = pos[a * n + i];
+    int c[3];
+    uint32_t lc;
+    if (dim == 2)
+    {
+        cell_index<2>(m, x, c);
+        lc = linear_cell<2>(m, c);
+    }
+    else
+    {
+        cell_index<3>(m, x, c);
+        lc = linear_cell<3>(m, c);
+    }
+    key[i] = morton_rank[lc];
+}
+} // namespace
+
+namespace sphx
+{
+int exclusive_scan(sphx_ctx ctx, const uint32_t *d_in, uint32_t *d_out, size_t n)
+{
+    if (n == 0)
+        return SPHX_OK;
+    size_t ntiles = (n + kScanTile - 1) / kScanTile;
+    SPHX_TRY(ctx->ensure_scratch((ntiles + 1) * sizeof(uint32_t)));
+    uint32_t *tiles = static_cast<uint32_t *>(ctx->d_scratch);
+    k_scan_tile_sums<<<unsigned(ntiles), kBlock, 0, ctx->stream>>>(d_in, n, tiles);
+    SPHX_LAUNCHED(ctx);
+    k_scan_tile_prefix<<<1, 1024, 0, ctx->stream>>>(tiles, ntiles, tiles + ntiles);
+    SPHX_LAUNCHED(ctx);
+    k_scan_apply<<<unsigned(ntiles), kBlock, 0, ctx->stream>>>(d_in, d_out, n, tiles);
+    SPHX_LAUNCHED(ctx);
+    return SPHX_OK;
+}
+
+// Stable counting sort of n keys in [0, nkeys): d_offset[nkeys+1] gets the key offsets,
+// d_perm[k] the index of the k-th particle in key order (ascending index within a key).
+int counting_sort_by_key(sphx_ctx ctx, const uint32_t *d_key, size_t n, uint32_t nkeys, uint32_t *d_offset,
+                         uint32_t *d_count, uint32_t *d_rank, uint32_t *d_perm)
+{
+    cudaStream_t s = ctx->stream;
+    SPHX_CUDA(cudaMemsetAsync(d_count, 0, size_t(nkeys) * sizeof(uint32_t), s));
+    SPHX_CUDA(cudaMemsetAsync(d_offset + nkeys, 0, sizeof(uint32_t), s));
+    if (n == 0)
+    {
+        SPHX_CUDA(cudaMemsetAsync(d_offset, 0, size_t(nkeys) * sizeof(uint32_t), s));
+        return SPHX_OK;
+    }
+    k_count_keys<<<grid_for(n, kBlock), kBlock, 0, s>>>(n, d_key, d_rank, d_count);
+    SPHX_LAUNCHED(ctx);
+    SPHX_TRY(exclusive_scan(ctx, d_count, d_offset, nkeys));
+    k_set_total<<<1, 1, 0, s>>>(d_offset, nkeys, uint32_t(n));
+    SPHX_LAUNCHED(ctx);
+    k_scatter<<<grid_for(n, kBlock), kBlock, 0, s>>>(n, d_key, d_rank, d_offset, d_perm);
+    SPHX_LAUNCHED(ctx);
+    k_sort_segments<<<grid_for(nkeys, kBlock), kBlock, 0, s>>>(nkeys, d_offset, d_perm);
+    SPHX_LAUNCHED(ctx);
+    return SPHX_OK;
+}
+} // namespace sphx
+
+int sphx_cell_list_s::reserve(size_t np)
+{
+    if (np <= capacity && particle_index)
+        return SPHX_OK;
+    cudaFree(particle_index);
+    cudaFree(cell_of);
+    cudaFree(rank);
+    cudaFree(sorted_pos);
+    cudaFree(sorted_off);
+    particle_index = cell_of = rank = nullptr;
+    sorted_pos = nullptr;
+    sorted_off = nullptr;
+    size_t cap = std::max<size_t>(np, 1);
+    SPHX_CUDA(cudaMalloc(&particle_index, std::max(cap, ncells) * sizeof(uint32_t)));
+    SPHX_CUDA(cudaMalloc(&cell_of, cap * sizeof(uint32_t)));
+    SPHX_CUDA(cudaMalloc(&rank, cap * sizeof(uint32_t)));
+    SPHX_CUDA(cudaMalloc(&sorted_pos, 3 * cap * sizeof(double)));
+    SPHX_CUDA(cudaMalloc(&sorted_off, 3 * cap * sizeof(float)));
+    capacity = cap;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_cell_list_create(sphx_ctx ctx, const sphx_mesh_desc *mesh, size_t particle_capacity,
+                                     sphx_cell_list *out)
+{
+    if (!ctx || !mesh || !out || (mesh->dim != 2 && mesh->dim != 3) || !(mesh->grid_spacing > 0))
+        return fail(SPHX_ERR_INVALID_ARG, "invalid cell list arguments");
+    size_t nc = 1;
+    for (int a = 0; a < mesh->dim; ++a)
+    {
+        if (mesh->all_cells[a] < 1)
+            return fail(SPHX_ERR_INVALID_ARG, "mesh axis %d has no cells", a);
+        nc *= size_t(mesh->all_cells[a]);
+    }
+    if (nc >= 0xffffffffull)
+        return fail(SPHX_ERR_INVALID_ARG, "mesh of %zu cells exceeds 32-bit cell indices", nc);
+    sphx_cell_list cl = new sphx_cell_list_s();
+    cl->ctx = ctx;
+    cl->mesh = *mesh;
+    cl->ncells = nc;
+    SPHX_CUDA(cudaMalloc(&cl->cell_offset, (nc + 1) * sizeof(uint32_t)));
+    SPHX_CUDA(cudaMalloc(&cl->cell_count, nc * sizeof(uint32_t)));
+    SPHX_CUDA(cudaMemsetAsync(cl->cell_offset, 0, (nc + 1) * sizeof(uint32_t), ctx->stream));
+    int st = cl->reserve(particle_capacity);
+    if (st != SPHX_OK)
+    {
+        delete cl;
+        return st;
+    }
+    *out = cl;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_cell_list_destroy(sphx_cell_list cl)
+{
+    if (!cl)
+        return SPHX_OK;
+    cudaStreamSynchronize(cl->ctx->stream);
+    cudaFree(cl->cell_offset);
+    cudaFree(cl->cell_count);
+    cudaFree(cl->particle_index);
+    cudaFree(cl->cell_of);
+    cudaFree(cl->rank);
+    cudaFree(cl->sorted_pos);
+    cudaFree(cl->sorted_off);
+    delete cl;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_cell_list_update(sphx_cell_list cl, sphx_body body)
+{
+    if (!cl || !body)
+        return fail(SPHX_ERR_INVALID_ARG, "null argument");
+    if (body->dim != cl->mesh.dim)
+        return fail(SPHX_ERR_INVALID_ARG, "body dimension %d differs from mesh dimension %d", body->dim, cl->mesh.dim);
+    Field *pos;
+    SPHX_TRY(body->need("Position", SPHX_F64, body->dim, &pos));
+    sphx_ctx ctx = cl->ctx;
+    size_t n = body->n;
+    SPHX_TRY(cl->reserve(n));
+    cl->n = n;
+    cudaStream_t s = ctx->stream;
+    MeshDev m = mesh_dev(cl->mesh);
+    const double *p = static_cast<const double *>(pos->dev);
+    SPHX_CUDA(cudaMemsetAsync(cl->cell_count, 0, cl->ncells * sizeof(uint32_t), s));
+    if (n > 0)
+    {
+        if (body->dim == 2)
+            k_hash_count<2><<<grid_for(n, kBlock), kBlock, 0, s>>>(n, p, m, cl->cell_of, cl->rank, cl->cell_count);
+        else
+            k_hash_count<3><<<grid_for(n, kBlock), kBlock, 0, s>>>(n, p, m, cl->cell_of, cl->rank, cl->cell_count);
+        SPHX_LAUNCHED(ctx);
+    }
+    SPHX_TRY(exclusive_scan(ctx, cl->cell_count, cl->cell_offset, cl->ncells));
+    k_set_total<<<1, 1, 0, s>>>(cl->cell_offset, uint32_t(cl->ncells), uint32_t(n));
+    SPHX_LAUNCHED(ctx);
+    if (n == 0)
+        return SPHX_OK;
+    k_scatter<<<grid_for(n, kBlock), kBlock, 0, s>>>(n, cl->cell_of, cl->rank, cl->cell_offset, cl->particle_index);
+    SPHX_LAUNCHED(ctx);
+    k_sort_segments<<<grid_for(cl->ncells, kBlock), kBlock, 0, s>>>(cl->ncells, cl->cell_offset, cl->particle_index);
+    SPHX_LAUNCHED(ctx);
+    if (body->dim == 2)
+        k_gather_sorted<2><<<grid_for(n, kBlock), kBlock, 0, s>>>(n, cl->particle_index, cl->cell_of, p, m,
+                                                                  cl->sorted_pos, cl->sorted_off);
+    else
+        k_gather_sorted<3><<<grid_for(n, kBlock), kBlock, 0, s>>>(n, cl->particle_index, cl->cell_of, p, m,
+                                                                  cl->sorted_pos, cl->sorted_off);
+    SPHX_LAUNCHED(ctx);
+    return SPHX_OK;
+}
+
+extern "C" int sphx_cell_list_num_cells(sphx_cell_list cl, size_t *ncells)
+{
+    if (!cl || !ncells)
+        return fail(SPHX_ERR_INVALID_ARG, "null argument");
+    *ncells = cl->ncells;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_cell_list_download(sphx_cell_list cl, uint32_t *cell_offset, uint32_t *particle_index, size_t n)
+{
+    if (!cl)
+        return fail(SPHX_ERR_INVALID_ARG, "null cell list");
+    if (n != cl->n)
+        return fail(SPHX_ERR_INVALID_ARG, "cell list holds %zu particles, not %zu", cl->n, n);
+    cudaStream_t s = cl->ctx->stream;
+    if (cell_offset)
+        SPHX_CUDA(cudaMemcpyAsync(cell_offset, cl->cell_offset, (cl->ncells + 1) * sizeof(uint32_t),
+                                  cudaMemcpyDeviceToHost, s));
+    if (particle_index && n > 0)
+        SPHX_CUDA(cudaMemcpyAsync(particle_index, cl->particle_index, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    SPHX_CUDA(cudaStreamSynchronize(s));
+    return SPHX_OK;
+}
+
+extern "C" int sphx_exclusive_scan_u32(sphx_ctx ctx, const uint32_t *d_in, uint32_t *d_out, size_t n, uint32_t *total)
+{
+    if (!ctx || (n > 0 && (!d_in || !d_out)))
+        return fail(SPHX_ERR_INVALID_ARG, "invalid scan arguments");
+    if (n == 0)
+    {
+        if (total)
+            *total = 0;
+        return SPHX_OK;
+    }
+    // The last entry of the input participates in the total only.
+    SPHX_TRY(exclusive_scan(ctx, d_in, d_out, n));
+    if (total)
+    {
+        uint32_t last_in = 0, last_out = 0;
+        SPHX_CUDA(cudaMemcpyAsync(&last_in, d_in + n - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        SPHX_CUDA(cudaMemcpyAsync(&last_out, d_out + n - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        SPHX_CUDA(cudaStreamSynchronize(ctx->stream));
+        *total = last_out + last_in;
+    }
+    return SPHX_OK;
+}
+
+extern "C" int sphx_particle_sorting(sphx_body body, const sphx_mesh_desc *mesh)
+{
+    if (!body || !mesh || mesh->dim != body->dim)
+        return fail(SPHX_ERR_INVALID_ARG, "invalid sorting arguments");
+    sphx_ctx ctx = body->ctx;
+    cudaStream_t s = ctx->stream;
+    size_t n = body->n;
+    Field *pos, *oid, *sid;
+    SPHX_TRY(body->need("Position", SPHX_F64, body->dim, &pos));
+    SPHX_TRY(body->require("OriginalID", SPHX_U32, 1, &oid));
+    SPHX_TRY(body->require("SortedID", SPHX_U32, 1, &sid));
+    if (n == 0)
+        return SPHX_OK;
+    size_t nc = 1;
+    for (int a = 0; a < mesh->dim; ++a)
+    {
+        if (mesh->all_cells[a] > 1024)
+            return fail(SPHX_ERR_INVALID_ARG, "Morton keys hold 10 bits per axis; mesh axis %d has %d cells", a,
+                        mesh->all_cells[a]);
+        nc *= size_t(mesh->all_cells[a]);
+    }
+    // Rank of each cell in Morton order (cells with distinct keys; keys are unique per cell).
+    std::vector<uint32_t> key_of_cell(nc);
+    std::vector<uint32_t> order(nc);
+    for (size_t lc = 0; lc < nc; ++lc)
+    {
+        int c[3];
+        size_t r = lc;
+        if (mesh->dim == 2)
+        {
+            c[1] = int(r % mesh->all_cells[1]);
+            c[0] = int(r / mesh->all_cells[1]);
+            key_of_cell[lc] = morton_key<2>(c);
+        }
+        else
+        {
+            c[2] = int(r % mesh->all_cells[2]);
+            r /= mesh->all_cells[2];
+            c[1] = int(r % mesh->all_cells[1]);
+            c[0] = int(r / mesh->all_cells[1]);
+            key_of_cell[lc] = morton_key<3>(c);
+        }
+        order[lc] = uint32_t(lc);
+    }
+    std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return key_of_cell[a] < key_of_cell[b]; });
+    std::vector<uint32_t> rank_of_cell(nc);
+    for (size_t r = 0; r < nc; ++r)
+        rank_of_cell[order[r]] = uint32_t(r);
+    // device buffers: morton_rank[nc], key[n], offset[nc+1], count[nc], rank[n], perm[n], tmp
+    size_t words = nc + n + (nc + 1) + nc + n + n;
+    size_t max_field = 0;
+    for (auto &kv : body->fields)
+        max_field = std::max(max_field, size_t(kv.second.ncomp) * dtype_size(kv.second.dtype));
+    size_t tmp_bytes = max_field * n;
+    uint32_t *buf = nullptr;
+    void *tmp = nullptr;
+    SPHX_CUDA(cudaMallocAsync((void **)&buf, words * sizeof(uint32_t), s));
+    SPHX_CUDA(cudaMallocAsync(&tmp, tmp_bytes, s));
+    uint32_t *d_mrank = buf, *d_key = d_mrank + nc, *d_off = d_key + n, *d_cnt = d_off + nc + 1,
+             *d_rank = d_cnt + nc, *d_perm = d_rank + n;
+    SPHX_CUDA(cudaMemcpyAsync(d_mrank, rank_of_cell.data(), nc * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    k_morton_rank_key<<<grid_for(n, kBlock), kBlock, 0, s>>>(n, static_cast<const double *>(pos->dev),
+                                                              mesh_dev(*mesh), body->dim, d_mrank, d_key);
+    SPHX_LAUNCHED(ctx);
+    SPHX_TRY(counting_sort_by_key(ctx, d_key, n, uint32_t(nc), d_off, d_cnt, d_rank, d_perm));
+    for (auto &kv : body->fields)
+    {
+        if (kv.first == "SortedID")
+            continue;
+        Field &f = kv.second;
+        size_t bytes = n * f.ncomp * dtype_size(f.dtype);
+        if (f.dtype == SPHX_F64)
+            k_permute<double><<<grid_for(n, kBlock), kBlock, 0, s>>>(n, f.ncomp, d_perm,
+                                                                     static_cast<const double *>(f.dev),
+                                                                     static_cast<double *>(tmp));
+        else
+            k_permute<uint32_t><<<grid_for(n, kBlock), kBlock, 0, s>>>(n, f.ncomp, d_perm,
+                                                                       static_cast<const uint32_t *>(f.dev),
+                                                                       static_cast<uint32_t *>(tmp));
+        SPHX_LAUNCHED(ctx);
+        SPHX_CUDA(cudaMemcpyAsync(f.dev, tmp, bytes, cudaMemcpyDeviceToDevice, s));
+    }
+    k_sorted_id<<<grid_for(n, kBlock), kBlock, 0, s>>>(n, static_cast<const uint32_t *>(oid->dev),
+                                                        static_cast<uint32_t *>(sid->dev));
+    SPHX_LAUNCHED(ctx);
+    SPHX_CUDA(cudaFreeAsync(buf, s));
+    SPHX_CUDA(cudaFreeAsync(tmp, s));
+    SPHX_CUDA(cudaStreamSynchronize(s));
+    return SPHX_OK;
+}

@@ -1,0 +1,335 @@
+// Context, particle-variable registry, mesh and kernel constants of libsphx_cuda.so.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+
+#include "sphx_internal.cuh"
+
+namespace sphx
+{
+static thread_local char g_err[512] = "";
+
+int fail(int code, const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line)
+{
+    return fail(e == cudaErrorMemoryAllocation ? SPHX_ERR_OUT_OF_MEMORY : SPHX_ERR_CUDA, "%s failed at %s:%d: %s",
+                what, file, line, cudaGetErrorString(e));
+}
+
+MeshDev mesh_dev(const sphx_mesh_desc &m)
+{
+    MeshDev d{};
+    for (int a = 0; a < 3; ++a)
+    {
+        d.lower[a] = m.lower[a];
+        d.all_cells[a] = a < m.dim ? m.all_cells[a] : 1;
+        d.grid_points[a] = d.all_cells[a] + 1;
+    }
+    d.gs = m.grid_spacing;
+    return d;
+}
+
+WendlandC2 wendland(int dim, double h)
+{
+    const double Pi = M_PI;
+    WendlandC2 k{};
+    k.h = h;
+    k.inv_h = 1.0 / h;
+    k.rc = 2.0 * h;
+    k.rc_sqr = k.rc * k.rc;
+    if (dim == 2)
+        k.factor_W = k.inv_h * k.inv_h * 7.0 / (4.0 * Pi);
+    else
+        k.factor_W = k.inv_h * k.inv_h * k.inv_h * 21.0 / (16.0 * Pi);
+    k.factor_dW = k.inv_h * k.factor_W;
+    // FP32 pre-filter on offsets of at most a few cells: relative rounding error of the
+    // squared distance stays far below 2^-10, so candidates above this bound are outside rc.
+    k.prefilter_sqr = float(k.rc_sqr * (1.0 + 1.0 / 1024.0));
+    return k;
+}
+} // namespace sphx
+
+using namespace sphx;
+
+int sphx_ctx_s::ensure_scratch(size_t bytes)
+{
+    if (bytes <= scratch_bytes)
+        return SPHX_OK;
+    if (d_scratch)
+        cudaFree(d_scratch);
+    d_scratch = nullptr;
+    scratch_bytes = 0;
+    size_t nb = bytes + bytes / 4 + 4096;
+    SPHX_CUDA(cudaMalloc(&d_scratch, nb));
+    scratch_bytes = nb;
+    return SPHX_OK;
+}
+
+int sphx_body_s::require(const char *name, sphx_dtype dtype, int nc, Field **out)
+{
+    Field *f = find(name);
+    if (f)
+    {
+        if (f->dtype != dtype || f->ncomp != nc)
+            return fail(SPHX_ERR_INVALID_ARG, "variable %s exists with another type or component count", name);
+        *out = f;
+        return SPHX_OK;
+    }
+    Field nf;
+    nf.dtype = dtype;
+    nf.ncomp = nc;
+    size_t bytes = std::max<size_t>(1, n) * size_t(nc) * dtype_size(dtype);
+    SPHX_CUDA(cudaMalloc(&nf.dev, bytes));
+    SPHX_CUDA(cudaMemsetAsync(nf.dev, 0, bytes, ctx->stream));
+    fields[name] = nf;
+    *out = &fields[name];
+    return SPHX_OK;
+}
+
+int sphx_body_s::need(const char *name, sphx_dtype dtype, int nc, Field **out)
+{
+    Field *f = find(name);
+    if (!f)
+        return fail(SPHX_ERR_NOT_FOUND, "variable %s is not registered on this body", name);
+    if (f->dtype != dtype || f->ncomp != nc)
+        return fail(SPHX_ERR_INVALID_ARG, "variable %s has another type or component count", name);
+    *out = f;
+    return SPHX_OK;
+}
+
+extern "C" const char *sphx_last_error(void) { return g_err; }
+extern "C" const char *sphx_version(void) { return "sphx-gb300 0.1 (sm_103a)"; }
+
+extern "C" int sphx_ctx_create(int device, void *stream, sphx_ctx *out)
+{
+    if (!out)
+        return fail(SPHX_ERR_INVALID_ARG, "null output handle");
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(SPHX_ERR_NO_DEVICE, "no CUDA device available (%s)", cudaGetErrorString(e));
+    if (device < 0 || device >= ndev)
+        return fail(SPHX_ERR_INVALID_ARG, "device %d out of range (%d devices)", device, ndev);
+    SPHX_CUDA(cudaSetDevice(device));
+    sphx_ctx c = new sphx_ctx_s();
+    c->device = device;
+    SPHX_CUDA(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
+    if (stream)
+        c->stream = static_cast<cudaStream_t>(stream);
+    else
+    {
+        SPHX_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        c->own_stream = true;
+    }
+    SPHX_CUDA(cudaMalloc(&c->d_red, 64 * sizeof(unsigned long long)));
+    SPHX_CUDA(cudaMallocHost(&c->h_red, 64 * sizeof(unsigned long long)));
+    *out = c;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_ctx_destroy(sphx_ctx c)
+{
+    if (!c)
+        return SPHX_OK;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    if (c->d_red)
+        cudaFree(c->d_red);
+    if (c->h_red)
+        cudaFreeHost(c->h_red);
+    if (c->d_scratch)
+        cudaFree(c->d_scratch);
+    if (c->own_stream)
+        cudaStreamDestroy(c->stream);
+    delete c;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_ctx_synchronize(sphx_ctx c)
+{
+    if (!c)
+        return fail(SPHX_ERR_INVALID_ARG, "null context");
+    SPHX_CUDA(cudaStreamSynchronize(c->stream));
+    return SPHX_OK;
+}
+
+extern "C" int sphx_ctx_launch_count(sphx_ctx c, uint64_t *count)
+{
+    if (!c || !count)
+        return fail(SPHX_ERR_INVALID_ARG, "null argument");
+    *count = c->launches;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_ctx_stream(sphx_ctx c, void **stream)
+{
+    if (!c || !stream)
+        return fail(SPHX_ERR_INVALID_ARG, "null argument");
+    *stream = c->stream;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_body_create(sphx_ctx ctx, int dim, size_t n, sphx_body *out)
+{
+    if (!ctx || !out || (dim != 2 && dim != 3))
+        return fail(SPHX_ERR_INVALID_ARG, "invalid body arguments (dim=%d)", dim);
+    if (n > 0xffffffffull)
+        return fail(SPHX_ERR_INVALID_ARG, "body size %zu exceeds 32-bit particle indices", n);
+    sphx_body b = new sphx_body_s();
+    b->ctx = ctx;
+    b->dim = dim;
+    b->n = n;
+    *out = b;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_body_destroy(sphx_body b)
+{
+    if (!b)
+        return SPHX_OK;
+    cudaStreamSynchronize(b->ctx->stream);
+    for (auto &kv : b->fields)
+        cudaFree(kv.second.dev);
+    delete b;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_body_size(sphx_body b, size_t *n)
+{
+    if (!b || !n)
+        return fail(SPHX_ERR_INVALID_ARG, "null argument");
+    *n = b->n;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_body_register(sphx_body b, const char *name, sphx_dtype dtype, int ncomp)
+{
+    if (!b || !name || ncomp < 1 || ncomp > 3)
+        return fail(SPHX_ERR_INVALID_ARG, "invalid register arguments");
+    Field *f;
+    return b->require(name, dtype, ncomp, &f);
+}
+
+extern "C" int sphx_body_upload(sphx_body b, const char *name, sphx_dtype dtype, int ncomp, const void *host,
+                                size_t n)
+{
+    if (!b || !name || !host || ncomp < 1 || ncomp > 3)
+        return fail(SPHX_ERR_INVALID_ARG, "invalid upload arguments");
+    if (n != b->n)
+        return fail(SPHX_ERR_INVALID_ARG, "upload of %s: %zu values for a body of %zu particles", name, n, b->n);
+    Field *f;
+    SPHX_TRY(b->require(name, dtype, ncomp, &f));
+    size_t es = dtype_size(dtype);
+    if (n == 0)
+        return SPHX_OK;
+    // AoS -> SoA transpose on the host, then one copy per component.
+    std::vector<unsigned char> soa(n * ncomp * es);
+    const unsigned char *src = static_cast<const unsigned char *>(host);
+    for (size_t i = 0; i < n; ++i)
+        for (int c = 0; c < ncomp; ++c)
+            std::memcpy(&soa[(c * n + i) * es], &src[(i * ncomp + c) * es], es);
+    SPHX_CUDA(cudaMemcpyAsync(f->dev, soa.data(), soa.size(), cudaMemcpyHostToDevice, b->ctx->stream));
+    SPHX_CUDA(cudaStreamSynchronize(b->ctx->stream));
+    return SPHX_OK;
+}
+
+extern "C" int sphx_body_download(sphx_body b, const char *name, void *host, size_t n)
+{
+    if (!b || !name || !host)
+        return fail(SPHX_ERR_INVALID_ARG, "invalid download arguments");
+    Field *f = b->find(name);
+    if (!f)
+        return fail(SPHX_ERR_NOT_FOUND, "variable %s is not registered", name);
+    if (n != b->n)
+        return fail(SPHX_ERR_INVALID_ARG, "download of %s: buffer for %zu of %zu particles", name, n, b->n);
+    size_t es = dtype_size(f->dtype);
+    if (n == 0)
+        return SPHX_OK;
+    std::vector<unsigned char> soa(n * f->ncomp * es);
+    SPHX_CUDA(cudaMemcpyAsync(soa.data(), f->dev, soa.size(), cudaMemcpyDeviceToHost, b->ctx->stream));
+    SPHX_CUDA(cudaStreamSynchronize(b->ctx->stream));
+    unsigned char *dst = static_cast<unsigned char *>(host);
+    for (size_t i = 0; i < n; ++i)
+        for (int c = 0; c < f->ncomp; ++c)
+            std::memcpy(&dst[(i * f->ncomp + c) * es], &soa[(c * n + i) * es], es);
+    return SPHX_OK;
+}
+
+extern "C" int sphx_body_device_ptr(sphx_body b, const char *name, void **dev, sphx_dtype *dtype, int *ncomp)
+{
+    if (!b || !name || !dev)
+        return fail(SPHX_ERR_INVALID_ARG, "invalid arguments");
+    Field *f = b->find(name);
+    if (!f)
+        return fail(SPHX_ERR_NOT_FOUND, "variable %s is not registered", name);
+    *dev = f->dev;
+    if (dtype)
+        *dtype = f->dtype;
+    if (ncomp)
+        *ncomp = f->ncomp;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_mesh_from_bounds(int dim, const double *lower, const double *upper, double gs, int buffer_width,
+                                     sphx_mesh_desc *out)
+{
+    if (!lower || !upper || !out || (dim != 2 && dim != 3) || !(gs > 0) || buffer_width < 0)
+        return fail(SPHX_ERR_INVALID_ARG, "invalid mesh arguments");
+    sphx_mesh_desc m{};
+    m.dim = dim;
+    m.grid_spacing = gs;
+    double buffer = double(buffer_width) * gs;
+    for (int a = 0; a < 3; ++a)
+    {
+        if (a < dim)
+        {
+            m.lower[a] = lower[a] - buffer;
+            double tentative = upper[a] + buffer - m.lower[a];
+            double cells = std::ceil(tentative / gs);
+            if (!(cells >= 1) || cells > 1.0e6)
+                return fail(SPHX_ERR_INVALID_ARG, "mesh axis %d has %g cells", a, cells);
+            m.all_cells[a] = int(cells) + 1 - 1;
+        }
+        else
+        {
+            m.lower[a] = 0;
+            m.all_cells[a] = 1;
+        }
+    }
+    *out = m;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_lattice_number_density(int dim, double h, double dp, double *sigma0)
+{
+    if ((dim != 2 && dim != 3) || !(h > 0) || !(dp > 0) || !sigma0)
+        return fail(SPHX_ERR_INVALID_ARG, "invalid lattice arguments");
+    WendlandC2 k = wendland(dim, h);
+    auto W = [&](double r) {
+        double q = r * k.inv_h;
+        return k.factor_W * (std::pow(1.0 - 0.5 * q, 4) * (1.0 + 2.0 * q));
+    };
+    double sigma = 0;
+    int depth = int(k.rc / dp) + 1;
+    int kmax = dim == 3 ? depth : 0;
+    for (int kk = -kmax; kk <= kmax; ++kk)
+        for (int j = -depth; j <= depth; ++j)
+            for (int i = -depth; i <= depth; ++i)
+            {
+                double x = i * dp, y = j * dp, z = kk * dp;
+                double d = dim == 2 ? std::sqrt(x * x + y * y) : std::sqrt((x * x + y * y) + z * z);
+                if (d < k.rc)
+                    sigma += W(d);
+            }
+    *sigma0 = sigma;
+    return SPHX_OK;
+}
