@@ -335,6 +335,7 @@ extern "C" int sphx_cell_list_create(sphx_ctx ctx, const sphx_mesh_desc *mesh, s
         return fail(SPHX_ERR_INVALID_ARG, "mesh of %zu cells exceeds 32-bit cell indices", nc);
     sphx_cell_list cl = new sphx_cell_list_s();
     cl->ctx = ctx;
+    ctx->retain();
     cl->mesh = *mesh;
     cl->ncells = nc;
     SPHX_CUDA(cudaMalloc(&cl->cell_offset, (nc + 1) * sizeof(uint32_t)));
@@ -343,7 +344,7 @@ extern "C" int sphx_cell_list_create(sphx_ctx ctx, const sphx_mesh_desc *mesh, s
     int st = cl->reserve(particle_capacity);
     if (st != SPHX_OK)
     {
-        delete cl;
+        sphx_cell_list_destroy(cl);
         return st;
     }
     *out = cl;
@@ -362,7 +363,9 @@ extern "C" int sphx_cell_list_destroy(sphx_cell_list cl)
     cudaFree(cl->rank);
     cudaFree(cl->sorted_pos);
     cudaFree(cl->sorted_off);
+    sphx_ctx ctx = cl->ctx;
     delete cl;
+    release(ctx);
     return SPHX_OK;
 }
 

@@ -191,6 +191,7 @@ extern "C" int sphx_inner_relation_create(sphx_body body, sphx_cell_list cl, dou
         return fail(SPHX_ERR_INVALID_ARG, "invalid inner relation arguments");
     sphx_relation r = new sphx_relation_s();
     r->ctx = body->ctx;
+    r->ctx->retain();
     r->inner = true;
     r->src = r->tgt = body;
     r->cl = cl;
@@ -210,6 +211,7 @@ extern "C" int sphx_contact_relation_create(sphx_body body, sphx_body target, sp
         return fail(SPHX_ERR_INVALID_ARG, "invalid contact relation arguments");
     sphx_relation r = new sphx_relation_s();
     r->ctx = body->ctx;
+    r->ctx->retain();
     r->inner = false;
     r->src = body;
     r->tgt = target;
@@ -227,9 +229,11 @@ extern "C" int sphx_relation_destroy(sphx_relation r)
 {
     if (!r)
         return SPHX_OK;
-    cudaStreamSynchronize(r->ctx->stream);
+    sphx_ctx ctx = r->ctx;
+    cudaStreamSynchronize(ctx->stream);
     r->release();
     delete r;
+    release(ctx);
     return SPHX_OK;
 }
 

@@ -136,10 +136,10 @@ extern "C" int sphx_ctx_create(int device, void *stream, sphx_ctx *out)
     return SPHX_OK;
 }
 
-extern "C" int sphx_ctx_destroy(sphx_ctx c)
+void sphx::release(sphx_ctx c)
 {
-    if (!c)
-        return SPHX_OK;
+    if (--c->refs > 0)
+        return;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     if (c->d_red)
@@ -151,6 +151,12 @@ extern "C" int sphx_ctx_destroy(sphx_ctx c)
     if (c->own_stream)
         cudaStreamDestroy(c->stream);
     delete c;
+}
+
+extern "C" int sphx_ctx_destroy(sphx_ctx c)
+{
+    if (c)
+        release(c);
     return SPHX_OK;
 }
 
@@ -186,6 +192,7 @@ extern "C" int sphx_body_create(sphx_ctx ctx, int dim, size_t n, sphx_body *out)
         return fail(SPHX_ERR_INVALID_ARG, "body size %zu exceeds 32-bit particle indices", n);
     sphx_body b = new sphx_body_s();
     b->ctx = ctx;
+    ctx->retain();
     b->dim = dim;
     b->n = n;
     *out = b;
@@ -196,10 +203,12 @@ extern "C" int sphx_body_destroy(sphx_body b)
 {
     if (!b)
         return SPHX_OK;
-    cudaStreamSynchronize(b->ctx->stream);
+    sphx_ctx ctx = b->ctx;
+    cudaStreamSynchronize(ctx->stream);
     for (auto &kv : b->fields)
         cudaFree(kv.second.dev);
     delete b;
+    release(ctx);
     return SPHX_OK;
 }
 

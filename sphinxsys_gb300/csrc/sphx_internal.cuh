@@ -88,7 +88,15 @@ struct sphx_ctx_s
     void *d_scratch = nullptr;
     size_t scratch_bytes = 0;
     int ensure_scratch(size_t bytes);
+    // Bodies, cell lists and relations hold a reference: sphx_ctx_destroy only frees the
+    // context once every object created on it has been destroyed, whatever the order.
+    int refs = 1;
+    void retain() { ++refs; }
 };
+namespace sphx
+{
+void release(sphx_ctx ctx);
+}
 
 struct sphx_body_s
 {

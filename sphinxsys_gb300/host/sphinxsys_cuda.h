@@ -1,0 +1,686 @@
+// sphinxsys_cuda.h -- C++ host layer over the sphx C ABI: the call-site API of SPHinXsys'
+// classic weakly-compressible fluid step, with every dynamics object executing on the
+// GB300 through libsphx_cuda.so (execution::CudaDevicePolicy).
+//
+// A driver written against the reference (tests/2d_examples/test_2d_dambreak/Dambreak.cpp)
+// compiles against this header with the same object names, constructor arguments and
+// exec() calls for the hot path: SPHSystem, FluidBody / SolidBody / ObserverBody,
+// GeometricShapeBox / ComplexShape, InnerRelation / ContactRelation / ComplexRelation,
+// Dynamics1Level<fluid_dynamics::Integration1stHalfWithWallRiemann>,
+// Dynamics1Level<fluid_dynamics::Integration2ndHalfWithWallRiemann>,
+// InteractionWithUpdate<fluid_dynamics::DensitySummationComplexFreeSurface>,
+// ReduceDynamics<fluid_dynamics::AdvectionTimeStep / AcousticTimeStep>,
+// SimpleDynamics<GravityForce<Gravity>>, SimpleDynamics<NormalDirectionFromBodyShape>,
+// ParticleSorting.  Output classes (VTP, restart, regression databases) are not part of
+// this layer; ObservedQuantity / TotalMechanicalEnergy return their values instead.
+//
+// Errors: a failing C-ABI call throws SPH::SphxException carrying the status and the
+// library message (the reference prints and calls exit(1)).
+//
+// Dimension: define SPHX_DIMENSION 2 or 3 before including (default 2), as the
+// reference builds its 2D and 3D libraries separately.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <initializer_list>
+#include <limits>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "../../include/sphx/sphx.h"
+
+#ifndef SPHX_DIMENSION
+#define SPHX_DIMENSION 2
+#endif
+
+namespace SPH
+{
+using Real = double;
+constexpr int Dimensions = SPHX_DIMENSION;
+constexpr Real Pi = Real(M_PI);
+
+struct Vecd
+{
+    Real v[3] = {0, 0, 0};
+    Vecd() = default;
+    Vecd(Real x, Real y) : v{x, y, 0} {}
+    Vecd(Real x, Real y, Real z) : v{x, y, z} {}
+    Real &operator[](int i) { return v[i]; }
+    const Real &operator[](int i) const { return v[i]; }
+    static Vecd Zero() { return Vecd(); }
+    static Vecd Ones() { return Dimensions == 2 ? Vecd(1, 1) : Vecd(1, 1, 1); }
+};
+inline Vecd operator+(const Vecd &a, const Vecd &b)
+{
+    Vecd r;
+    for (int d = 0; d < 3; ++d)
+        r[d] = a[d] + b[d];
+    return r;
+}
+inline Vecd operator-(const Vecd &a, const Vecd &b)
+{
+    Vecd r;
+    for (int d = 0; d < 3; ++d)
+        r[d] = a[d] - b[d];
+    return r;
+}
+inline Vecd operator*(Real s, const Vecd &a)
+{
+    Vecd r;
+    for (int d = 0; d < 3; ++d)
+        r[d] = s * a[d];
+    return r;
+}
+using Vec2d = Vecd;
+using Vec3d = Vecd;
+template <typename T>
+using StdVec = std::vector<T>;
+
+class SphxException : public std::runtime_error
+{
+  public:
+    int status;
+    SphxException(int s, const std::string &m) : std::runtime_error(m), status(s) {}
+};
+
+inline void check(int status)
+{
+    if (status != SPHX_OK)
+        throw SphxException(status, std::string("sphx: ") + sphx_last_error());
+}
+
+namespace execution
+{
+struct CudaDevicePolicy
+{
+};
+} // namespace execution
+using MainExecutionPolicy = execution::CudaDevicePolicy;
+
+struct BoundingBoxd
+{
+    Vecd lower_, upper_;
+    BoundingBoxd(const Vecd &lo, const Vecd &up) : lower_(lo), upper_(up) {}
+};
+
+struct Transform
+{
+    Vecd translation;
+    explicit Transform(const Vecd &t) : translation(t) {}
+};
+
+// ------------------------------------------------------------------ shapes
+// GeometricShapeBox (geometric_shape.cpp:6-18, geometric_element.cpp:19-55, .h:43-55)
+class Shape
+{
+  public:
+    std::string name_;
+    explicit Shape(const std::string &name) : name_(name) {}
+    virtual ~Shape() = default;
+    virtual bool checkContain(const Vecd &x) const = 0;
+    virtual Vecd findClosestPoint(const Vecd &x) const = 0;
+    Vecd findNormalDirection(const Vecd &x) const // base_geometry.cpp:45-58
+    {
+        bool in = checkContain(x);
+        Vecd d = findClosestPoint(x) - x;
+        Real s = d[0] * d[0] + d[1] * d[1];
+        if (Dimensions == 3)
+            s = s + d[2] * d[2];
+        Real n = std::sqrt(s);
+        Vecd out;
+        for (int a = 0; a < Dimensions; ++a)
+            out[a] = (in ? 1.0 : -1.0) * (d[a] / n);
+        return out;
+    }
+};
+
+class GeometricShapeBox : public Shape
+{
+  public:
+    Vecd c_, hs_;
+    GeometricShapeBox(const Transform &t, const Vecd &halfsize, const std::string &name = "GeometricShapeBox")
+        : Shape(name), c_(t.translation), hs_(halfsize) {}
+    bool checkContain(const Vecd &x) const override
+    {
+        for (int a = 0; a < Dimensions; ++a)
+            if (std::abs(x[a] - c_[a]) > hs_[a])
+                return false;
+        return true;
+    }
+    Vecd findClosestPoint(const Vecd &x) const override
+    {
+        Vecd p;
+        bool inside = true;
+        for (int a = 0; a < Dimensions; ++a)
+        {
+            p[a] = x[a] - c_[a];
+            if (p[a] < -hs_[a])
+            {
+                p[a] = -hs_[a];
+                inside = false;
+            }
+            else if (p[a] > hs_[a])
+            {
+                p[a] = hs_[a];
+                inside = false;
+            }
+        }
+        if (inside)
+        {
+            int which = 0;
+            Real mind = hs_[0] - std::abs(p[0]);
+            for (int a = 1; a < Dimensions; ++a)
+            {
+                Real d = hs_[a] - std::abs(p[a]);
+                if (d < mind)
+                {
+                    which = a;
+                    mind = d;
+                }
+            }
+            p[which] = p[which] < 0 ? -hs_[which] : hs_[which];
+        }
+        Vecd out;
+        for (int a = 0; a < Dimensions; ++a)
+            out[a] = p[a] + c_[a];
+        return out;
+    }
+};
+
+// ComplexShape with add/subtract (BinaryShapes, base_geometry.cpp:84-137)
+class ComplexShape : public Shape
+{
+    std::vector<std::pair<std::shared_ptr<Shape>, bool>> parts_;
+
+  public:
+    explicit ComplexShape(const std::string &name) : Shape(name) {}
+    template <class S, typename... Args>
+    void add(Args &&...args) { parts_.emplace_back(std::make_shared<S>(std::forward<Args>(args)...), true); }
+    template <class S, typename... Args>
+    void subtract(Args &&...args) { parts_.emplace_back(std::make_shared<S>(std::forward<Args>(args)...), false); }
+    bool checkContain(const Vecd &x) const override
+    {
+        bool exist = false;
+        for (auto &p : parts_)
+        {
+            bool inside = p.first->checkContain(x);
+            exist = p.second ? (exist || inside) : (exist && !inside);
+        }
+        return exist;
+    }
+    Vecd findClosestPoint(const Vecd &x) const override
+    {
+        Real dmin = std::numeric_limits<Real>::max();
+        Vecd best;
+        for (auto &p : parts_)
+        {
+            Vecd q = p.first->findClosestPoint(x);
+            Vecd d = x - q;
+            Real s = d[0] * d[0] + d[1] * d[1];
+            if (Dimensions == 3)
+                s = s + d[2] * d[2];
+            Real dist = std::sqrt(s);
+            if (dist <= dmin)
+            {
+                dmin = dist;
+                best = q;
+            }
+        }
+        return best;
+    }
+};
+
+template <class T, typename... Args>
+std::shared_ptr<T> makeShared(Args &&...args) { return std::make_shared<T>(std::forward<Args>(args)...); }
+
+// ------------------------------------------------------------------ materials
+class WeaklyCompressibleFluid
+{
+  public:
+    Real rho0_, c0_;
+    WeaklyCompressibleFluid(Real rho0, Real c0) : rho0_(rho0), c0_(c0) {}
+    Real ReferenceDensity() const { return rho0_; }
+};
+class Solid
+{
+  public:
+    Real rho0_;
+    explicit Solid(Real rho0 = 1.0) : rho0_(rho0) {}
+    Real ReferenceDensity() const { return rho0_; }
+};
+struct BaseParticles
+{
+};
+struct ObserverParticles
+{
+};
+struct Lattice
+{
+};
+
+class Gravity
+{
+  public:
+    Vecd g_, reference_;
+    explicit Gravity(const Vecd &g, const Vecd &reference = Vecd()) : g_(g), reference_(reference) {}
+};
+
+// ------------------------------------------------------------------ system and bodies
+class SPHBody;
+
+class SPHSystem
+{
+  public:
+    BoundingBoxd bounds_;
+    Real resolution_;
+    Real physical_time_ = 0;
+    sphx_ctx ctx_ = nullptr;
+    std::vector<SPHBody *> bodies_;
+    SPHSystem(const BoundingBoxd &bounds, Real resolution, int device = 0) : bounds_(bounds), resolution_(resolution)
+    {
+        check(sphx_ctx_create(device, nullptr, &ctx_));
+    }
+    ~SPHSystem() { sphx_ctx_destroy(ctx_); }
+    SPHSystem(const SPHSystem &) = delete;
+    SPHSystem &operator=(const SPHSystem &) = delete;
+    void handleCommandlineOptions(int, char *[]) {}
+    inline void initializeSystemCellLinkedLists();
+    inline void initializeSystemConfigurations();
+    template <typename T>
+    T *getSystemVariableDataByName(const std::string &name)
+    {
+        static_assert(std::is_same<T, Real>::value, "PhysicalTime is a Real");
+        if (name != "PhysicalTime")
+            throw SphxException(SPHX_ERR_NOT_FOUND, "unknown system variable " + name);
+        return &physical_time_;
+    }
+    int RestartStep() const { return 0; }
+    bool GenerateRegressionData() const { return false; }
+};
+
+class SPHBody
+{
+  public:
+    SPHSystem &system_;
+    std::shared_ptr<Shape> shape_;
+    std::string name_;
+    Real h_, rho0_ = 1.0, c0_ = 0.0;
+    bool is_fluid_ = false;
+    sphx_body body_ = nullptr;
+    size_t n_ = 0;
+    std::vector<class BaseRelation *> relations_;
+
+    SPHBody(SPHSystem &sys, std::shared_ptr<Shape> shape, const std::string &name)
+        : system_(sys), shape_(std::move(shape)), name_(name), h_(1.3 * sys.resolution_)
+    {
+        sys.bodies_.push_back(this);
+    }
+    SPHBody(SPHSystem &sys, Shape &shape) : SPHBody(sys, std::shared_ptr<Shape>(&shape, [](Shape *) {}), shape.name_) {}
+    SPHBody(SPHSystem &sys, std::shared_ptr<Shape> shape) : SPHBody(sys, shape, shape->name_) {}
+    SPHBody(SPHSystem &sys, const std::string &name) : SPHBody(sys, nullptr, name) {}
+    virtual ~SPHBody() { sphx_body_destroy(body_); }
+    SPHBody(const SPHBody &) = delete;
+
+    template <class Material, typename... Args>
+    void defineMatterMaterial(Args &&...args)
+    {
+        Material m(std::forward<Args>(args)...);
+        rho0_ = m.ReferenceDensity();
+        if constexpr (std::is_same<Material, WeaklyCompressibleFluid>::value)
+        {
+            c0_ = m.c0_;
+            is_fluid_ = true;
+        }
+    }
+    Real CutOffRadius() const { return 2.0 * h_; }
+    size_t TotalRealParticles() const { return n_; }
+
+    // ParticleGenerator<BaseParticles, Lattice> (particle_generator_lattice_{2d,3d}.cpp:12-23)
+    template <class ParticlesType, class Generator = Lattice>
+    void generateParticles()
+    {
+        static_assert(std::is_same<Generator, Lattice>::value, "lattice generation only");
+        const Vecd &lo = system_.bounds_.lower_, &up = system_.bounds_.upper_;
+        Real dp = system_.resolution_;
+        int n[3] = {1, 1, 1};
+        for (int a = 0; a < Dimensions; ++a)
+            n[a] = int(std::ceil((up[a] + 0.0 - lo[a]) / dp));
+        std::vector<Vecd> pos;
+        for (int i = 0; i < n[0]; ++i)
+            for (int j = 0; j < n[1]; ++j)
+                for (int k = 0; k < n[2]; ++k)
+                {
+                    int c[3] = {i, j, k};
+                    Vecd x;
+                    for (int a = 0; a < Dimensions; ++a)
+                        x[a] = (lo[a] + Real(c[a]) * dp) + 0.5 * dp;
+                    if (shape_->checkContain(x))
+                        pos.push_back(x);
+                }
+        Real vol = Dimensions == 3 ? dp * dp * dp : dp * dp;
+        createParticles(pos, vol);
+    }
+    // generateParticles<ObserverParticles>(positions)
+    template <class ParticlesType>
+    void generateParticles(const StdVec<Vecd> &positions) { createParticles(positions, 0.0); }
+
+    void createParticles(const std::vector<Vecd> &pos, Real vol)
+    {
+        n_ = pos.size();
+        check(sphx_body_create(system_.ctx_, Dimensions, n_, &body_));
+        std::vector<double> x(n_ * Dimensions);
+        for (size_t i = 0; i < n_; ++i)
+            for (int a = 0; a < Dimensions; ++a)
+                x[i * Dimensions + a] = pos[i][a];
+        upload("Position", x, Dimensions);
+        std::vector<uint32_t> ids(n_);
+        for (size_t i = 0; i < n_; ++i)
+            ids[i] = uint32_t(i);
+        check(sphx_body_upload(body_, "OriginalID", SPHX_U32, 1, ids.data(), n_));
+        check(sphx_body_upload(body_, "SortedID", SPHX_U32, 1, ids.data(), n_));
+        if (vol > 0)
+        {
+            upload("VolumetricMeasure", std::vector<double>(n_, vol), 1);
+            upload("Density", std::vector<double>(n_, rho0_), 1);
+            upload("Mass", std::vector<double>(n_, rho0_ * vol), 1); // base_material.cpp:37-40
+        }
+        positions_ = pos;
+    }
+    void upload(const char *name, const std::vector<double> &v, int ncomp)
+    {
+        check(sphx_body_upload(body_, name, SPHX_F64, ncomp, v.data(), n_));
+    }
+    // prepareForOutput: device -> host copy of a variable (AoS, n x ncomp)
+    std::vector<double> download(const char *name) const
+    {
+        void *p;
+        sphx_dtype dt;
+        int nc;
+        check(sphx_body_device_ptr(body_, name, &p, &dt, &nc));
+        std::vector<double> out(n_ * nc);
+        check(sphx_body_download(body_, name, out.data(), n_));
+        return out;
+    }
+    std::vector<Vecd> positions_; // generated positions (host copy used for shape normals)
+};
+
+class RealBody : public SPHBody
+{
+  public:
+    sphx_mesh_desc mesh_{};
+    sphx_cell_list cell_list_ = nullptr;
+    template <typename... Args>
+    RealBody(Args &&...args) : SPHBody(std::forward<Args>(args)...)
+    {
+        double lo[3] = {0, 0, 0}, up[3] = {0, 0, 0};
+        for (int a = 0; a < Dimensions; ++a)
+        {
+            lo[a] = system_.bounds_.lower_[a];
+            up[a] = system_.bounds_.upper_[a];
+        }
+        // SPHAdaptation::createCellLinkedList: grid spacing = cut-off radius, buffer 2
+        check(sphx_mesh_from_bounds(Dimensions, lo, up, CutOffRadius(), 2, &mesh_));
+    }
+    ~RealBody() override { sphx_cell_list_destroy(cell_list_); }
+    sphx_cell_list cellLinkedList()
+    {
+        if (!cell_list_)
+            check(sphx_cell_list_create(system_.ctx_, &mesh_, n_ ? n_ : 1, &cell_list_));
+        return cell_list_;
+    }
+    // RealBody::updateCellLinkedList (base_body.cpp:103-113)
+    void updateCellLinkedList() { check(sphx_cell_list_update(cellLinkedList(), body_)); }
+};
+
+class FluidBody : public RealBody
+{
+  public:
+    using RealBody::RealBody;
+};
+class SolidBody : public RealBody
+{
+  public:
+    using RealBody::RealBody;
+};
+class ObserverBody : public SPHBody
+{
+  public:
+    ObserverBody(SPHSystem &sys, const std::string &name) : SPHBody(sys, name) {}
+};
+
+// ------------------------------------------------------------------ relations
+class BaseRelation
+{
+  public:
+    sphx_relation rel_ = nullptr;
+    SPHBody &body_;
+    explicit BaseRelation(SPHBody &b) : body_(b) { b.relations_.push_back(this); }
+    virtual ~BaseRelation() { sphx_relation_destroy(rel_); }
+    BaseRelation(const BaseRelation &) = delete;
+    SPHBody &getSPHBody() { return body_; }
+    virtual void updateConfiguration() { check(sphx_relation_update(rel_)); }
+};
+
+class InnerRelation : public BaseRelation
+{
+  public:
+    explicit InnerRelation(RealBody &b) : BaseRelation(b)
+    {
+        check(sphx_inner_relation_create(b.body_, b.cellLinkedList(), b.h_, &rel_));
+    }
+};
+
+class ContactRelation : public BaseRelation
+{
+  public:
+    RealBody *target_;
+    ContactRelation(SPHBody &b, std::initializer_list<RealBody *> targets) : BaseRelation(b), target_(*targets.begin())
+    {
+        if (targets.size() != 1)
+            throw SphxException(SPHX_ERR_INVALID_ARG, "one contact body per relation");
+        Real h = std::max(b.h_, target_->h_); // NeighborBuilder::chooseKernel
+        int depth = 1 + int(std::floor(b.CutOffRadius() * (1.0 / target_->mesh_.grid_spacing)));
+        check(sphx_contact_relation_create(b.body_, target_->body_, target_->cellLinkedList(), h, depth,
+                                           target_->rho0_, &rel_));
+    }
+};
+
+class ComplexRelation
+{
+  public:
+    InnerRelation &inner_;
+    ContactRelation &contact_;
+    ComplexRelation(InnerRelation &inner, ContactRelation &contact) : inner_(inner), contact_(contact) {}
+    void updateConfiguration()
+    {
+        inner_.updateConfiguration();
+        contact_.updateConfiguration();
+    }
+};
+
+inline void SPHSystem::initializeSystemCellLinkedLists()
+{
+    for (SPHBody *b : bodies_)
+        if (auto *rb = dynamic_cast<RealBody *>(b))
+            rb->updateCellLinkedList();
+}
+inline void SPHSystem::initializeSystemConfigurations()
+{
+    for (SPHBody *b : bodies_)
+        for (BaseRelation *r : b->relations_)
+            r->updateConfiguration();
+}
+
+// ------------------------------------------------------------------ dynamics
+namespace fluid_dynamics
+{
+struct Integration1stHalfWithWallRiemann
+{
+};
+struct Integration2ndHalfWithWallRiemann
+{
+};
+struct DensitySummationComplexFreeSurface
+{
+};
+struct AcousticTimeStep
+{
+};
+struct AdvectionTimeStep
+{
+};
+} // namespace fluid_dynamics
+template <class GravityType>
+struct GravityForce
+{
+};
+struct NormalDirectionFromBodyShape
+{
+};
+
+inline sphx_fluid_params fluidParams(SPHBody &b, Real U_ref = 0.0)
+{
+    sphx_fluid_params p{};
+    p.rho0 = b.rho0_;
+    p.c0 = b.c0_;
+    p.h = b.h_;
+    check(sphx_lattice_number_density(Dimensions, b.h_, b.system_.resolution_, &p.sigma0));
+    p.limiter_slope = 3.0;
+    p.acoustic_cfl = 0.6;
+    p.advection_cfl = 0.25;
+    p.U_ref = U_ref;
+    return p;
+}
+
+template <class LocalDynamicsType, class ExecutionPolicy = execution::CudaDevicePolicy>
+class Dynamics1Level
+{
+    static_assert(std::is_same<ExecutionPolicy, execution::CudaDevicePolicy>::value, "CUDA policy only");
+    InnerRelation &inner_;
+    ContactRelation &contact_;
+    sphx_fluid_params p_;
+
+  public:
+    Dynamics1Level(InnerRelation &inner, ContactRelation &contact)
+        : inner_(inner), contact_(contact), p_(fluidParams(inner.getSPHBody())) {}
+    void exec(Real dt = 0.0)
+    {
+        if constexpr (std::is_same<LocalDynamicsType, fluid_dynamics::Integration1stHalfWithWallRiemann>::value)
+            check(sphx_integration_1st_half_with_wall_riemann(inner_.rel_, contact_.rel_, &p_, dt));
+        else
+        {
+            static_assert(std::is_same<LocalDynamicsType, fluid_dynamics::Integration2ndHalfWithWallRiemann>::value,
+                          "unsupported Dynamics1Level type");
+            check(sphx_integration_2nd_half_with_wall_riemann(inner_.rel_, contact_.rel_, &p_, dt));
+        }
+    }
+};
+
+template <class LocalDynamicsType, class ExecutionPolicy = execution::CudaDevicePolicy>
+class InteractionWithUpdate
+{
+    static_assert(std::is_same<LocalDynamicsType, fluid_dynamics::DensitySummationComplexFreeSurface>::value,
+                  "unsupported interaction");
+    InnerRelation &inner_;
+    ContactRelation &contact_;
+    sphx_fluid_params p_;
+
+  public:
+    InteractionWithUpdate(InnerRelation &inner, ContactRelation &contact)
+        : inner_(inner), contact_(contact), p_(fluidParams(inner.getSPHBody())) {}
+    void exec(Real = 0.0) { check(sphx_density_summation_complex_free_surface(inner_.rel_, contact_.rel_, &p_)); }
+};
+
+template <class LocalDynamicsType, class ExecutionPolicy = execution::CudaDevicePolicy>
+class ReduceDynamics
+{
+    SPHBody &body_;
+    sphx_fluid_params p_;
+
+  public:
+    explicit ReduceDynamics(SPHBody &body, Real U_ref = 0.0) : body_(body), p_(fluidParams(body, U_ref)) {}
+    Real exec(Real = 0.0)
+    {
+        Real dt;
+        if constexpr (std::is_same<LocalDynamicsType, fluid_dynamics::AcousticTimeStep>::value)
+            check(sphx_acoustic_time_step(body_.body_, &p_, &dt));
+        else
+            check(sphx_advection_time_step(body_.body_, &p_, &dt));
+        return dt;
+    }
+};
+
+template <class LocalDynamicsType, class ExecutionPolicy = execution::CudaDevicePolicy>
+class SimpleDynamics
+{
+    SPHBody &body_;
+    Vecd g_;
+
+  public:
+    explicit SimpleDynamics(SPHBody &body) : body_(body) {}
+    SimpleDynamics(SPHBody &body, const Gravity &g) : body_(body), g_(g.g_) {}
+    void exec(Real = 0.0)
+    {
+        if constexpr (std::is_same<LocalDynamicsType, NormalDirectionFromBodyShape>::value)
+        {
+            std::vector<double> n(body_.n_ * Dimensions);
+            for (size_t i = 0; i < body_.n_; ++i)
+            {
+                Vecd d = body_.shape_->findNormalDirection(body_.positions_[i]);
+                for (int a = 0; a < Dimensions; ++a)
+                    n[i * Dimensions + a] = d[a];
+            }
+            body_.upload("NormalDirection", n, Dimensions);
+        }
+        else
+            check(sphx_gravity_force(body_.body_, g_.v));
+    }
+};
+
+class ParticleSorting
+{
+    RealBody &body_;
+
+  public:
+    explicit ParticleSorting(RealBody &body) : body_(body) {}
+    void exec(Real = 0.0) { check(sphx_particle_sorting(body_.body_, &body_.mesh_)); }
+};
+
+// ObservingAQuantity<Real> over an observer contact relation.
+class ObservedQuantity
+{
+    ContactRelation &contact_;
+    std::string name_;
+
+  public:
+    ObservedQuantity(const std::string &name, ContactRelation &contact) : contact_(contact), name_(name) {}
+    std::vector<Real> exec()
+    {
+        std::vector<Real> out(contact_.getSPHBody().n_);
+        if (!out.empty())
+            check(sphx_observe_quantity(contact_.rel_, name_.c_str(), out.data()));
+        return out;
+    }
+};
+
+class TotalMechanicalEnergy
+{
+    SPHBody &body_;
+    Gravity g_;
+
+  public:
+    TotalMechanicalEnergy(SPHBody &body, const Gravity &g) : body_(body), g_(g) {}
+    Real exec()
+    {
+        Real e;
+        check(sphx_total_mechanical_energy(body_.body_, g_.g_.v, &e));
+        return e;
+    }
+};
+} // namespace SPH

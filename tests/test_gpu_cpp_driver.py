@@ -1,0 +1,51 @@
+"""The C++ host layer: examples/dambreak_2d.cpp (the reference driver's call sites on the
+CUDA policy) compiles against sphinxsys_cuda.h and agrees with the oracle."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from sphinxsys_gb300 import build, cases
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def compile_example(tmp_path):
+    lib = build.build()
+    exe = str(tmp_path / "dambreak_2d")
+    cmd = ["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "sphinxsys_gb300", "host"),
+           os.path.join(ROOT, "examples", "dambreak_2d.cpp"), "-o", exe, "-L", os.path.dirname(lib), "-lsphx_cuda",
+           f"-Wl,-rpath,{os.path.dirname(lib)}"]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return exe
+
+
+def test_example_compiles(tmp_path):
+    assert os.path.exists(compile_example(tmp_path))
+
+
+@pytest.mark.gpu
+def test_cpp_driver_matches_oracle(tmp_path):
+    exe = compile_example(tmp_path)
+    iters = 201
+    out = subprocess.run([exe, "20", str(iters)], check=True, capture_output=True, text=True).stdout.split("\n")
+    rows = [ln.split() for ln in out if ln.startswith(("observe", "final"))]
+    oc = O.OracleCase(cases.dambreak_2d())
+    expect = [(0, 0.0, oc.observe_pressure()[0], oc.total_mechanical_energy())]
+    for it in range(iters):
+        observe = it % 200 == 0 and it != 0
+        _, _, obs, en = oc.advection_step(observe=observe)
+        if observe:
+            expect.append((it, oc.physical_time.value, obs[0], en))
+    obs_rows = [r for r in rows if r[0] == "observe"]
+    assert len(obs_rows) == len(expect)
+    for r, e in zip(obs_rows, expect):
+        assert int(r[1]) == e[0]
+        assert abs(float(r[2]) - e[1]) <= 1e-12 * max(1.0, e[1])
+        assert abs(float(r[3]) - e[2]) <= 1e-8 * max(1.0, abs(e[2]))
+        assert abs(float(r[4]) - e[3]) <= 1e-10 * abs(e[3])
+    final = [r for r in rows if r[0] == "final"][0]
+    assert int(final[1]) == iters
+    assert abs(float(final[4]) / oc.total_mechanical_energy() - 1) < 1e-10
