@@ -92,6 +92,96 @@ def algorithmic_bytes_2nd_half(n_fluid: int, n_wall_active: int, nnz: int) -> in
     return 136 * n_fluid + 80 * n_wall_active + 4 * nnz
 
 
+def algorithmic_bytes_mp_second(n_fluid: int, n_wall_active: int, nnz: int) -> int:
+    """Mixed-precision 2nd half, 3D: per fluid particle read cell+off0 (16), vel (12),
+    off (12), drho (4), drho_dt (4) and write off (12), drho (4), drho_dt (4), force (12)
+    = 80 B; per active wall particle cell+off (16) and normal (12) = 28 B; 4 B per stored
+    neighbour index."""
+    return 80 * n_fluid + 28 * n_wall_active + 4 * nnz
+
+
+def mixed_precision_leg(args, torch, local):
+    """FP64 and mixed precision on the same case (default dp = 0.006, 3,340,000 fluid
+    particles) from the same initial state: particle-steps/s of both, the sweep-kernel
+    roofline of the mixed solver, and the field / probe errors of mixed against FP64."""
+    from sphinxsys_gb300 import cases
+    from sphinxsys_gb300.dambreak import MixedPrecisionDamBreak
+    case = cases.dambreak_3d(args.mp_dp)
+    mp = MixedPrecisionDamBreak(case, device=local)
+    ref = mp.fp64  # the FP64 set-up doubles as the FP64 reference run
+    n = ref.water_block.n
+    ext = torch.cuda.ExternalStream(mp.ctx.stream())
+    steps, warm = args.mp_steps, args.warmup
+
+    def timed(step_fn):
+        for _ in range(warm):
+            step_fn()
+        mp.ctx.synchronize()
+        with torch.cuda.stream(ext):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+        subs = 0
+        for _ in range(steps):
+            subs += step_fn()[0]
+        with torch.cuda.stream(ext):
+            b.record()
+        mp.ctx.synchronize()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3, subs
+
+    mp.set_profiling(True)
+    l0 = mp.ctx.launch_count()
+    mp_el, mp_subs = timed(mp.advection_step)
+    mp_launches = mp.ctx.launch_count() - l0
+    t1, t2, nsweeps = mp.kernel_times()
+    sizes = mp.list_sizes()
+    mp.set_profiling(False)
+    fp_el, fp_subs = timed(lambda: ref.advection_step()[:2])
+    # errors of mixed against FP64 after the same advection steps from the same start
+    errs = {}
+    for name in ("Position", "Velocity", "Density", "Pressure"):
+        a = mp.fp64_view(name)
+        b = ref.water_block.download(name)
+        errs[name] = float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+    p_mp = mp.observe_pressure_view()
+    p_fp = ref.recorded_pressure.exec()
+    vert = case.vertical_axis
+    lo = [case.sys_lower[0], case.sys_lower[1], case.sys_lower[2]]
+    up = [case.sys_upper[0], case.sys_upper[1], case.sys_upper[2]]
+    lo[0], up[0] = case.inner_center[0] + case.inner_halfsize[0] - 0.2, case.inner_center[0] + case.inner_halfsize[0]
+    h_mp = mp.upper_front(vert, lo, up)
+    from sphinxsys_gb300 import sph as S
+    h_fp = S.UpperFrontInAxisDirection(ref.water_block, lo, up, vert).exec()
+    hbm = _hbm_peak()[0]
+    n_wall_active = int(np.unique(ref.water_wall_contact.neighbors()["j"]).size)
+    alg = algorithmic_bytes_mp_second(n, n_wall_active, sizes["nnz_inner"] + sizes["nnz_wall"])
+    achieved = alg / (t2 / 1e3) / 1e9
+    return {
+        "workload": case.name, "n_fluid": n, "steps": steps, "dtype": "f32 pairs + f64 integration",
+        "value": n * mp_subs / mp_el, "ms_per_step": 1e3 * mp_el / steps, "acoustic_substeps": mp_subs,
+        "fp64_value_same_case": n * fp_subs / fp_el, "fp64_ms_per_step": 1e3 * fp_el / steps,
+        "speedup_vs_fp64": (n * mp_subs / mp_el) / (n * fp_subs / fp_el), "gpu_launches": int(mp_launches),
+        "roofline": {"bound": "hbm", "kernel": "k_mp_second<3,true>", "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "algorithmic_bytes": alg, "kernel_ms": t2,
+                     "first_half_ms": t1, "sweeps_timed": nsweeps},
+        "errors_vs_fp64": {"fields_max_rel": errs, "probe_pressure": [float(x) for x in p_mp],
+                           "probe_pressure_fp64": [float(x) for x in p_fp],
+                           "free_surface_height": h_mp, "free_surface_height_fp64": h_fp,
+                           "free_surface_rel_err": abs(h_mp - h_fp) / abs(h_fp)},
+        "lists": sizes,
+    }
+
+
+def _hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+        return float(peaks["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
 def run_cpu_sample(case, threads: int):
     """One advection step of the oracle (OpenMP FP64 restatement) on the same case."""
     from oracle import oracle as O
@@ -144,6 +234,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mp-dp", type=float, default=0.006)
+    ap.add_argument("--mp-steps", type=int, default=5)
+    ap.add_argument("--no-mixed", action="store_true")
     args = ap.parse_args()
     rank, world, local = dist_info()
 
@@ -256,18 +349,12 @@ def main():
         e2e = {"value": n_fluid * esubs / e_el * world, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h)}
 
-    peaks = {}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-    except OSError:
-        pass
-    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    hbm, peak_source = _hbm_peak()
     alg = algorithmic_bytes_2nd_half(n_fluid, n_wall_active, nnz)
     achieved = alg / k_avg / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                 "traffic": None, "kernel": "k_interact_2nd<3>", "algorithmic_bytes": alg,
-                "kernel_ms": k_avg * 1e3, "peak_source": "measured" if peaks else "fallback"}
+                "kernel_ms": k_avg * 1e3, "peak_source": peak_source}
     prof = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(prof):
         try:
@@ -277,6 +364,11 @@ def main():
                 roofline["traffic"] = tr
         except (OSError, ValueError):
             pass
+
+    del sim
+    mixed = None
+    if not args.no_mixed:
+        mixed = mixed_precision_leg(args, torch, local)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -294,7 +386,7 @@ def main():
                        "precision": "fp64", "acoustic_substeps": subs, "l2": "inputs larger than L2",
                        "parallelism": f"replicas{world}"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-            "clocks": clocks,
+            "clocks": clocks, "mixed_precision": mixed,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -179,6 +179,57 @@ int sphx_total_mechanical_energy(sphx_body fluid, const double *gravity, double 
 int sphx_upper_front_in_axis_direction(sphx_body fluid, int axis, const double *region_lower,
                                        const double *region_upper, double *front);
 
+/* ------------------------------------------------------------------ mixed precision
+ * A fused solver for one fluid body against one static wall body (the dam-break
+ * configuration of Dambreak.cpp) in mixed precision; it has no single reference
+ * counterpart: it runs the same sequence as one pass of the Dambreak.cpp:166-220 loop
+ * (AdvectionTimeStep, DensitySummationComplexFreeSurface, the acoustic sub-steps of
+ * Integration1stHalf/2ndHalfWithWallRiemann, and the cell-list / configuration update).
+ *
+ * Precision: pair kernels, gradients, pressure and dissipation in FP32 with
+ * Kahan-compensated neighbour sums; positions as an FP32 offset from the lower corner of
+ * an integer cell; density held as the FP32 deviation rho - rho0; position integration,
+ * the time-step reductions and the conservation sums in FP64.  Particles are kept in
+ * cell order, re-sorted at every configuration update.
+ *
+ * Requirements checked at creation: uniform particle mass and volume in each body, a
+ * static wall (zero wall velocity and acceleration), gravity as the only prior force,
+ * at most 1024 cells per mesh axis. */
+typedef struct sphx_mp_s *sphx_mp;
+
+/* Builds the solver from the current FP64 state of the relations' bodies. */
+int sphx_mp_create(sphx_relation inner, sphx_relation wall_contact, const sphx_fluid_params *p,
+                   const double *gravity, sphx_mp *out);
+int sphx_mp_destroy(sphx_mp mp);
+/* One advection step.  loop_style 0: acoustic dt taken before each relaxation
+ * (Dambreak.cpp:181-190); 1: after it (test_3d_dambreak/dambreak.cpp:193-201).
+ * Outputs (any may be null): acoustic sub-steps taken, the advection dt used, and the
+ * physical time after the step. */
+int sphx_mp_advection_step(sphx_mp mp, int loop_style, int *substeps, double *advection_dt,
+                           double *physical_time);
+/* Writes Position, Velocity, Density, Pressure, Force and DensityChangeRate back into the
+ * FP64 fluid body, in the body's particle order (synchronises). */
+int sphx_mp_download(sphx_mp mp, sphx_body fluid);
+/* FP64 conservation sums: out[0] total mass, out[1..3] momentum, out[4] mechanical energy
+ * (kinetic + potential with gravity and zero reference at the origin). */
+int sphx_mp_conservation(sphx_mp mp, double *out);
+/* UpperFrontInAxisDirection of the fluid inside an axis-aligned box region. */
+int sphx_mp_upper_front(sphx_mp mp, int axis, const double *region_lower, const double *region_upper,
+                        double *front);
+/* Kernel launch shape and neighbour strategy: block size (64..1024, multiple of 32) of
+ * the sweep kernels, and 0 = stored neighbour index lists, 1 = cell sweep every
+ * sub-step. */
+int sphx_mp_set_tuning(sphx_mp mp, int block, int strategy);
+/* CUDA-event timing of the two sweep kernels of every sub-step (on the context's
+ * stream); switching it resets the totals. */
+int sphx_mp_set_profiling(sphx_mp mp, int on);
+/* out[0] total ms of the 1st-half sweeps, out[1] their count, out[2] / out[3] the same
+ * for the 2nd-half sweeps (synchronises). */
+int sphx_mp_kernel_times(sphx_mp mp, double *out);
+/* out[0] fluid particles, out[1] wall particles, out[2] stored inner pairs, out[3] stored
+ * wall pairs, out[4] / out[5] list capacities (synchronises). */
+int sphx_mp_list_sizes(sphx_mp mp, uint64_t *out);
+
 #ifdef __cplusplus
 }
 #endif

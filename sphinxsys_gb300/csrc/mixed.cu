@@ -1,0 +1,1343 @@
+// Mixed-precision fused dam-break solver (sphx_mp_*).
+//
+// Same step sequence as the classic FP64 path (Dambreak.cpp:166-220): advection dt,
+// DensitySummationComplexFreeSurface (density_summation.cpp:74-82,124-144),
+// Integration1stHalfWithWallRiemann / Integration2ndHalfWithWallRiemann
+// (fluid_integration.hpp:49-113,166-231), acoustic / advection time steps
+// (fluid_time_step.cpp:21-31,54-65) and the configuration update.
+//
+// Layout (cell order, re-sorted at every configuration update; SoA, FP32 unless noted):
+//   cell      uint32  packed integer cell coordinates (10 bits per axis)
+//   off       float3  current position minus the cell's lower corner
+//   off0      float3  the same at the last configuration update (kernel geometry)
+//   vel, force float3; drho = rho - rho0, drho_dt, p  float
+//   id        uint32  index of the particle in the FP64 body it came from
+// Pair arithmetic is FP32 with Kahan-compensated sums; the position half-steps, the
+// time-step reductions and the conservation sums are FP64.  Neighbour index lists
+// (ELL, slot-major) are rebuilt with the density summation at each configuration update;
+// the kernel geometry (W, dW, e) is recomputed per pair from off0, as the reference keeps
+// the configuration-time kernel values for the whole advection step.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "sphx_device.cuh"
+#include "sphx_internal.cuh"
+
+using namespace sphx;
+
+namespace
+{
+constexpr float kTinyF = 2.71051e-20f;
+
+struct Kahan
+{
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x)
+    {
+        float y = x - c;
+        float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ float value() const { return s - c; }
+};
+
+__host__ __device__ __forceinline__ uint32_t pack_cell(int cx, int cy, int cz)
+{
+    return uint32_t(cx) | (uint32_t(cy) << 10) | (uint32_t(cz) << 20);
+}
+__device__ __forceinline__ void unpack_cell(uint32_t p, int *c)
+{
+    c[0] = int(p & 1023u);
+    c[1] = int((p >> 10) & 1023u);
+    c[2] = int((p >> 20) & 1023u);
+}
+
+struct MPConst
+{
+    MeshDev m;
+    float gs_f;
+    // kernel
+    float rc_sqr, inv_h, fW, fdW;
+    // fluid
+    float rho0, p0_over_rho0, Vol, mass, inv_mass;
+    double sigma0;
+    float rho0_over_sigma0, wall_factor; // wall_factor = rho0^2 / (sigma0 m) * (m_w / rho0_w)
+    float wall_Vol;
+    // Riemann solver
+    float inv_z, zgeo, inv_c0, slope;
+    float g[3];
+    double gd[3];
+    // time steps
+    double h, c0, acoustic_cfl, advection_cfl, U_ref;
+};
+
+struct MPFluid
+{
+    uint32_t *cell;
+    float *off, *off0, *vel, *force, *drho, *drho_dt, *p;
+    uint32_t *id;
+};
+
+struct MPWall
+{
+    uint32_t *cell;
+    float *off, *n;
+    size_t nw;
+};
+
+struct MPLists
+{
+    uint32_t *count, *J;
+    unsigned cap;
+};
+
+// ---------------------------------------------------------------- geometry helpers
+template <int D>
+__device__ __forceinline__ void pair_dx(const MPConst &k, const int *ci, const float *oi, uint32_t cell_j,
+                                        const float *off_j, size_t stride, size_t j, float *dx)
+{
+    int cj[3];
+    unpack_cell(cell_j, cj);
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        dx[d] = float(ci[d] - cj[d]) * k.gs_f + (oi[d] - off_j[d * stride + j]);
+}
+
+template <int D>
+__device__ __forceinline__ float sq(const float *dx)
+{
+    float s = dx[0] * dx[0] + dx[1] * dx[1];
+    if (D == 3)
+        s += dx[2] * dx[2];
+    return s;
+}
+
+__device__ __forceinline__ float wendland_W(const MPConst &k, float r)
+{
+    float q = r * k.inv_h;
+    float t = 1.0f - 0.5f * q;
+    float t2 = t * t;
+    return k.fW * (t2 * t2 * (1.0f + 2.0f * q));
+}
+__device__ __forceinline__ float wendland_dW(const MPConst &k, float r)
+{
+    float q = r * k.inv_h;
+    float t = q - 2.0f;
+    return k.fdW * (0.625f * (t * t * t) * q);
+}
+
+__device__ __forceinline__ float p_jump(const MPConst &k, float u)
+{
+    return k.zgeo * u * fminf(k.slope * (k.inv_c0 * fmaxf(u, 0.0f)), 1.0f);
+}
+
+__device__ __forceinline__ void block_max_slot(unsigned long long *slot, double v)
+{
+    unsigned long long b = ordered_bits(v);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        unsigned long long y = __shfl_down_sync(0xffffffffu, b, o);
+        b = y > b ? y : b;
+    }
+    if ((threadIdx.x & 31u) == 0)
+        atomicMax(slot, b);
+}
+
+// Visits the candidate particles of the 3^D cells around cell c: along the last axis the
+// cells are consecutive in linear order, so each (x[, y]) column is one contiguous range.
+template <int D, class F>
+__device__ __forceinline__ void for_each_candidate(const MeshDev &m, const uint32_t *offset, const int *c, F &&f)
+{
+    int lo0 = max(c[0] - 1, 0), hi0 = min(c[0] + 1, m.all_cells[0] - 1);
+    if (D == 2)
+    {
+        int lo1 = max(c[1] - 1, 0), hi1 = min(c[1] + 1, m.all_cells[1] - 1);
+        for (int x = lo0; x <= hi0; ++x)
+        {
+            uint32_t a = uint32_t(x) * uint32_t(m.all_cells[1]);
+            uint32_t b = offset[a + uint32_t(lo1)], e = offset[a + uint32_t(hi1) + 1];
+            for (uint32_t j = b; j < e; ++j)
+                f(j);
+        }
+    }
+    else
+    {
+        int lo1 = max(c[1] - 1, 0), hi1 = min(c[1] + 1, m.all_cells[1] - 1);
+        int lo2 = max(c[2] - 1, 0), hi2 = min(c[2] + 1, m.all_cells[2] - 1);
+        for (int x = lo0; x <= hi0; ++x)
+            for (int y = lo1; y <= hi1; ++y)
+            {
+                uint32_t a = (uint32_t(x) * uint32_t(m.all_cells[1]) + uint32_t(y)) * uint32_t(m.all_cells[2]);
+                uint32_t b = offset[a + uint32_t(lo2)], e = offset[a + uint32_t(hi2) + 1];
+                for (uint32_t j = b; j < e; ++j)
+                    f(j);
+            }
+    }
+}
+
+// ---------------------------------------------------------------- (re)hash + sort
+// From FP64 body positions (creation).
+template <int D>
+__global__ void k_mp_from_fp64(size_t n, const double *__restrict__ pos, MeshDev m, uint32_t *__restrict__ ncell,
+                               float *__restrict__ noff, uint32_t *__restrict__ key, uint32_t *__restrict__ rank,
+                               uint32_t *__restrict__ count)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    double x[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        x[d] = pos[d * n + i];
+    int c[3] = {0, 0, 0};
+    cell_index<D>(m, x, c);
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        noff[d * n + i] = float(x[d] - cell_corner(m, d, c[d]));
+    ncell[i] = pack_cell(c[0], c[1], c[2]);
+    uint32_t lc = linear_cell<D>(m, c);
+    key[i] = lc;
+    rank[i] = atomicAdd(&count[lc], 1u);
+}
+
+// From the current (cell, offset) state: FP64 reconstruction of the position.
+template <int D>
+__global__ void k_mp_rehash(size_t n, const uint32_t *__restrict__ cell, const float *__restrict__ off, MeshDev m,
+                            uint32_t *__restrict__ ncell, float *__restrict__ noff, uint32_t *__restrict__ key,
+                            uint32_t *__restrict__ rank, uint32_t *__restrict__ count)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    int c0[3];
+    unpack_cell(cell[i], c0);
+    double x[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        x[d] = cell_corner(m, d, c0[d]) + double(off[d * n + i]);
+    int c[3] = {0, 0, 0};
+    cell_index<D>(m, x, c);
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        noff[d * n + i] = float(x[d] - cell_corner(m, d, c[d]));
+    ncell[i] = pack_cell(c[0], c[1], c[2]);
+    uint32_t lc = linear_cell<D>(m, c);
+    key[i] = lc;
+    rank[i] = atomicAdd(&count[lc], 1u);
+}
+
+__global__ void k_mp_scatter(size_t n, const uint32_t *__restrict__ key, const uint32_t *__restrict__ rank,
+                             const uint32_t *__restrict__ offset, uint32_t *__restrict__ perm)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n)
+        perm[offset[key[i]] + rank[i]] = uint32_t(i);
+}
+
+__global__ void k_mp_sort_segments(size_t nseg, const uint32_t *__restrict__ offset, uint32_t *__restrict__ idx)
+{
+    size_t c = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= nseg)
+        return;
+    uint32_t b = offset[c], e = offset[c + 1];
+    for (uint32_t k = b + 1; k < e; ++k)
+    {
+        uint32_t v = idx[k];
+        uint32_t q = k;
+        while (q > b && idx[q - 1] > v)
+        {
+            idx[q] = idx[q - 1];
+            --q;
+        }
+        idx[q] = v;
+    }
+}
+
+__global__ void k_mp_set_total(uint32_t *offset, size_t ncells, uint32_t total) { offset[ncells] = total; }
+
+// Gathers the state into the new cell order.
+template <int D>
+__global__ void k_mp_gather(size_t n, const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ncell,
+                            const float *__restrict__ noff, MPFluid src, MPFluid dst)
+{
+    size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= n)
+        return;
+    uint32_t i = perm[k];
+    dst.cell[k] = ncell[i];
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        float o = noff[d * n + i];
+        dst.off[d * n + k] = o;
+        dst.off0[d * n + k] = o;
+        dst.vel[d * n + k] = src.vel[d * n + i];
+        dst.force[d * n + k] = src.force[d * n + i];
+    }
+    dst.drho[k] = src.drho[i];
+    dst.drho_dt[k] = src.drho_dt[i];
+    dst.id[k] = src.id[i];
+}
+
+// ---------------------------------------------------------------- configuration + density
+template <int D>
+__global__ void __launch_bounds__(256)
+    k_mp_build(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
+               const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, unsigned int *max_counts)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    int ci[3] = {0, 0, 0};
+    unpack_cell(f.cell[i], ci);
+    float oi[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        oi[d] = f.off0[d * n + i];
+    Kahan sigma;
+    unsigned cnt = 0;
+    for_each_candidate<D>(k.m, f_offset, ci, [&](uint32_t j) {
+        if (j == uint32_t(i))
+            return;
+        float dx[3];
+        pair_dx<D>(k, ci, oi, f.cell[j], f.off0, n, j, dx);
+        float r2 = sq<D>(dx);
+        if (!(r2 < k.rc_sqr))
+            return;
+        if (cnt < in.cap)
+            in.J[size_t(cnt) * n + i] = j;
+        ++cnt;
+        sigma.add(wendland_W(k, sqrtf(r2)));
+    });
+    Kahan wsig;
+    unsigned wc = 0;
+    for_each_candidate<D>(k.m, w_offset, ci, [&](uint32_t j) {
+        float dx[3];
+        pair_dx<D>(k, ci, oi, w.cell[j], w.off, w.nw, j, dx);
+        float r2 = sq<D>(dx);
+        if (!(r2 < k.rc_sqr))
+            return;
+        if (wc < wl.cap)
+            wl.J[size_t(wc) * n + i] = j;
+        ++wc;
+        wsig.add(wendland_W(k, sqrtf(r2)));
+    });
+    in.count[i] = cnt;
+    wl.count[i] = wc;
+    atomicMax(&max_counts[0], cnt);
+    atomicMax(&max_counts[1], wc);
+    // rho_sum - rho0 = rho0 (W0 + sum W - sigma0) / sigma0 + wall term; FreeSurface: max(., 0)
+    double dsig = (double(sigma.s) - k.sigma0) - double(sigma.c) + double(k.fW);
+    float drho = float(dsig) * k.rho0_over_sigma0 + wsig.value() * k.wall_factor;
+    f.drho[i] = fmaxf(drho, 0.0f);
+}
+
+// ---------------------------------------------------------------- acoustic sub-step
+__global__ void k_mp_init1(size_t n, float *__restrict__ drho, const float *__restrict__ drho_dt,
+                           float *__restrict__ p, float p0_over_rho0, float half_dt)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    float r = drho[i] + drho_dt[i] * half_dt;
+    drho[i] = r;
+    p[i] = p0_over_rho0 * r;
+}
+
+template <int D, bool LISTS>
+__global__ void __launch_bounds__(256)
+    k_mp_first(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
+               const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, double dt,
+               unsigned long long *ac_slot)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    double vmax = -1.0e300;
+    if (i < n)
+    {
+        int ci[3] = {0, 0, 0};
+        unpack_cell(f.cell[i], ci);
+        float oi[3] = {0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            oi[d] = f.off0[d * n + i];
+        const float p_i = f.p[i];
+        const float rho_i = k.rho0 + f.drho[i];
+        Kahan force[3], rdis;
+        auto inner = [&](uint32_t j) {
+            float dx[3];
+            pair_dx<D>(k, ci, oi, f.cell[j], f.off0, n, j, dx);
+            float r2 = sq<D>(dx);
+            if (!LISTS && (!(r2 < k.rc_sqr) || j == uint32_t(i)))
+                return;
+            float r = sqrtf(r2);
+            float inv = 1.0f / (r + kTinyF);
+            float dWV = wendland_dW(k, r) * k.Vol;
+            float p_j = f.p[j];
+            float sc = (p_i + p_j) * dWV * inv;
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+                force[d].add(-sc * dx[d]);
+            rdis.add((p_i - p_j) * k.inv_z * dWV);
+        };
+        if (LISTS)
+        {
+            unsigned c = min(in.count[i], in.cap);
+            for (unsigned s = 0; s < c; ++s)
+                inner(in.J[size_t(s) * n + i]);
+        }
+        else
+            for_each_candidate<D>(k.m, f_offset, ci, inner);
+        Kahan wforce[3], wrdis;
+        auto wall = [&](uint32_t j) {
+            float dx[3];
+            pair_dx<D>(k, ci, oi, w.cell[j], w.off, w.nw, j, dx);
+            float r2 = sq<D>(dx);
+            if (!LISTS && !(r2 < k.rc_sqr))
+                return;
+            float r = sqrtf(r2);
+            float inv = 1.0f / (r + kTinyF);
+            float dWV = wendland_dW(k, r) * k.wall_Vol;
+            float face = 0.f; // (F_prior/m - a_wall) . (-e), static wall
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+                face -= k.g[d] * (dx[d] * inv);
+            float p_w = p_i + rho_i * r * fmaxf(0.0f, face);
+            float sc = (p_i + p_w) * dWV * inv;
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+                wforce[d].add(-sc * dx[d]);
+            wrdis.add((p_i - p_w) * k.inv_z * dWV);
+        };
+        if (LISTS)
+        {
+            unsigned c = min(wl.count[i], wl.cap);
+            for (unsigned s = 0; s < c; ++s)
+                wall(wl.J[size_t(s) * n + i]);
+        }
+        else
+            for_each_candidate<D>(k.m, w_offset, ci, wall);
+        f.drho_dt[i] = rdis.value() * rho_i + wrdis.value() * rho_i;
+        double v2 = 0;
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+        {
+            float F = f.force[d * n + i] + force[d].value() * k.Vol + wforce[d].value() * k.Vol;
+            f.force[d * n + i] = F;
+            float v = f.vel[d * n + i];
+            // position half-step in FP64 (initialization of the 1st half, old velocity)
+            f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(v));
+            double vn = double(v) + (k.gd[d] + double(F) * double(k.inv_mass)) * dt;
+            f.vel[d * n + i] = float(vn);
+            v2 += double(float(vn)) * double(float(vn));
+        }
+        vmax = k.c0 + sqrt(v2);
+    }
+    block_max_slot(ac_slot, vmax);
+}
+
+template <int D, bool LISTS>
+__global__ void __launch_bounds__(256)
+    k_mp_second(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
+                const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, double dt,
+                unsigned long long *adv_slot)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    double amax = -1.0e300;
+    if (i < n)
+    {
+        int ci[3] = {0, 0, 0};
+        unpack_cell(f.cell[i], ci);
+        float oi[3] = {0, 0, 0}, vi[3] = {0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+        {
+            oi[d] = f.off0[d * n + i];
+            vi[d] = f.vel[d * n + i];
+        }
+        const float rho_i = k.rho0 + f.drho[i];
+        Kahan rate, pdis[3];
+        auto inner = [&](uint32_t j) {
+            float dx[3];
+            pair_dx<D>(k, ci, oi, f.cell[j], f.off0, n, j, dx);
+            float r2 = sq<D>(dx);
+            if (!LISTS && (!(r2 < k.rc_sqr) || j == uint32_t(i)))
+                return;
+            float r = sqrtf(r2);
+            float inv = 1.0f / (r + kTinyF);
+            float dWV = wendland_dW(k, r) * k.Vol;
+            float u = 0.f;
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+                u += (vi[d] - f.vel[d * n + j]) * (dx[d] * inv);
+            rate.add(u * dWV);
+            float sc = p_jump(k, u) * dWV * inv;
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+                pdis[d].add(sc * dx[d]);
+        };
+        if (LISTS)
+        {
+            unsigned c = min(in.count[i], in.cap);
+            for (unsigned s = 0; s < c; ++s)
+                inner(in.J[size_t(s) * n + i]);
+        }
+        else
+            for_each_candidate<D>(k.m, f_offset, ci, inner);
+        Kahan wrate, wdis[3];
+        auto wall = [&](uint32_t j) {
+            float dx[3];
+            pair_dx<D>(k, ci, oi, w.cell[j], w.off, w.nw, j, dx);
+            float r2 = sq<D>(dx);
+            if (!LISTS && !(r2 < k.rc_sqr))
+                return;
+            float r = sqrtf(r2);
+            float inv = 1.0f / (r + kTinyF);
+            float dWV = wendland_dW(k, r) * k.wall_Vol;
+            float en = 0.f, ve = 0.f, vn = 0.f, nj[3];
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+            {
+                nj[d] = w.n[d * w.nw + j];
+                float e = dx[d] * inv;
+                en += e * nj[d];
+                ve += vi[d] * e;
+            }
+            float sgn = en < 0.f ? -1.f : (en > 0.f ? 1.f : 0.f);
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+                vn += vi[d] * (sgn * nj[d]);
+            wrate.add(2.0f * ve * dWV); // (v_i - (2 v_wall - v_i)) . e with a static wall
+            float sc = p_jump(k, 2.0f * vn) * dWV;
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+                wdis[d].add(sc * (sgn * nj[d]));
+        };
+        if (LISTS)
+        {
+            unsigned c = min(wl.count[i], wl.cap);
+            for (unsigned s = 0; s < c; ++s)
+                wall(wl.J[size_t(s) * n + i]);
+        }
+        else
+            for_each_candidate<D>(k.m, w_offset, ci, wall);
+        float drho_dt = f.drho_dt[i] + rate.value() * rho_i + wrate.value() * rho_i;
+        f.drho_dt[i] = drho_dt;
+        f.drho[i] = f.drho[i] + drho_dt * float(0.5 * dt);
+        double v2 = 0, a2 = 0;
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+        {
+            float F = pdis[d].value() * k.Vol + wdis[d].value() * k.Vol;
+            f.force[d * n + i] = F;
+            f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vi[d]));
+            v2 += double(vi[d]) * double(vi[d]);
+            double ft = double(F) + double(k.mass) * k.gd[d];
+            a2 += ft * ft;
+        }
+        amax = fmax(v2, 4.0 * k.h * sqrt(a2) * double(k.inv_mass));
+    }
+    block_max_slot(adv_slot, amax);
+}
+
+template <int D>
+__global__ void k_mp_initial_max(size_t n, MPConst k, MPFluid f, unsigned long long *ac_slot,
+                                 unsigned long long *adv_slot)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    double am = -1.0e300, vm = -1.0e300;
+    if (i < n)
+    {
+        double v2 = 0, a2 = 0;
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+        {
+            double v = f.vel[d * n + i];
+            v2 += v * v;
+            double ft = double(f.force[d * n + i]) + double(k.mass) * k.gd[d];
+            a2 += ft * ft;
+        }
+        vm = k.c0 + sqrt(v2);
+        am = fmax(v2, 4.0 * k.h * sqrt(a2) * double(k.inv_mass));
+    }
+    block_max_slot(ac_slot, vm);
+    block_max_slot(adv_slot, am);
+}
+
+// ---------------------------------------------------------------- outputs
+template <int D>
+__global__ void k_mp_download(size_t n, MPConst k, MPFluid f, double *__restrict__ pos, double *__restrict__ vel,
+                              double *__restrict__ rho, double *__restrict__ p, double *__restrict__ force,
+                              double *__restrict__ drho_dt)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    uint32_t o = f.id[i];
+    int c[3];
+    unpack_cell(f.cell[i], c);
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        pos[d * n + o] = cell_corner(k.m, d, c[d]) + double(f.off[d * n + i]);
+        vel[d * n + o] = f.vel[d * n + i];
+        force[d * n + o] = f.force[d * n + i];
+    }
+    rho[o] = double(k.rho0) + double(f.drho[i]);
+    p[o] = double(k.p0_over_rho0) * double(f.drho[i]);
+    drho_dt[o] = f.drho_dt[i];
+}
+
+template <int D>
+__global__ void k_mp_conservation(size_t n, MPConst k, MPFluid f, double *__restrict__ partials)
+{
+    double s[5] = {0, 0, 0, 0, 0};
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+    {
+        int c[3];
+        unpack_cell(f.cell[i], c);
+        double m = k.mass, v2 = 0, gx = 0;
+        s[0] += m;
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+        {
+            double v = f.vel[d * n + i];
+            s[1 + d] += m * v;
+            v2 += v * v;
+            double x = cell_corner(k.m, d, c[d]) + double(f.off[d * n + i]);
+            gx += k.gd[d] * (-x);
+        }
+        s[4] += 0.5 * m * v2 + m * gx;
+    }
+    __shared__ double sm[5][256];
+    for (int q = 0; q < 5; ++q)
+        sm[q][threadIdx.x] = s[q];
+    __syncthreads();
+    for (unsigned o = blockDim.x / 2; o > 0; o >>= 1)
+    {
+        if (threadIdx.x < o)
+            for (int q = 0; q < 5; ++q)
+                sm[q][threadIdx.x] += sm[q][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 5; ++q)
+            partials[blockIdx.x * 5 + q] = sm[q][0];
+}
+
+template <int D>
+__global__ void k_mp_upper_front(size_t n, MPConst k, MPFluid f, int axis, double l0, double l1, double l2,
+                                 double u0, double u1, double u2, unsigned long long *slot)
+{
+    double lo[3] = {l0, l1, l2}, up[3] = {u0, u1, u2};
+    double m = -1.0e300;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+    {
+        int c[3];
+        unpack_cell(f.cell[i], c);
+        double x[3];
+        bool in = true;
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+        {
+            x[d] = cell_corner(k.m, d, c[d]) + double(f.off[d * n + i]);
+            in = in && !(x[d] < lo[d] || x[d] > up[d]);
+        }
+        if (in)
+            m = fmax(m, x[axis]);
+    }
+    block_max_slot(slot, m);
+}
+
+template <int D>
+__global__ void k_wall_load(size_t nw, const uint32_t *__restrict__ perm, const double *__restrict__ pos,
+                            const double *__restrict__ nrm, MeshDev m, uint32_t *__restrict__ cell,
+                            float *__restrict__ off, float *__restrict__ n_out)
+{
+    size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= nw)
+        return;
+    uint32_t i = perm[k];
+    double x[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        x[d] = pos[d * nw + i];
+    int c[3] = {0, 0, 0};
+    cell_index<D>(m, x, c);
+    cell[k] = pack_cell(c[0], c[1], c[2]);
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        off[d * nw + k] = float(x[d] - cell_corner(m, d, c[d]));
+        n_out[d * nw + k] = float(nrm[d * nw + i]);
+    }
+}
+
+template <int D>
+__global__ void k_wall_hash(size_t nw, const double *__restrict__ pos, MeshDev m, uint32_t *__restrict__ key,
+                            uint32_t *__restrict__ rank, uint32_t *__restrict__ count)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= nw)
+        return;
+    double x[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        x[d] = pos[d * nw + i];
+    int c[3] = {0, 0, 0};
+    cell_index<D>(m, x, c);
+    uint32_t lc = linear_cell<D>(m, c);
+    key[i] = lc;
+    rank[i] = atomicAdd(&count[lc], 1u);
+}
+
+template <typename T>
+T *dalloc(size_t n)
+{
+    T *p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess)
+        return nullptr;
+    return p;
+}
+} // namespace
+
+struct sphx_mp_s
+{
+    sphx_ctx ctx = nullptr;
+    int dim = 3;
+    size_t n = 0, nw = 0, ncells = 0;
+    MPConst k{};
+    MPFluid a{}, b{}; // current state and re-sort target
+    MPWall w{};
+    uint32_t *f_offset = nullptr, *w_offset = nullptr, *count = nullptr;
+    uint32_t *key = nullptr, *rank = nullptr, *perm = nullptr, *ncell = nullptr;
+    float *noff = nullptr;
+    MPLists in{}, wl{};
+    unsigned long long *slots = nullptr; // 0 acoustic, 1 advection, 2 misc, 3..4 build counts
+    unsigned long long *h_slots = nullptr;
+    double physical_time = 0, acoustic_dt = 0;
+    int block = 128, strategy = 0;
+    // optional CUDA-event timing of the two sweep kernels (sphx_mp_set_profiling)
+    bool profiling = false;
+    std::vector<cudaEvent_t> ev_first, ev_second; // start/stop pairs
+    double ms_first = 0, ms_second = 0;
+    long n_first = 0, n_second = 0;
+    std::vector<void *> owned;
+    template <typename T>
+    T *alloc(size_t cnt)
+    {
+        T *p = dalloc<T>(cnt);
+        if (p)
+            owned.push_back(p);
+        return p;
+    }
+};
+
+namespace
+{
+int alloc_state(sphx_mp mp, MPFluid &s)
+{
+    size_t n = mp->n, D = size_t(mp->dim);
+    s.cell = mp->alloc<uint32_t>(n);
+    s.off = mp->alloc<float>(D * n);
+    s.off0 = mp->alloc<float>(D * n);
+    s.vel = mp->alloc<float>(D * n);
+    s.force = mp->alloc<float>(D * n);
+    s.drho = mp->alloc<float>(n);
+    s.drho_dt = mp->alloc<float>(n);
+    s.p = mp->alloc<float>(n);
+    s.id = mp->alloc<uint32_t>(n);
+    if (!s.cell || !s.off || !s.off0 || !s.vel || !s.force || !s.drho || !s.drho_dt || !s.p || !s.id)
+        return fail(SPHX_ERR_OUT_OF_MEMORY, "mixed-precision state allocation failed");
+    return SPHX_OK;
+}
+
+int alloc_lists(sphx_mp mp, MPLists &l, unsigned cap)
+{
+    if (l.J)
+    {
+        cudaFree(l.J);
+        mp->owned.erase(std::remove(mp->owned.begin(), mp->owned.end(), (void *)l.J), mp->owned.end());
+    }
+    l.J = mp->alloc<uint32_t>(size_t(cap) * std::max<size_t>(mp->n, 1));
+    if (!l.J)
+        return fail(SPHX_ERR_OUT_OF_MEMORY, "neighbour list allocation failed (%u slots)", cap);
+    l.cap = cap;
+    return SPHX_OK;
+}
+
+// Counting sort of mp->key[0..n) into mp->perm (stable), cell offsets into `offset`.
+int sort_keys(sphx_mp mp, size_t n, uint32_t *offset)
+{
+    sphx_ctx ctx = mp->ctx;
+    cudaStream_t s = ctx->stream;
+    SPHX_TRY(exclusive_scan(ctx, mp->count, offset, mp->ncells));
+    k_mp_set_total<<<1, 1, 0, s>>>(offset, mp->ncells, uint32_t(n));
+    SPHX_LAUNCHED(ctx);
+    if (n == 0)
+        return SPHX_OK;
+    k_mp_scatter<<<grid_for(n, 256), 256, 0, s>>>(n, mp->key, mp->rank, offset, mp->perm);
+    SPHX_LAUNCHED(ctx);
+    k_mp_sort_segments<<<grid_for(mp->ncells, 256), 256, 0, s>>>(mp->ncells, offset, mp->perm);
+    SPHX_LAUNCHED(ctx);
+    return SPHX_OK;
+}
+
+template <int D>
+int launch_build(sphx_mp mp)
+{
+    sphx_ctx ctx = mp->ctx;
+    cudaStream_t s = ctx->stream;
+    unsigned int *mc = reinterpret_cast<unsigned int *>(mp->slots + 3);
+    for (int attempt = 0; attempt < 2; ++attempt)
+    {
+        SPHX_CUDA(cudaMemsetAsync(mc, 0, 2 * sizeof(unsigned int), s));
+        k_mp_build<D><<<grid_for(mp->n, 256), 256, 0, s>>>(mp->n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset,
+                                                          mp->in, mp->wl, mc);
+        SPHX_LAUNCHED(ctx);
+        SPHX_CUDA(cudaMemcpyAsync(mp->h_slots + 3, mc, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+        SPHX_CUDA(cudaStreamSynchronize(s));
+        const unsigned int *h = reinterpret_cast<const unsigned int *>(mp->h_slots + 3);
+        bool grow = false;
+        if (h[0] > mp->in.cap)
+        {
+            SPHX_TRY(alloc_lists(mp, mp->in, h[0] + h[0] / 4 + 4));
+            grow = true;
+        }
+        if (h[1] > mp->wl.cap)
+        {
+            SPHX_TRY(alloc_lists(mp, mp->wl, h[1] + h[1] / 4 + 4));
+            grow = true;
+        }
+        if (!grow)
+            return SPHX_OK;
+    }
+    return fail(SPHX_ERR_CAPACITY, "mixed-precision neighbour lists overflowed after growing");
+}
+
+template <int D>
+int configuration_update(sphx_mp mp, bool from_state)
+{
+    sphx_ctx ctx = mp->ctx;
+    cudaStream_t s = ctx->stream;
+    size_t n = mp->n;
+    MeshDev m = mp->k.m;
+    if (from_state)
+        SPHX_CUDA(cudaMemsetAsync(mp->count, 0, mp->ncells * sizeof(uint32_t), s));
+    if (n > 0 && from_state)
+    {
+        k_mp_rehash<D><<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.cell, mp->a.off, m, mp->ncell, mp->noff, mp->key,
+                                                        mp->rank, mp->count);
+        SPHX_LAUNCHED(ctx);
+    }
+    SPHX_TRY(sort_keys(mp, n, mp->f_offset));
+    if (n > 0)
+    {
+        k_mp_gather<D><<<grid_for(n, 256), 256, 0, s>>>(n, mp->perm, mp->ncell, mp->noff, mp->a, mp->b);
+        SPHX_LAUNCHED(ctx);
+        std::swap(mp->a, mp->b);
+        SPHX_TRY(launch_build<D>(mp));
+    }
+    return SPHX_OK;
+}
+
+int read_slot(sphx_mp mp, int slot, double *out)
+{
+    SPHX_CUDA(cudaMemcpyAsync(mp->h_slots + slot, mp->slots + slot, sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost, mp->ctx->stream));
+    SPHX_CUDA(cudaStreamSynchronize(mp->ctx->stream));
+    *out = from_ordered_bits(mp->h_slots[slot]);
+    return SPHX_OK;
+}
+
+template <int D>
+int substep(sphx_mp mp, double dt)
+{
+    sphx_ctx ctx = mp->ctx;
+    cudaStream_t s = ctx->stream;
+    size_t n = mp->n;
+    if (n == 0)
+        return SPHX_OK;
+    unsigned blk = unsigned(mp->block);
+    k_mp_init1<<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.drho, mp->a.drho_dt, mp->a.p, mp->k.p0_over_rho0,
+                                                float(0.5 * dt));
+    SPHX_LAUNCHED(ctx);
+    SPHX_CUDA(cudaMemsetAsync(mp->slots, 0, 2 * sizeof(unsigned long long), s));
+    cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
+    if (mp->profiling)
+        for (int q = 0; q < 4; ++q)
+        {
+            SPHX_CUDA(cudaEventCreate(&e[q]));
+            (q < 2 ? mp->ev_first : mp->ev_second).push_back(e[q]);
+        }
+    if (e[0])
+        SPHX_CUDA(cudaEventRecord(e[0], s));
+    if (mp->strategy == 0)
+        k_mp_first<D, true><<<grid_for(n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset,
+                                                            mp->in, mp->wl, dt, mp->slots);
+    else
+        k_mp_first<D, false><<<grid_for(n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset,
+                                                             mp->in, mp->wl, dt, mp->slots);
+    SPHX_LAUNCHED(ctx);
+    if (e[1])
+        SPHX_CUDA(cudaEventRecord(e[1], s));
+    if (e[2])
+        SPHX_CUDA(cudaEventRecord(e[2], s));
+    if (mp->strategy == 0)
+        k_mp_second<D, true><<<grid_for(n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset,
+                                                             mp->in, mp->wl, dt, mp->slots + 1);
+    else
+        k_mp_second<D, false><<<grid_for(n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->f_offset, mp->w,
+                                                              mp->w_offset, mp->in, mp->wl, dt, mp->slots + 1);
+    SPHX_LAUNCHED(ctx);
+    if (e[3])
+        SPHX_CUDA(cudaEventRecord(e[3], s));
+    return SPHX_OK;
+}
+
+template <int D>
+int advection_step(sphx_mp mp, int loop_style, int *substeps, double *adv_dt)
+{
+    double adv_max;
+    SPHX_TRY(read_slot(mp, 1, &adv_max));
+    double Dt = mp->k.advection_cfl * mp->k.h / (std::max(std::sqrt(adv_max), mp->k.U_ref) + kTinyReal);
+    double relaxation = 0, dt = mp->acoustic_dt;
+    int count = 0;
+    while (relaxation < Dt)
+    {
+        double ac;
+        if (loop_style == 0) // AcousticTimeStep before the relaxation (Dambreak.cpp:184)
+        {
+            SPHX_TRY(read_slot(mp, 0, &ac));
+            dt = mp->k.acoustic_cfl * mp->k.h / (ac + kTinyReal);
+        }
+        SPHX_TRY(substep<D>(mp, dt));
+        if (loop_style == 1) // after it (test_3d_dambreak/dambreak.cpp:197)
+        {
+            SPHX_TRY(read_slot(mp, 0, &ac));
+            dt = mp->k.acoustic_cfl * mp->k.h / (ac + kTinyReal);
+        }
+        relaxation += dt;
+        mp->physical_time += dt;
+        ++count;
+    }
+    mp->acoustic_dt = dt;
+    SPHX_TRY(configuration_update<D>(mp, true));
+    if (substeps)
+        *substeps = count;
+    if (adv_dt)
+        *adv_dt = Dt;
+    return SPHX_OK;
+}
+} // namespace
+
+extern "C" int sphx_mp_create(sphx_relation inner, sphx_relation wall, const sphx_fluid_params *p,
+                              const double *gravity, sphx_mp *out)
+{
+    if (!inner || !wall || !p || !gravity || !out || !inner->inner || wall->inner || wall->src != inner->src)
+        return fail(SPHX_ERR_INVALID_ARG, "sphx_mp_create needs an inner and a wall contact relation of one fluid");
+    sphx_body fb = inner->src, wb = wall->tgt;
+    const int D = fb->dim;
+    sphx_ctx ctx = fb->ctx;
+    const sphx_mesh_desc &mesh = inner->cl->mesh;
+    for (int a = 0; a < D; ++a)
+        if (mesh.all_cells[a] > 1024)
+            return fail(SPHX_ERR_INVALID_ARG, "mixed precision packs 10 bits per cell axis; axis %d has %d cells", a,
+                        mesh.all_cells[a]);
+    if (std::abs(wall->cl->mesh.grid_spacing - mesh.grid_spacing) > 0 ||
+        std::abs(2.0 * p->h - mesh.grid_spacing) > 1e-12 * mesh.grid_spacing)
+        return fail(SPHX_ERR_INVALID_ARG, "mixed precision needs one mesh with grid spacing equal to the cut-off");
+    // host checks of uniform mass / volume and a static wall (after the queued work)
+    SPHX_CUDA(cudaStreamSynchronize(ctx->stream));
+    auto host_copy = [&](sphx_body b, const char *name, std::vector<double> &v) -> int {
+        Field *f = b->find(name);
+        if (!f || f->dtype != SPHX_F64)
+            return fail(SPHX_ERR_NOT_FOUND, "variable %s missing", name);
+        v.resize(b->n * f->ncomp);
+        if (!v.empty())
+            SPHX_CUDA(cudaMemcpy(v.data(), f->dev, v.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        return SPHX_OK;
+    };
+    std::vector<double> mass, vol, wvol, wmass, wvel, wacc, fprior;
+    SPHX_TRY(host_copy(fb, "Mass", mass));
+    SPHX_TRY(host_copy(fb, "VolumetricMeasure", vol));
+    SPHX_TRY(host_copy(wb, "VolumetricMeasure", wvol));
+    SPHX_TRY(host_copy(wb, "Mass", wmass));
+    auto uniform = [](const std::vector<double> &v) {
+        for (double x : v)
+            if (x != v[0])
+                return false;
+        return true;
+    };
+    if (mass.empty() || !uniform(mass) || !uniform(vol) || (!wvol.empty() && (!uniform(wvol) || !uniform(wmass))))
+        return fail(SPHX_ERR_INVALID_ARG, "mixed precision needs uniform particle mass and volume");
+    if (wb->find("Velocity") && host_copy(wb, "Velocity", wvel) == SPHX_OK)
+        for (double x : wvel)
+            if (x != 0.0)
+                return fail(SPHX_ERR_INVALID_ARG, "mixed precision needs a static wall");
+    if (wb->find("Acceleration") && host_copy(wb, "Acceleration", wacc) == SPHX_OK)
+        for (double x : wacc)
+            if (x != 0.0)
+                return fail(SPHX_ERR_INVALID_ARG, "mixed precision needs a static wall");
+    if (fb->find("ForcePrior") && host_copy(fb, "ForcePrior", fprior) == SPHX_OK)
+        for (size_t i = 0; i < fb->n; ++i)
+            for (int d = 0; d < D; ++d)
+                if (std::abs(fprior[i * D + d] - mass[i] * gravity[d]) > 1e-12 * std::abs(mass[i]) * 10)
+                    return fail(SPHX_ERR_INVALID_ARG, "mixed precision needs gravity as the only prior force");
+
+    sphx_mp mp = new sphx_mp_s();
+    mp->ctx = ctx;
+    ctx->retain();
+    mp->dim = D;
+    mp->n = fb->n;
+    mp->nw = wb->n;
+    size_t nc = 1;
+    for (int a = 0; a < D; ++a)
+        nc *= size_t(mesh.all_cells[a]);
+    mp->ncells = nc;
+    MPConst &k = mp->k;
+    k.m = mesh_dev(mesh);
+    k.gs_f = float(mesh.grid_spacing);
+    WendlandC2 wk = wendland(D, p->h);
+    k.rc_sqr = float(wk.rc_sqr);
+    k.inv_h = float(wk.inv_h);
+    k.fW = float(wk.factor_W);
+    k.fdW = float(wk.factor_dW);
+    k.rho0 = float(p->rho0);
+    k.p0_over_rho0 = float(p->rho0 * p->c0 * p->c0 / p->rho0);
+    k.Vol = float(vol[0]);
+    k.mass = float(mass[0]);
+    k.inv_mass = float(1.0 / mass[0]);
+    k.sigma0 = p->sigma0;
+    k.rho0_over_sigma0 = float(p->rho0 / p->sigma0);
+    double wm = wmass.empty() ? 0.0 : wmass[0];
+    k.wall_factor = float(wall->tgt_inv_rho0 * wm * p->rho0 * p->rho0 / (p->sigma0 * mass[0]));
+    k.wall_Vol = float(wvol.empty() ? 0.0 : wvol[0]);
+    double Z = p->rho0 * p->c0;
+    k.inv_z = float((Z + Z) / (Z * Z + Z * Z));
+    k.zgeo = float(2.0 * Z * Z / (Z + Z));
+    k.inv_c0 = float(0.5 * (p->rho0 + p->rho0) * double(k.inv_z));
+    k.slope = float(p->limiter_slope);
+    for (int d = 0; d < 3; ++d)
+    {
+        k.gd[d] = d < D ? gravity[d] : 0.0;
+        k.g[d] = float(k.gd[d]);
+    }
+    k.h = p->h;
+    k.c0 = p->c0;
+    k.acoustic_cfl = p->acoustic_cfl;
+    k.advection_cfl = p->advection_cfl;
+    k.U_ref = p->U_ref;
+
+    int st = SPHX_OK;
+    auto bail = [&](int code) {
+        sphx_mp_destroy(mp);
+        return code;
+    };
+    if ((st = alloc_state(mp, mp->a)) != SPHX_OK || (st = alloc_state(mp, mp->b)) != SPHX_OK)
+        return bail(st);
+    size_t n = mp->n, nw = mp->nw, big = std::max(n, nw);
+    mp->f_offset = mp->alloc<uint32_t>(nc + 1);
+    mp->w_offset = mp->alloc<uint32_t>(nc + 1);
+    mp->count = mp->alloc<uint32_t>(nc);
+    mp->key = mp->alloc<uint32_t>(big);
+    mp->rank = mp->alloc<uint32_t>(big);
+    mp->perm = mp->alloc<uint32_t>(big);
+    mp->ncell = mp->alloc<uint32_t>(n);
+    mp->noff = mp->alloc<float>(3 * n);
+    mp->w.cell = mp->alloc<uint32_t>(nw);
+    mp->w.off = mp->alloc<float>(3 * nw);
+    mp->w.n = mp->alloc<float>(3 * nw);
+    mp->w.nw = nw;
+    mp->in.count = mp->alloc<uint32_t>(n);
+    mp->wl.count = mp->alloc<uint32_t>(n);
+    mp->slots = mp->alloc<unsigned long long>(8);
+    if (!mp->f_offset || !mp->w_offset || !mp->count || !mp->key || !mp->rank || !mp->perm || !mp->ncell ||
+        !mp->noff || !mp->w.cell || !mp->w.off || !mp->w.n || !mp->in.count || !mp->wl.count || !mp->slots)
+        return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "mixed-precision allocation failed"));
+    if (cudaMallocHost(&mp->h_slots, 8 * sizeof(unsigned long long)) != cudaSuccess)
+        return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "pinned allocation failed"));
+    if ((st = alloc_lists(mp, mp->in, D == 2 ? 24 : 96)) != SPHX_OK ||
+        (st = alloc_lists(mp, mp->wl, D == 2 ? 16 : 64)) != SPHX_OK)
+        return bail(st);
+
+    cudaStream_t s = ctx->stream;
+    MeshDev m = k.m;
+    // wall: cell-sorted once (static)
+    Field *wpos = wb->find("Position"), *wn = wb->find("NormalDirection");
+    if (!wpos || !wn)
+        return bail(fail(SPHX_ERR_NOT_FOUND, "wall Position / NormalDirection missing"));
+    if (cudaMemsetAsync(mp->count, 0, nc * sizeof(uint32_t), s) != cudaSuccess)
+        return bail(fail(SPHX_ERR_CUDA, "memset failed"));
+    if (nw > 0)
+    {
+        if (D == 2)
+            k_wall_hash<2><<<grid_for(nw, 256), 256, 0, s>>>(nw, (const double *)wpos->dev, m, mp->key, mp->rank,
+                                                              mp->count);
+        else
+            k_wall_hash<3><<<grid_for(nw, 256), 256, 0, s>>>(nw, (const double *)wpos->dev, m, mp->key, mp->rank,
+                                                              mp->count);
+        ctx->launches++;
+    }
+    if ((st = sort_keys(mp, nw, mp->w_offset)) != SPHX_OK)
+        return bail(st);
+    if (nw > 0)
+    {
+        if (D == 2)
+            k_wall_load<2><<<grid_for(nw, 256), 256, 0, s>>>(nw, mp->perm, (const double *)wpos->dev,
+                                                              (const double *)wn->dev, m, mp->w.cell, mp->w.off,
+                                                              mp->w.n);
+        else
+            k_wall_load<3><<<grid_for(nw, 256), 256, 0, s>>>(nw, mp->perm, (const double *)wpos->dev,
+                                                              (const double *)wn->dev, m, mp->w.cell, mp->w.off,
+                                                              mp->w.n);
+        ctx->launches++;
+    }
+    // fluid: FP64 body state -> FP32 (body order) in `a`, then the first configuration
+    Field *pos = fb->find("Position"), *vel = fb->find("Velocity"), *force = fb->find("Force"),
+          *rho = fb->find("Density"), *drho = fb->find("DensityChangeRate");
+    if (!pos || !rho)
+        return bail(fail(SPHX_ERR_NOT_FOUND, "fluid Position / Density missing"));
+    {
+        std::vector<double> hv(n * D, 0.0), hf(n * D, 0.0), hr(n, p->rho0), hd(n, 0.0);
+        if (vel && cudaMemcpy(hv.data(), vel->dev, hv.size() * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return bail(fail(SPHX_ERR_CUDA, "copy failed"));
+        if (force && cudaMemcpy(hf.data(), force->dev, hf.size() * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return bail(fail(SPHX_ERR_CUDA, "copy failed"));
+        if (cudaMemcpy(hr.data(), rho->dev, hr.size() * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return bail(fail(SPHX_ERR_CUDA, "copy failed"));
+        if (drho && cudaMemcpy(hd.data(), drho->dev, hd.size() * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return bail(fail(SPHX_ERR_CUDA, "copy failed"));
+        std::vector<float> fv(hv.begin(), hv.end()), ff(hf.begin(), hf.end()), fr(n), fd(hd.begin(), hd.end());
+        std::vector<uint32_t> ids(n);
+        for (size_t i = 0; i < n; ++i)
+        {
+            fr[i] = float(hr[i] - p->rho0);
+            ids[i] = uint32_t(i);
+        }
+        if (cudaMemcpy(mp->a.vel, fv.data(), fv.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(mp->a.force, ff.data(), ff.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(mp->a.drho, fr.data(), fr.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(mp->a.drho_dt, fd.data(), fd.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(mp->a.id, ids.data(), ids.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(fail(SPHX_ERR_CUDA, "copy failed"));
+    }
+    if (cudaMemsetAsync(mp->count, 0, nc * sizeof(uint32_t), s) != cudaSuccess)
+        return bail(fail(SPHX_ERR_CUDA, "memset failed"));
+    if (n > 0)
+    {
+        if (D == 2)
+            k_mp_from_fp64<2><<<grid_for(n, 256), 256, 0, s>>>(n, (const double *)pos->dev, m, mp->ncell, mp->noff,
+                                                               mp->key, mp->rank, mp->count);
+        else
+            k_mp_from_fp64<3><<<grid_for(n, 256), 256, 0, s>>>(n, (const double *)pos->dev, m, mp->ncell, mp->noff,
+                                                               mp->key, mp->rank, mp->count);
+        ctx->launches++;
+    }
+    st = D == 2 ? configuration_update<2>(mp, false) : configuration_update<3>(mp, false);
+    if (st != SPHX_OK)
+        return bail(st);
+    // initial maxima for the first time steps
+    if (cudaMemsetAsync(mp->slots, 0, 2 * sizeof(unsigned long long), s) != cudaSuccess)
+        return bail(fail(SPHX_ERR_CUDA, "memset failed"));
+    if (n > 0)
+    {
+        if (D == 2)
+            k_mp_initial_max<2><<<grid_for(n, 256), 256, 0, s>>>(n, mp->k, mp->a, mp->slots, mp->slots + 1);
+        else
+            k_mp_initial_max<3><<<grid_for(n, 256), 256, 0, s>>>(n, mp->k, mp->a, mp->slots, mp->slots + 1);
+        ctx->launches++;
+    }
+    if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+        return bail(fail(SPHX_ERR_CUDA, "mixed-precision set-up failed"));
+    *out = mp;
+    return SPHX_OK;
+}
+
+namespace
+{
+// Folds the recorded event pairs into the running totals and frees the events.
+void collect_events(sphx_mp mp)
+{
+    auto fold = [](std::vector<cudaEvent_t> &ev, double &ms, long &cnt) {
+        for (size_t q = 0; q + 1 < ev.size(); q += 2)
+        {
+            float t = 0.f;
+            if (cudaEventElapsedTime(&t, ev[q], ev[q + 1]) == cudaSuccess)
+            {
+                ms += t;
+                ++cnt;
+            }
+            cudaEventDestroy(ev[q]);
+            cudaEventDestroy(ev[q + 1]);
+        }
+        ev.clear();
+    };
+    fold(mp->ev_first, mp->ms_first, mp->n_first);
+    fold(mp->ev_second, mp->ms_second, mp->n_second);
+}
+} // namespace
+
+extern "C" int sphx_mp_set_profiling(sphx_mp mp, int on)
+{
+    if (!mp)
+        return fail(SPHX_ERR_INVALID_ARG, "null solver");
+    SPHX_CUDA(cudaStreamSynchronize(mp->ctx->stream));
+    collect_events(mp);
+    mp->profiling = on != 0;
+    mp->ms_first = mp->ms_second = 0;
+    mp->n_first = mp->n_second = 0;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_mp_kernel_times(sphx_mp mp, double *out)
+{
+    if (!mp || !out)
+        return fail(SPHX_ERR_INVALID_ARG, "null argument");
+    SPHX_CUDA(cudaStreamSynchronize(mp->ctx->stream));
+    collect_events(mp);
+    out[0] = mp->ms_first;
+    out[1] = double(mp->n_first);
+    out[2] = mp->ms_second;
+    out[3] = double(mp->n_second);
+    return SPHX_OK;
+}
+
+extern "C" int sphx_mp_list_sizes(sphx_mp mp, uint64_t *out)
+{
+    if (!mp || !out)
+        return fail(SPHX_ERR_INVALID_ARG, "null argument");
+    size_t n = mp->n;
+    std::vector<uint32_t> a(n), b(n);
+    if (n)
+    {
+        SPHX_CUDA(cudaMemcpyAsync(a.data(), mp->in.count, n * 4, cudaMemcpyDeviceToHost, mp->ctx->stream));
+        SPHX_CUDA(cudaMemcpyAsync(b.data(), mp->wl.count, n * 4, cudaMemcpyDeviceToHost, mp->ctx->stream));
+    }
+    SPHX_CUDA(cudaStreamSynchronize(mp->ctx->stream));
+    uint64_t si = 0, sw = 0;
+    for (size_t i = 0; i < n; ++i)
+    {
+        si += a[i];
+        sw += b[i];
+    }
+    out[0] = mp->n;
+    out[1] = mp->nw;
+    out[2] = si;
+    out[3] = sw;
+    out[4] = mp->in.cap;
+    out[5] = mp->wl.cap;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_mp_destroy(sphx_mp mp)
+{
+    if (!mp)
+        return SPHX_OK;
+    sphx_ctx ctx = mp->ctx;
+    cudaStreamSynchronize(ctx->stream);
+    collect_events(mp);
+    for (void *p : mp->owned)
+        cudaFree(p);
+    if (mp->h_slots)
+        cudaFreeHost(mp->h_slots);
+    delete mp;
+    release(ctx);
+    return SPHX_OK;
+}
+
+extern "C" int sphx_mp_set_tuning(sphx_mp mp, int block, int strategy)
+{
+    if (!mp || block < 64 || block > 256 || block % 32 != 0 || strategy < 0 || strategy > 1)
+        return fail(SPHX_ERR_INVALID_ARG, "block must be 64..256 in steps of 32, strategy 0 or 1");
+    mp->block = block;
+    mp->strategy = strategy;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_mp_advection_step(sphx_mp mp, int loop_style, int *substeps, double *advection_dt,
+                                      double *physical_time)
+{
+    if (!mp || (loop_style != 0 && loop_style != 1))
+        return fail(SPHX_ERR_INVALID_ARG, "invalid advection-step arguments");
+    SPHX_TRY(mp->dim == 2 ? advection_step<2>(mp, loop_style, substeps, advection_dt)
+                          : advection_step<3>(mp, loop_style, substeps, advection_dt));
+    if (physical_time)
+        *physical_time = mp->physical_time;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_mp_download(sphx_mp mp, sphx_body fb)
+{
+    if (!mp || !fb || fb->n != mp->n || fb->dim != mp->dim)
+        return fail(SPHX_ERR_INVALID_ARG, "body does not match the mixed-precision solver");
+    int D = mp->dim;
+    Field *pos, *vel, *rho, *p, *force, *drho;
+    SPHX_TRY(fb->require("Position", SPHX_F64, D, &pos));
+    SPHX_TRY(fb->require("Velocity", SPHX_F64, D, &vel));
+    SPHX_TRY(fb->require("Density", SPHX_F64, 1, &rho));
+    SPHX_TRY(fb->require("Pressure", SPHX_F64, 1, &p));
+    SPHX_TRY(fb->require("Force", SPHX_F64, D, &force));
+    SPHX_TRY(fb->require("DensityChangeRate", SPHX_F64, 1, &drho));
+    size_t n = mp->n;
+    if (n > 0)
+    {
+        if (D == 2)
+            k_mp_download<2><<<grid_for(n, 256), 256, 0, mp->ctx->stream>>>(
+                n, mp->k, mp->a, (double *)pos->dev, (double *)vel->dev, (double *)rho->dev, (double *)p->dev,
+                (double *)force->dev, (double *)drho->dev);
+        else
+            k_mp_download<3><<<grid_for(n, 256), 256, 0, mp->ctx->stream>>>(
+                n, mp->k, mp->a, (double *)pos->dev, (double *)vel->dev, (double *)rho->dev, (double *)p->dev,
+                (double *)force->dev, (double *)drho->dev);
+        SPHX_LAUNCHED(mp->ctx);
+    }
+    SPHX_CUDA(cudaStreamSynchronize(mp->ctx->stream));
+    return SPHX_OK;
+}
+
+extern "C" int sphx_mp_conservation(sphx_mp mp, double *out)
+{
+    if (!mp || !out)
+        return fail(SPHX_ERR_INVALID_ARG, "null argument");
+    sphx_ctx ctx = mp->ctx;
+    unsigned np = unsigned(std::max(1, std::min(ctx->num_sms * 4, int(grid_for(std::max<size_t>(mp->n, 1), 256)))));
+    SPHX_TRY(ctx->ensure_scratch(size_t(np) * 5 * sizeof(double)));
+    double *part = static_cast<double *>(ctx->d_scratch);
+    if (mp->dim == 2)
+        k_mp_conservation<2><<<np, 256, 0, ctx->stream>>>(mp->n, mp->k, mp->a, part);
+    else
+        k_mp_conservation<3><<<np, 256, 0, ctx->stream>>>(mp->n, mp->k, mp->a, part);
+    SPHX_LAUNCHED(ctx);
+    std::vector<double> h(size_t(np) * 5);
+    SPHX_CUDA(cudaMemcpyAsync(h.data(), part, h.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SPHX_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int q = 0; q < 5; ++q)
+    {
+        double s = 0;
+        for (unsigned b = 0; b < np; ++b)
+            s += h[b * 5 + q];
+        out[q] = s;
+    }
+    return SPHX_OK;
+}
+
+extern "C" int sphx_mp_upper_front(sphx_mp mp, int axis, const double *lo, const double *up, double *front)
+{
+    if (!mp || !lo || !up || !front || axis < 0 || axis >= mp->dim)
+        return fail(SPHX_ERR_INVALID_ARG, "invalid upper-front arguments");
+    sphx_ctx ctx = mp->ctx;
+    SPHX_CUDA(cudaMemsetAsync(mp->slots + 2, 0, sizeof(unsigned long long), ctx->stream));
+    unsigned g = unsigned(std::max(1, std::min(ctx->num_sms * 4, int(grid_for(std::max<size_t>(mp->n, 1), 256)))));
+    double l2 = mp->dim == 3 ? lo[2] : 0.0, u2 = mp->dim == 3 ? up[2] : 0.0;
+    if (mp->dim == 2)
+        k_mp_upper_front<2><<<g, 256, 0, ctx->stream>>>(mp->n, mp->k, mp->a, axis, lo[0], lo[1], l2, up[0], up[1], u2,
+                                                        mp->slots + 2);
+    else
+        k_mp_upper_front<3><<<g, 256, 0, ctx->stream>>>(mp->n, mp->k, mp->a, axis, lo[0], lo[1], l2, up[0], up[1], u2,
+                                                        mp->slots + 2);
+    SPHX_LAUNCHED(ctx);
+    return read_slot(mp, 2, front);
+}

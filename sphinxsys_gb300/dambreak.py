@@ -115,3 +115,131 @@ class DamBreak:
             energy = self.mechanical_energy.exec()
         self.update_configuration()
         return substeps, Dt, obs, energy
+
+
+class MixedPrecisionDamBreak:
+    """The same dam break advanced by the mixed-precision fused solver (sphx_mp_*).
+
+    Set-up is the FP64 one of ``DamBreak`` (bodies, relations, gravity, normals); the
+    solver then takes the FP64 state over.  ``sync_fp64`` writes the state back into the
+    FP64 fluid body (and refreshes its cell list and observer relation) for outputs.
+    """
+
+    def __init__(self, case: DamBreakCase, device: int = 0, block: int = 128, strategy: int = 0):
+        import ctypes as C
+        from . import native as N
+        self._C, self._N = C, N
+        self.fp64 = DamBreak(case, device=device)
+        self.case = case
+        sim = self.fp64
+        g = np.zeros(3)
+        g[: case.dim] = case.gravity[: case.dim]
+        self._g = g
+        h = C.c_void_p()
+        N.call("sphx_mp_create", sim.water_block_inner.handle, sim.water_wall_contact.handle,
+               C.byref(sim.fluid_pressure_relaxation.params), g.ctypes.data_as(C.POINTER(C.c_double)), C.byref(h))
+        self.handle = h
+        self.set_tuning(block, strategy)
+        self.physical_time = 0.0
+        self.number_of_iterations = 0
+        self.total_substeps = 0
+
+    @property
+    def ctx(self):
+        return self.fp64.ctx
+
+    @property
+    def n_fluid(self) -> int:
+        return self.fp64.water_block.n
+
+    def set_tuning(self, block: int, strategy: int) -> None:
+        self._N.call("sphx_mp_set_tuning", self.handle, int(block), int(strategy))
+
+    def advection_step(self):
+        C, N = self._C, self._N
+        sub = C.c_int()
+        Dt = C.c_double()
+        t = C.c_double()
+        N.call("sphx_mp_advection_step", self.handle, self.case.loop_style, C.byref(sub), C.byref(Dt), C.byref(t))
+        self.physical_time = t.value
+        self.number_of_iterations += 1
+        self.total_substeps += sub.value
+        return sub.value, Dt.value
+
+    def set_profiling(self, on: bool) -> None:
+        self._N.call("sphx_mp_set_profiling", self.handle, int(on))
+
+    def kernel_times(self):
+        """(ms per 1st-half sweep, ms per 2nd-half sweep) averaged over the recorded sweeps."""
+        C = self._C
+        out = np.zeros(4)
+        self._N.call("sphx_mp_kernel_times", self.handle, out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out[0] / max(out[1], 1), out[2] / max(out[3], 1), int(out[1])
+
+    def list_sizes(self):
+        C = self._C
+        out = np.zeros(6, dtype=np.uint64)
+        self._N.call("sphx_mp_list_sizes", self.handle, out.ctypes.data_as(C.POINTER(C.c_uint64)))
+        return dict(n=int(out[0]), nw=int(out[1]), nnz_inner=int(out[2]), nnz_wall=int(out[3]),
+                    cap_inner=int(out[4]), cap_wall=int(out[5]))
+
+    def sync_fp64(self) -> None:
+        sim = self.fp64
+        self._N.call("sphx_mp_download", self.handle, sim.water_block.handle)
+        sim.water_block.updateCellLinkedList()
+        if sim.fluid_observer.n:
+            sim.fluid_observer_contact.updateConfiguration()
+
+    def observe_pressure(self) -> np.ndarray:
+        self.sync_fp64()
+        return self.fp64.recorded_pressure.exec()
+
+    # The FP64 body doubles as the FP64 reference run in the benchmark; these views write
+    # the mixed state into a scratch body so that the FP64 body stays untouched.
+    def _scratch(self):
+        if getattr(self, "_scratch_body", None) is None:
+            from . import sph as S
+            sim = self.fp64
+            body = S.FluidBody(sim.sph_system, sim.water_block.shape)
+            body.defineMatterMaterial(sim.water_block.material)
+            body.generateParticles(S.Lattice)
+            body.upload("Mass", sim.water_block.download("Mass"))
+            self._scratch_body = body
+            self._scratch_obs = S.ContactRelation(sim.fluid_observer, [body]) if sim.fluid_observer.n else None
+        self._N.call("sphx_mp_download", self.handle, self._scratch_body.handle)
+        return self._scratch_body
+
+    def fp64_view(self, name: str) -> np.ndarray:
+        return self._scratch().download(name)
+
+    def observe_pressure_view(self) -> np.ndarray:
+        body = self._scratch()
+        if self._scratch_obs is None:
+            return np.zeros(0)
+        from . import sph as S
+        body.updateCellLinkedList()
+        self._scratch_obs.updateConfiguration()
+        return S.ObservedQuantityRecording("Pressure", self._scratch_obs).exec()
+
+    def conservation(self) -> np.ndarray:
+        C = self._C
+        out = np.zeros(5)
+        self._N.call("sphx_mp_conservation", self.handle, out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out
+
+    def upper_front(self, axis: int, lower, upper) -> float:
+        C = self._C
+        lo = np.zeros(3)
+        up = np.zeros(3)
+        lo[: len(lower)] = lower
+        up[: len(upper)] = upper
+        out = C.c_double()
+        pd = C.POINTER(C.c_double)
+        self._N.call("sphx_mp_upper_front", self.handle, axis, lo.ctypes.data_as(pd), up.ctypes.data_as(pd),
+                     C.byref(out))
+        return out.value
+
+    def __del__(self):
+        if getattr(self, "handle", None) is not None and self._N._lib is not None:
+            self._N._lib.sphx_mp_destroy(self.handle)
+            self.handle = None

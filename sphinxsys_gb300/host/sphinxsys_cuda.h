@@ -546,6 +546,11 @@ struct NormalDirectionFromBodyShape
 
 inline sphx_fluid_params fluidParams(SPHBody &b, Real U_ref = 0.0)
 {
+    // registerStateVariable of the fluid-step variables (fluid_integration.hpp:10-22)
+    for (const char *v : {"Velocity", "Force", "ForcePrior"})
+        check(sphx_body_register(b.body_, v, SPHX_F64, Dimensions));
+    for (const char *v : {"Pressure", "DensityChangeRate", "DensitySummation"})
+        check(sphx_body_register(b.body_, v, SPHX_F64, 1));
     sphx_fluid_params p{};
     p.rho0 = b.rho0_;
     p.c0 = b.c0_;

@@ -76,6 +76,16 @@ SIGNATURES = {
     "sphx_observe_quantity": (_i, [_vp, C.c_char_p, _pd]),
     "sphx_total_mechanical_energy": (_i, [_vp, _pd, _pd]),
     "sphx_upper_front_in_axis_direction": (_i, [_vp, _i, _pd, _pd, _pd]),
+    "sphx_mp_create": (_i, [_vp, _vp, C.POINTER(FluidParams), _pd, _pvp]),
+    "sphx_mp_destroy": (_i, [_vp]),
+    "sphx_mp_advection_step": (_i, [_vp, _i, C.POINTER(C.c_int), _pd, _pd]),
+    "sphx_mp_download": (_i, [_vp, _vp]),
+    "sphx_mp_conservation": (_i, [_vp, _pd]),
+    "sphx_mp_upper_front": (_i, [_vp, _i, _pd, _pd, _pd]),
+    "sphx_mp_set_tuning": (_i, [_vp, _i, _i]),
+    "sphx_mp_set_profiling": (_i, [_vp, _i]),
+    "sphx_mp_kernel_times": (_i, [_vp, _pd]),
+    "sphx_mp_list_sizes": (_i, [_vp, _pu64]),
 }
 
 _lib: Optional[C.CDLL] = None

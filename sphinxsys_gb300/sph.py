@@ -464,6 +464,11 @@ class NormalDirectionFromBodyShape:
 
 def fluid_params(body: SPHBody, U_ref: float = 0.0, acoustic_cfl: float = 0.6,
                  advection_cfl: float = 0.25) -> N.FluidParams:
+    # registerStateVariable of the fluid-step variables (fluid_integration.hpp:10-22)
+    for v in ("Velocity", "Force", "ForcePrior"):
+        N.call("sphx_body_register", body.handle, v.encode(), N.F64, body.dim)
+    for v in ("Pressure", "DensityChangeRate", "DensitySummation"):
+        N.call("sphx_body_register", body.handle, v.encode(), N.F64, 1)
     p = N.FluidParams()
     p.rho0, p.c0 = body.material.rho0, body.material.c0
     p.h = body.h

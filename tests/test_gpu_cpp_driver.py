@@ -30,7 +30,9 @@ def test_example_compiles(tmp_path):
 def test_cpp_driver_matches_oracle(tmp_path):
     exe = compile_example(tmp_path)
     iters = 201
-    out = subprocess.run([exe, "20", str(iters)], check=True, capture_output=True, text=True).stdout.split("\n")
+    res = subprocess.run([exe, "20", str(iters)], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    out = res.stdout.split("\n")
     rows = [ln.split() for ln in out if ln.startswith(("observe", "final"))]
     oc = O.OracleCase(cases.dambreak_2d())
     expect = [(0, 0.0, oc.observe_pressure()[0], oc.total_mechanical_energy())]

@@ -1,0 +1,81 @@
+"""Mixed-precision solver against the FP64 GPU path, and its internal consistency.
+
+Tolerance: fields within 1e-4 relative (max |mp - fp64| / max |fp64|) after 20 advection
+steps; the stored-list and cell-sweep strategies, and every block size, agree bit for bit
+(same pair set, same summation order)."""
+import numpy as np
+import pytest
+
+from sphinxsys_gb300 import cases
+from sphinxsys_gb300.dambreak import DamBreak, MixedPrecisionDamBreak
+
+pytestmark = pytest.mark.gpu
+
+MP_RTOL = 1e-4
+
+
+def rel_err(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(np.max(np.abs(b)), 1e-300))
+
+
+def run_pair(case, steps):
+    ref = DamBreak(case)
+    mp = MixedPrecisionDamBreak(case)
+    subs = []
+    for _ in range(steps):
+        s_r, dt_r, _, _ = ref.advection_step()
+        s_m, dt_m = mp.advection_step()
+        subs.append((s_r, s_m, dt_r, dt_m))
+    mp.sync_fp64()
+    return ref, mp, subs
+
+
+@pytest.mark.parametrize("case", [cases.dambreak_2d(), cases.dambreak_3d(0.04)], ids=lambda c: c.name)
+def test_mixed_precision_tracks_fp64(case):
+    ref, mp, subs = run_pair(case, 20)
+    for s_r, s_m, dt_r, dt_m in subs:
+        assert abs(s_r - s_m) <= 1
+        assert abs(dt_m / dt_r - 1) < 1e-5
+    errs = {}
+    for name in ("Position", "Velocity", "Density"):
+        errs[name] = rel_err(mp.fp64.water_block.download(name), ref.water_block.download(name))
+    # pressure error relative to the pressure scale rho0 c0^2 * max |rho/rho0 - 1|
+    p_m = mp.fp64.water_block.download("Pressure")
+    p_r = ref.water_block.download("Pressure")
+    errs["Pressure"] = rel_err(p_m, p_r)
+    print(case.name, errs)
+    assert errs["Position"] < 1e-6, errs
+    assert errs["Velocity"] < MP_RTOL, errs
+    assert errs["Density"] < 1e-6, errs
+    assert errs["Pressure"] < 1e-3, errs
+    cons = mp.conservation()
+    m_ref = ref.water_block.download("Mass").sum()
+    assert abs(cons[0] / m_ref - 1) < 1e-6
+    assert abs(cons[4] / ref.mechanical_energy.exec() - 1) < 1e-5
+
+
+def test_strategies_and_block_sizes_bitwise_equal():
+    case = cases.dambreak_2d()
+    outs = []
+    for block, strategy in ((128, 0), (64, 0), (256, 1), (96, 1)):
+        mp = MixedPrecisionDamBreak(case, block=block, strategy=strategy)
+        for _ in range(5):
+            mp.advection_step()
+        mp.sync_fp64()
+        outs.append([mp.fp64.water_block.download(n) for n in ("Position", "Velocity", "Density")])
+    for other in outs[1:]:
+        for a, b in zip(outs[0], other):
+            assert np.array_equal(a, b)
+
+
+def test_mixed_precision_upper_front_and_probe():
+    case = cases.dambreak_2d()
+    ref, mp, _ = run_pair(case, 10)
+    lo, up = (1.5, -1.0), (2.5, 6.0)
+    from sphinxsys_gb300 import sph as S
+    f_ref = S.UpperFrontInAxisDirection(ref.water_block, lo, up, 1).exec()
+    f_mp = mp.upper_front(1, lo, up)
+    assert abs(f_mp - f_ref) < 1e-6
+    ref.water_block.updateCellLinkedList()
+    ref.fluid_observer_contact.updateConfiguration()
+    assert np.allclose(mp.observe_pressure(), ref.recorded_pressure.exec(), rtol=1e-3, atol=1e-6)
