@@ -984,7 +984,7 @@ extern "C" int sphx_mp_create(sphx_relation inner, sphx_relation wall, const sph
     if (fb->find("ForcePrior") && host_copy(fb, "ForcePrior", fprior) == SPHX_OK)
         for (size_t i = 0; i < fb->n; ++i)
             for (int d = 0; d < D; ++d)
-                if (std::abs(fprior[i * D + d] - mass[i] * gravity[d]) > 1e-12 * std::abs(mass[i]) * 10)
+                if (std::abs(fprior[size_t(d) * fb->n + i] - mass[i] * gravity[d]) > 1e-11 * std::abs(mass[i]))
                     return fail(SPHX_ERR_INVALID_ARG, "mixed precision needs gravity as the only prior force");
 
     sphx_mp mp = new sphx_mp_s();
