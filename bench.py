@@ -365,6 +365,7 @@ def main():
         except (OSError, ValueError):
             pass
 
+    n_wall = sim.wall_boundary.n
     del sim
     mixed = None
     if not args.no_mixed:
@@ -382,7 +383,7 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic dam-break lattice",
-            "config": {"workload": case.name, "n_fluid": n_fluid, "n_wall": sim.wall_boundary.n, "dp": args.dp,
+            "config": {"workload": case.name, "n_fluid": n_fluid, "n_wall": n_wall, "dp": args.dp,
                        "precision": "fp64", "acoustic_substeps": subs, "l2": "inputs larger than L2",
                        "parallelism": f"replicas{world}"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),

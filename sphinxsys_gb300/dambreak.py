@@ -137,7 +137,8 @@ class MixedPrecisionDamBreak:
         self._g = g
         h = C.c_void_p()
         N.call("sphx_mp_create", sim.water_block_inner.handle, sim.water_wall_contact.handle,
-               C.byref(sim.fluid_pressure_relaxation.params), g.ctypes.data_as(C.POINTER(C.c_double)), C.byref(h))
+               C.byref(sim.fluid_advection_time_step.params), g.ctypes.data_as(C.POINTER(C.c_double)),
+               C.byref(h))
         self.handle = h
         self.set_tuning(block, strategy)
         self.physical_time = 0.0
