@@ -113,6 +113,19 @@ int sphx_cell_list_download(sphx_cell_list cl, uint32_t *cell_offset, uint32_t *
  * algorithm_primitive_sycl.h:96-122): device u32 exclusive prefix sum of n entries,
  * returns the total through *total (synchronises). */
 int sphx_exclusive_scan_u32(sphx_ctx ctx, const uint32_t *d_in, uint32_t *d_out, size_t n, uint32_t *total);
+/* The same scan for callers that cannot allocate device memory while they run (their
+ * device memory belongs to another allocator, or their loop must not pay the device-wide
+ * synchronisation of cudaMalloc / cudaFree).  It has no counterpart in the reference.
+ * Needs no context: enqueues on `stream` (0 = the legacy default stream) of the current
+ * device, and calls no cudaMalloc, cudaFree or other allocating routine; its scratch is a
+ * fixed 128 KiB device array of the library that every GPU loading the library holds until
+ * the process exits.  At most SPHX_SCAN_NOALLOC_MAX_N entries (larger n returns
+ * SPHX_ERR_INVALID_ARG).  The first call on a device looks up the array's address and
+ * should come before any stream capture.  Calls share the array: calls that overlap on the
+ * GPU race, so serialise them on one stream.  With `total` non-null the call synchronises
+ * `stream` to return the sum of all n inputs. */
+#define SPHX_SCAN_NOALLOC_MAX_N 67108864u
+int sphx_exclusive_scan_u32_noalloc(void *stream, const uint32_t *d_in, uint32_t *d_out, size_t n, uint32_t *total);
 
 /* ------------------------------------------------------------------ relations
  * InnerRelation (src/shared/body_relations/inner_body_relation.cpp:10-20) and

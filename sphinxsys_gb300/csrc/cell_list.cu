@@ -7,6 +7,7 @@
 // (src/shared/meshes/base_mesh.hxx:9-26,68-99), ParticleSorting
 // (src/shared/particle_dynamics/configuration_dynamics/particle_sorting.cpp:25-58).
 #include <algorithm>
+#include <mutex>
 
 #include "sphx_device.cuh"
 #include "sphx_internal.cuh"
@@ -547,5 +548,89 @@ extern "C" int sphx_particle_sorting(sphx_body body, const sphx_mesh_desc *mesh)
     SPHX_CUDA(cudaFreeAsync(buf, s));
     SPHX_CUDA(cudaFreeAsync(tmp, s));
     SPHX_CUDA(cudaStreamSynchronize(s));
+    return SPHX_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Exclusive scan that allocates nothing.
+//
+// Some callers cannot allocate device memory while they run: an application whose device
+// memory belongs to another allocator (a framework's caching pool that has reserved the
+// GPU and forbids allocations behind its back), or a time-stepping loop that must not pay
+// the implicit device-wide synchronisation of cudaMalloc / cudaFree.  This entry point
+// computes the same result as sphx_exclusive_scan_u32 with its per-tile partial sums in a
+// fixed device array of this library instead of the context's growable scratch buffer.
+//
+// The array is a file-scope __device__ variable: every GPU that loads the library holds
+// it (kNoAllocScanMaxTiles + 1 words, 128 KiB) until the process exits.  Host code cannot
+// use the array's name as a device address, so the first call on each device looks the
+// address up with cudaGetSymbolAddress (with that device current) and caches it; make that
+// first call before any stream capture.  All calls share the one array and it keeps the
+// last call's contents; every word a call reads is written earlier in the same call, so
+// nothing has to be cleared first.  Calls whose work overlaps on the GPU (two streams,
+// or two host threads at once) race on the array: serialise them on one stream.
+constexpr size_t kNoAllocScanMaxTiles = 32768;
+constexpr size_t kNoAllocScanMaxN = kNoAllocScanMaxTiles * kScanTile; // 67,108,864 entries
+
+static __device__ __align__(256) uint32_t g_noalloc_scan_scratch[kNoAllocScanMaxTiles + 1];
+
+namespace
+{
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+uint32_t *g_noalloc_scratch_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on the current device (looked up once per device).
+int noalloc_scratch(uint32_t **out)
+{
+    int device = -1;
+    SPHX_CUDA(cudaGetDevice(&device));
+    if (device < 0 || device >= kNoAllocMaxDevices)
+        return fail(SPHX_ERR_INVALID_ARG, "device %d beyond the %d devices the scratch table covers", device,
+                    kNoAllocMaxDevices);
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_scratch_ptr[device])
+    {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scan_scratch);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scan_scratch)", __FILE__, __LINE__);
+        g_noalloc_scratch_ptr[device] = static_cast<uint32_t *>(p);
+    }
+    *out = g_noalloc_scratch_ptr[device];
+    return SPHX_OK;
+}
+} // namespace
+
+extern "C" int sphx_exclusive_scan_u32_noalloc(void *stream, const uint32_t *d_in, uint32_t *d_out, size_t n,
+                                               uint32_t *total)
+{
+    if (n > 0 && (!d_in || !d_out))
+        return fail(SPHX_ERR_INVALID_ARG, "null device buffer");
+    if (n > kNoAllocScanMaxN)
+        return fail(SPHX_ERR_INVALID_ARG,
+                    "sphx_exclusive_scan_u32_noalloc scans at most %zu entries (fixed scratch); got %zu",
+                    kNoAllocScanMaxN, n);
+    if (n == 0)
+    {
+        if (total)
+            *total = 0;
+        return SPHX_OK;
+    }
+    uint32_t *tiles = nullptr;
+    SPHX_TRY(noalloc_scratch(&tiles));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    size_t ntiles = (n + kScanTile - 1) / kScanTile;
+    k_scan_tile_sums<<<unsigned(ntiles), kBlock, 0, s>>>(d_in, n, tiles);
+    SPHX_CUDA(cudaGetLastError());
+    k_scan_tile_prefix<<<1, 1024, 0, s>>>(tiles, ntiles, tiles + ntiles);
+    SPHX_CUDA(cudaGetLastError());
+    k_scan_apply<<<unsigned(ntiles), kBlock, 0, s>>>(d_in, d_out, n, tiles);
+    SPHX_CUDA(cudaGetLastError());
+    if (total)
+    {
+        SPHX_CUDA(cudaMemcpyAsync(total, tiles + ntiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        SPHX_CUDA(cudaStreamSynchronize(s));
+    }
     return SPHX_OK;
 }

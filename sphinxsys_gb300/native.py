@@ -60,6 +60,7 @@ SIGNATURES = {
     "sphx_cell_list_num_cells": (_i, [_vp, _psz]),
     "sphx_cell_list_download": (_i, [_vp, _pu32, _pu32, _sz]),
     "sphx_exclusive_scan_u32": (_i, [_vp, _vp, _vp, _sz, _pu32]),
+    "sphx_exclusive_scan_u32_noalloc": (_i, [_vp, _vp, _vp, _sz, _pu32]),
     "sphx_inner_relation_create": (_i, [_vp, _vp, _d, _pvp]),
     "sphx_contact_relation_create": (_i, [_vp, _vp, _vp, _d, _i, _d, _pvp]),
     "sphx_relation_destroy": (_i, [_vp]),
