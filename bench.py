@@ -1,17 +1,22 @@
 """Benchmark: particle-steps/s of the weakly-compressible dam-break step on one GB300.
 
-Workload (default): the 3D dam break of a 3.2 x 1.0 x 1.8 tank with a 1.2 x 1.0 x 0.6
-water block, dp = 0.0075 (1,702,400 fluid particles, 4 wall layers), FP64, the
-Dambreak.cpp loop.  One bench step is one advection step: advection dt, density
-summation, the acoustic sub-steps (1st + 2nd half each), the Morton re-sort every 100
-steps, the cell-list rebuild and the configuration update.  particle-steps/s counts
-fluid particles x acoustic sub-steps.
+Headline workload: the 3D dam break of a 3.2 x 1.0 x 1.8 tank with a 1.2 x 1.0 x 0.6
+water block at dp = 0.006 (3,340,000 fluid particles, 2,456,600 wall particles), advanced
+by the mixed-precision solver (FP32 pair arithmetic with compensated sums, FP64 position
+integration, dt reductions and conservation sums), timed beside the FP64 path on the same
+case from the same initial state, with the field / probe / free-surface errors of mixed
+against FP64.  The FP64 drop-in is also measured on dp = 0.0075 (1,702,400 fluid
+particles) through the reference-shaped API (``fp64_drop_in``).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--dp DP]
+One bench step is one advection step of the Dambreak.cpp loop: advection dt, density
+summation, the acoustic sub-steps (1st + 2nd half each) and the cell-list / configuration
+update.  particle-steps/s = fluid particles x acoustic sub-steps / time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Under torchrun each rank advances its own dam break (replicas, weak scaling).
 `--impl reference` times the FP64 CPU restatement of the reference (the oracle, OpenMP
-over all host cores) on the same workload.
+over all host cores) on the headline case; it never touches a GPU.
 """
 from __future__ import annotations
 
@@ -85,59 +90,77 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def algorithmic_bytes_2nd_half(n_fluid: int, n_wall_active: int, nnz: int) -> int:
+def hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_of(key):
+    """ncu DRAM bytes per launch recorded under profiles/traffic.json, if any."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get(key)
+    except (OSError, ValueError):
+        return None
+
+
+def bytes_fp64_second(n_fluid: int, n_wall_active: int, nnz: int) -> int:
     """Integration2ndHalf, FP64 3D: 136 B per fluid particle (read x, v, rho, drho, Vol;
-    write x, rho, drho, F), 80 B per active wall particle (x, V, v_ave, n) and 4 B per
-    stored neighbour index."""
+    write x, rho, drho, F), 80 B per active wall particle (x, V, v_ave, n), 4 B per stored
+    neighbour index."""
     return 136 * n_fluid + 80 * n_wall_active + 4 * nnz
 
 
-def algorithmic_bytes_mp_second(n_fluid: int, n_wall_active: int, nnz: int) -> int:
-    """Mixed-precision 2nd half, 3D: per fluid particle read cell+off0 (16), vel (12),
-    off (12), drho (4), drho_dt (4) and write off (12), drho (4), drho_dt (4), force (12)
-    = 80 B; per active wall particle cell+off (16) and normal (12) = 28 B; 4 B per stored
-    neighbour index."""
-    return 80 * n_fluid + 28 * n_wall_active + 4 * nnz
+def bytes_mp_second(n_fluid: int, n_wall_active: int, nnz: int) -> int:
+    """Mixed 2nd half, 3D: per fluid particle read geo0 (16), dyn (16), off (12), drho (4),
+    drho_dt (4), write off (12), drho (4), drho_dt (4), force (12) = 84 B; per active wall
+    particle geo (16) and normal (16) = 32 B; 4 B per stored neighbour index."""
+    return 84 * n_fluid + 32 * n_wall_active + 4 * nnz
 
 
-def mixed_precision_leg(args, torch, local):
-    """FP64 and mixed precision on the same case (default dp = 0.006, 3,340,000 fluid
-    particles) from the same initial state: particle-steps/s of both, the sweep-kernel
-    roofline of the mixed solver, and the field / probe errors of mixed against FP64."""
+def timed_steps(torch, ctx, step_fn, steps, warmup, sampler=None):
+    ext = torch.cuda.ExternalStream(ctx.stream())
+    for _ in range(warmup):
+        step_fn()
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    launches0 = ctx.launch_count()
+    if sampler:
+        sampler.start()
+    with torch.cuda.stream(ext):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+    subs = 0
+    for _ in range(steps):
+        subs += step_fn()[0]
+    with torch.cuda.stream(ext):
+        b.record()
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    clocks = sampler.stop() if sampler else None
+    return a.elapsed_time(b) / 1e3, subs, ctx.launch_count() - launches0, clocks
+
+
+def mixed_leg(args, torch, local, world):
     from sphinxsys_gb300 import cases
+    from sphinxsys_gb300 import sph as S
     from sphinxsys_gb300.dambreak import MixedPrecisionDamBreak
     case = cases.dambreak_3d(args.mp_dp)
     mp = MixedPrecisionDamBreak(case, device=local)
-    ref = mp.fp64  # the FP64 set-up doubles as the FP64 reference run
+    ref = mp.fp64  # the FP64 set-up is also the FP64 reference run (same initial state)
     n = ref.water_block.n
-    ext = torch.cuda.ExternalStream(mp.ctx.stream())
-    steps, warm = args.mp_steps, args.warmup
-
-    def timed(step_fn):
-        for _ in range(warm):
-            step_fn()
-        mp.ctx.synchronize()
-        with torch.cuda.stream(ext):
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record()
-        subs = 0
-        for _ in range(steps):
-            subs += step_fn()[0]
-        with torch.cuda.stream(ext):
-            b.record()
-        mp.ctx.synchronize()
-        torch.cuda.synchronize()
-        return a.elapsed_time(b) / 1e3, subs
-
+    tuned = mp.autotune(reps=2) if args.autotune else None
     mp.set_profiling(True)
-    l0 = mp.ctx.launch_count()
-    mp_el, mp_subs = timed(mp.advection_step)
-    mp_launches = mp.ctx.launch_count() - l0
+    el, subs, launches, clocks = timed_steps(torch, mp.ctx, mp.advection_step, args.steps, args.warmup,
+                                             ClockSampler(local))
     t1, t2, nsweeps = mp.kernel_times()
     sizes = mp.list_sizes()
     mp.set_profiling(False)
-    fp_el, fp_subs = timed(lambda: ref.advection_step()[:2])
+    fp_el, fp_subs, _, _ = timed_steps(torch, mp.ctx, lambda: ref.advection_step()[:2], args.steps, args.warmup)
     # errors of mixed against FP64 after the same advection steps from the same start
     errs = {}
     for name in ("Position", "Velocity", "Density", "Pressure"):
@@ -147,39 +170,102 @@ def mixed_precision_leg(args, torch, local):
     p_mp = mp.observe_pressure_view()
     p_fp = ref.recorded_pressure.exec()
     vert = case.vertical_axis
-    lo = [case.sys_lower[0], case.sys_lower[1], case.sys_lower[2]]
-    up = [case.sys_upper[0], case.sys_upper[1], case.sys_upper[2]]
-    lo[0], up[0] = case.inner_center[0] + case.inner_halfsize[0] - 0.2, case.inner_center[0] + case.inner_halfsize[0]
+    lo = list(case.sys_lower)
+    up = list(case.sys_upper)
+    lo[0], up[0] = case.water_center[0] - case.water_halfsize[0], case.water_center[0] + case.water_halfsize[0]
     h_mp = mp.upper_front(vert, lo, up)
-    from sphinxsys_gb300 import sph as S
     h_fp = S.UpperFrontInAxisDirection(ref.water_block, lo, up, vert).exec()
-    hbm = _hbm_peak()[0]
     n_wall_active = int(np.unique(ref.water_wall_contact.neighbors()["j"]).size)
-    alg = algorithmic_bytes_mp_second(n, n_wall_active, sizes["nnz_inner"] + sizes["nnz_wall"])
+    hbm, src = hbm_peak()
+    alg = bytes_mp_second(n, n_wall_active, sizes["nnz_inner"] + sizes["nnz_wall"])
     achieved = alg / (t2 / 1e3) / 1e9
-    return {
-        "workload": case.name, "n_fluid": n, "steps": steps, "dtype": "f32 pairs + f64 integration",
-        "value": n * mp_subs / mp_el, "ms_per_step": 1e3 * mp_el / steps, "acoustic_substeps": mp_subs,
-        "fp64_value_same_case": n * fp_subs / fp_el, "fp64_ms_per_step": 1e3 * fp_el / steps,
-        "speedup_vs_fp64": (n * mp_subs / mp_el) / (n * fp_subs / fp_el), "gpu_launches": int(mp_launches),
-        "roofline": {"bound": "hbm", "kernel": "k_mp_second<3,true>", "achieved": achieved, "peak": hbm,
-                     "unit": "GB/s", "frac": achieved / hbm, "algorithmic_bytes": alg, "kernel_ms": t2,
-                     "first_half_ms": t1, "sweeps_timed": nsweeps},
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "traffic": traffic_of("k_mp_second"), "kernel": "k_mp_second<3,lists>", "algorithmic_bytes": alg,
+                "kernel_ms": t2, "first_half_ms": t1, "sweeps_timed": nsweeps, "peak_source": src}
+    # end to end through the public API: host FP64 state in, one advection step, state out
+    e2e = None
+    if args.e2e_steps > 0:
+        body = ref.water_block
+        names = ("Position", "Velocity", "Force", "Density", "DensityChangeRate")
+        host = {nm: mp.fp64_view(nm) for nm in names}
+        h2d = sum(a.nbytes for a in host.values())
+        mp.ctx.synchronize()
+        t0 = time.perf_counter()
+        esubs, d2h = 0, 0
+        for _ in range(args.e2e_steps):
+            for nm in names:
+                body.upload(nm, host[nm])
+            mp.upload(body)
+            s, _ = mp.advection_step()
+            esubs += s
+            mp.download(body)
+            d2h = 0
+            for nm in ("Position", "Velocity", "Density", "Pressure"):
+                arr = body.download(nm)
+                d2h += arr.nbytes
+                if nm in host:
+                    host[nm] = arr
+        e_el = time.perf_counter() - t0
+        e2e = {"value": n * esubs / e_el * world, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h)}
+    out = {
+        "case": case, "n": n, "n_wall": ref.wall_boundary.n, "elapsed": el, "subs": subs, "launches": launches,
+        "clocks": clocks, "roofline": roofline, "e2e": e2e, "tuning": tuned,
+        "fp64_same_case": {"value": n * fp_subs / fp_el, "ms_per_step": 1e3 * fp_el / args.steps,
+                           "acoustic_substeps": fp_subs},
+        "speedup_vs_fp64": (n * subs / el) / (n * fp_subs / fp_el),
         "errors_vs_fp64": {"fields_max_rel": errs, "probe_pressure": [float(x) for x in p_mp],
-                           "probe_pressure_fp64": [float(x) for x in p_fp],
-                           "free_surface_height": h_mp, "free_surface_height_fp64": h_fp,
-                           "free_surface_rel_err": abs(h_mp - h_fp) / abs(h_fp)},
+                           "probe_pressure_fp64": [float(x) for x in p_fp], "free_surface_height": h_mp,
+                           "free_surface_height_fp64": h_fp,
+                           "free_surface_rel_err": abs(h_mp - h_fp) / max(abs(h_fp), 1e-300)},
         "lists": sizes,
     }
+    del mp, ref
+    return out
 
 
-def _hbm_peak():
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-        return float(peaks["hbm_gbs"]), "measured"
-    except (OSError, KeyError, ValueError):
-        return 6800.0, "fallback"
+def fp64_leg(args, torch, local):
+    """The FP64 drop-in (reference-shaped calls) on dp = args.dp; per-launch CUDA events
+    around every 2nd-half call inside the timed region give the roofline kernel time."""
+    from sphinxsys_gb300 import cases
+    from sphinxsys_gb300.dambreak import DamBreak
+    case = cases.dambreak_3d(args.dp)
+    sim = DamBreak(case, device=local)
+    n = sim.water_block.n
+    ext = torch.cuda.ExternalStream(sim.ctx.stream())
+    for _ in range(args.warmup):
+        sim.advection_step()
+    wn = sim.water_wall_contact.neighbors()
+    n_wall_active = int(np.unique(wn["j"]).size)
+    nnz = int(sim.water_block_inner.neighbors()["counts"].sum()) + int(wn["counts"].sum())
+    events = []
+    orig = sim.fluid_density_relaxation.exec
+
+    def timed_exec(dt=0.0):
+        with torch.cuda.stream(ext):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            orig(dt)
+            b.record()
+        events.append((a, b))
+
+    sim.fluid_density_relaxation.exec = timed_exec
+    el, subs, launches, _ = timed_steps(torch, sim.ctx, lambda: sim.advection_step()[:2], args.fp64_steps, 0)
+    sim.fluid_density_relaxation.exec = orig
+    k_ms = sum(a.elapsed_time(b) for a, b in events) / max(len(events), 1)
+    hbm, src = hbm_peak()
+    alg = bytes_fp64_second(n, n_wall_active, nnz)
+    achieved = alg / (k_ms / 1e3) / 1e9
+    out = {"workload": case.name, "n_fluid": n, "dtype": "f64", "value": n * subs / el,
+           "ms_per_step": 1e3 * el / args.fp64_steps, "steps": args.fp64_steps, "acoustic_substeps": subs,
+           "gpu_launches": int(launches),
+           "roofline": {"bound": "fp64 pipe (reported against hbm)", "achieved": achieved, "peak": hbm,
+                        "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic_of("k_interact_2nd"),
+                        "kernel": "k_interact_2nd<3>", "algorithmic_bytes": alg, "kernel_ms": k_ms,
+                        "peak_source": src}}
+    del sim
+    return out
 
 
 def run_cpu_sample(case, threads: int):
@@ -194,11 +280,12 @@ def run_cpu_sample(case, threads: int):
 
 
 def reference_arm(args, rank, world):
+    """The reference's CPU path: the FP64 oracle over all host cores on the headline case."""
     from sphinxsys_gb300 import cases
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    case = cases.dambreak_3d(args.dp)
+    case = cases.dambreak_3d(args.mp_dp)
     from oracle import oracle as O
     O.set_num_threads(threads)
     oc = O.OracleCase(case)
@@ -216,7 +303,7 @@ def reference_arm(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * el / max(args.steps, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic dam-break lattice",
-        "config": {"workload": case.name, "n_fluid": n, "dp": args.dp, "precision": "fp64"},
+        "config": {"workload": case.name, "n_fluid": n, "dp": args.mp_dp},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} advection steps ({subs} acoustic sub-steps) of {case.name}"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -230,13 +317,14 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--dp", type=float, default=0.0075)
+    ap.add_argument("--mp-dp", type=float, default=0.006, help="headline (mixed-precision) case spacing")
+    ap.add_argument("--dp", type=float, default=0.0075, help="FP64 drop-in case spacing")
+    ap.add_argument("--fp64-steps", type=int, default=5)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mp-dp", type=float, default=0.006)
-    ap.add_argument("--mp-steps", type=int, default=5)
-    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--autotune", type=int, default=1)
     args = ap.parse_args()
     rank, world, local = dist_info()
 
@@ -248,146 +336,45 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist.barrier()
     torch.cuda.set_device(local)
 
-    from sphinxsys_gb300 import cases
-    from sphinxsys_gb300.dambreak import DamBreak
-
-    case = cases.dambreak_3d(args.dp)
-    sim = DamBreak(case, device=local)
-    n_fluid = sim.water_block.n
-    ext = torch.cuda.ExternalStream(sim.ctx.stream())
-
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
-
-    for _ in range(args.warmup):
-        sim.advection_step()
-    # active wall particles and stored neighbour indices for the roofline bytes
-    wn = sim.water_wall_contact.neighbors()
-    n_wall_active = int(np.unique(wn["j"]).size)
-    nnz = int(sim.water_block_inner.neighbors()["counts"].sum()) + int(wn["counts"].sum())
-
-    # per-launch events around the 2nd half (dominant sweep) inside the timed region
-    k_events = []
-    orig_exec = sim.fluid_density_relaxation.exec
-
-    def timed_exec(dt=0.0):
-        with torch.cuda.stream(ext):
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record()
-            orig_exec(dt)
-            b.record()
-        k_events.append((a, b))
-
-    sim.fluid_density_relaxation.exec = timed_exec
-
-    sampler = ClockSampler(local)
-    barrier()
-    sim.ctx.synchronize()
-    torch.cuda.synchronize()
-    launches0 = sim.ctx.launch_count()
-    sampler.start()
-    with torch.cuda.stream(ext):
-        t_start = torch.cuda.Event(enable_timing=True)
-        t_end = torch.cuda.Event(enable_timing=True)
-        t_start.record()
-    subs = 0
-    for _ in range(args.steps):
-        s, _, _, _ = sim.advection_step()
-        subs += s
-    with torch.cuda.stream(ext):
-        t_end.record()
-    sim.ctx.synchronize()
-    torch.cuda.synchronize()
-    barrier()
-    clocks = sampler.stop()
-    launches = sim.ctx.launch_count() - launches0
-    elapsed = t_start.elapsed_time(t_end) / 1e3
-    sim.fluid_density_relaxation.exec = orig_exec
-    k_ms = [a.elapsed_time(b) for a, b in k_events]
-    k_avg = sum(k_ms) / len(k_ms) / 1e3 if k_ms else float("nan")
-
-    # aggregate over ranks: total particle-steps over the slowest rank's time
-    ps = float(n_fluid * subs)
+    mixed = mixed_leg(args, torch, local, world)
+    el = mixed["elapsed"]
+    ps = float(mixed["n"] * mixed["subs"])
     if world > 1:
         import torch.distributed as dist
-        t = torch.tensor([ps, elapsed], dtype=torch.float64, device="cuda")
-        tot = t.clone()
-        dist.all_reduce(tot[:1], op=dist.ReduceOp.SUM)
-        mx = t[1:].clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        ps, elapsed = float(tot[0]), float(mx[0])
-    value = ps / elapsed
-
-    # end to end through the public API: host state in, step, host state out
-    e2e = None
-    if args.e2e_steps > 0:
-        names = [("Position", 3), ("Velocity", 3), ("Force", 3), ("ForcePrior", 3), ("Density", 1),
-                 ("DensityChangeRate", 1), ("Mass", 1), ("VolumetricMeasure", 1)]
-        host = {nm: sim.water_block.download(nm) for nm, _ in names}
-        h2d = sum(a.nbytes for a in host.values())
-        d2h = 0
-        sim.ctx.synchronize()
-        t0 = time.perf_counter()
-        esubs = 0
-        for _ in range(args.e2e_steps):
-            for nm, _ in names:
-                sim.water_block.upload(nm, host[nm])
-            s, _, _, _ = sim.advection_step()
-            esubs += s
-            d2h = 0
-            for nm in ("Position", "Velocity", "Density", "Pressure"):
-                arr = sim.water_block.download(nm)
-                d2h += arr.nbytes
-                if nm in host:
-                    host[nm] = arr
-        e_el = time.perf_counter() - t0
-        e2e = {"value": n_fluid * esubs / e_el * world, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h)}
-
-    hbm, peak_source = _hbm_peak()
-    alg = algorithmic_bytes_2nd_half(n_fluid, n_wall_active, nnz)
-    achieved = alg / k_avg / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "traffic": None, "kernel": "k_interact_2nd<3>", "algorithmic_bytes": alg,
-                "kernel_ms": k_avg * 1e3, "peak_source": peak_source}
-    prof = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(prof):
-        try:
-            with open(prof) as f:
-                tr = json.load(f).get(f"dambreak3d_dp{args.dp}")
-            if tr:
-                roofline["traffic"] = tr
-        except (OSError, ValueError):
-            pass
-
-    n_wall = sim.wall_boundary.n
-    del sim
-    mixed = None
-    if not args.no_mixed:
-        mixed = mixed_precision_leg(args, torch, local)
+        t = torch.tensor([ps], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        m = torch.tensor([el], dtype=torch.float64, device="cuda")
+        dist.all_reduce(m, op=dist.ReduceOp.MAX)
+        ps, el = float(t[0]), float(m[0])
+    fp64 = None if args.no_fp64 else fp64_leg(args, torch, local)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
+        from sphinxsys_gb300 import cases
         threads = args.cpu_threads or (os.cpu_count() or 1)
-        v, sub, dt = run_cpu_sample(case, threads)
+        v, sub, dt = run_cpu_sample(cases.dambreak_3d(args.mp_dp), threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"1 advection step ({sub} acoustic sub-steps, {dt:.1f} s) of {case.name}"}
+               "sample": f"1 advection step ({sub} acoustic sub-steps, {dt:.1f} s) of {mixed['case'].name}"}
 
     if rank == 0:
+        case = mixed["case"]
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic dam-break lattice",
-            "config": {"workload": case.name, "n_fluid": n_fluid, "n_wall": n_wall, "dp": args.dp,
-                       "precision": "fp64", "acoustic_substeps": subs, "l2": "inputs larger than L2",
-                       "parallelism": f"replicas{world}"},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-            "clocks": clocks, "mixed_precision": mixed,
+            "metric": METRIC, "value": ps / el, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 pairs / f64 integration",
+            "data": "synthetic dam-break lattice",
+            "config": {"workload": case.name, "n_fluid": mixed["n"], "n_wall": mixed["n_wall"], "dp": args.mp_dp,
+                       "precision": "mixed", "acoustic_substeps": mixed["subs"], "l2": "inputs larger than L2",
+                       "parallelism": f"replicas{world}", "tuning": mixed["tuning"]},
+            "roofline": mixed["roofline"], "cpu_baseline": cpu, "e2e": mixed["e2e"],
+            "gpu_launches": int(mixed["launches"]), "clocks": mixed["clocks"],
+            "mixed_precision": {"speedup_vs_fp64_same_case": mixed["speedup_vs_fp64"],
+                                "fp64_same_case": mixed["fp64_same_case"],
+                                "errors_vs_fp64": mixed["errors_vs_fp64"], "lists": mixed["lists"]},
+            "fp64_drop_in": fp64,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

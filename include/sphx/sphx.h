@@ -220,6 +220,10 @@ int sphx_mp_destroy(sphx_mp mp);
  * physical time after the step. */
 int sphx_mp_advection_step(sphx_mp mp, int loop_style, int *substeps, double *advection_dt,
                            double *physical_time);
+/* Reloads the solver from the FP64 fluid body (Position, Velocity, Force, Density,
+ * DensityChangeRate; any particle order): re-sorts, rebuilds the configuration and the
+ * time-step maxima.  Physical time and the last acoustic dt are kept (synchronises). */
+int sphx_mp_upload(sphx_mp mp, sphx_body fluid);
 /* Writes Position, Velocity, Density, Pressure, Force and DensityChangeRate back into the
  * FP64 fluid body, in the body's particle order (synchronises). */
 int sphx_mp_download(sphx_mp mp, sphx_body fluid);
@@ -233,6 +237,10 @@ int sphx_mp_upper_front(sphx_mp mp, int axis, const double *region_lower, const 
  * the sweep kernels, and 0 = stored neighbour index lists, 1 = cell sweep every
  * sub-step. */
 int sphx_mp_set_tuning(sphx_mp mp, int block, int strategy);
+/* Times one acoustic sub-step for every block size (64, 128, 256) and both neighbour
+ * strategies, restores the state it advanced, and keeps the fastest setting; outputs
+ * (any may be null) the chosen block, strategy and ms per sub-step. */
+int sphx_mp_autotune(sphx_mp mp, int reps, int *best_block, int *best_strategy, double *best_ms);
 /* CUDA-event timing of the two sweep kernels of every sub-step (on the context's
  * stream); switching it resets the totals. */
 int sphx_mp_set_profiling(sphx_mp mp, int on);

@@ -6,17 +6,21 @@
 // (fluid_integration.hpp:49-113,166-231), acoustic / advection time steps
 // (fluid_time_step.cpp:21-31,54-65) and the configuration update.
 //
-// Layout (cell order, re-sorted at every configuration update; SoA, FP32 unless noted):
-//   cell      uint32  packed integer cell coordinates (10 bits per axis)
-//   off       float3  current position minus the cell's lower corner
-//   off0      float3  the same at the last configuration update (kernel geometry)
-//   vel, force float3; drho = rho - rho0, drho_dt, p  float
-//   id        uint32  index of the particle in the FP64 body it came from
-// Pair arithmetic is FP32 with Kahan-compensated sums; the position half-steps, the
-// time-step reductions and the conservation sums are FP64.  Neighbour index lists
-// (ELL, slot-major) are rebuilt with the density summation at each configuration update;
-// the kernel geometry (W, dW, e) is recomputed per pair from off0, as the reference keeps
-// the configuration-time kernel values for the whole advection step.
+// Layout (cell order, re-sorted at every configuration update):
+//   geo0   float4  {offset from the cell's lower corner at the last configuration
+//                   update (x, y, z), packed integer cell coordinates (10 bits per axis)}
+//   dyn    float4  {velocity (x, y, z), pressure}
+//   off    float3  current offset from the same cell corner (SoA)
+//   force  float3 (SoA); drho = rho - rho0, drho_dt, drho_sum (density summation) float
+//   id     uint32  index of the particle in the FP64 body it came from
+// A neighbour's data is one 16-byte load: geo0 for the kernel geometry (both sweeps),
+// dyn for its pressure (1st half) or velocity (2nd half).  Pair arithmetic is FP32 with
+// compensated sums (plain partial sums over groups of 8 neighbours, Kahan-added); the
+// position half-steps, the time-step reductions and the conservation sums are FP64.
+// Neighbour index lists (ELL, slot-major) are rebuilt at each configuration update
+// together with the density summation's sums; the kernel geometry (W, dW, e) is
+// recomputed per pair from geo0, as the reference keeps the configuration-time kernel
+// values for the whole advection step.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -29,6 +33,8 @@ using namespace sphx;
 namespace
 {
 constexpr float kTinyF = 2.71051e-20f;
+constexpr int kGroup = 8;  // neighbours per plain partial sum
+constexpr int kUnroll = 4; // neighbour records in flight per thread in the list sweeps
 
 struct Kahan
 {
@@ -41,6 +47,20 @@ struct Kahan
         s = t;
     }
     __device__ __forceinline__ float value() const { return s - c; }
+};
+
+// Compensated neighbour sum: plain FP32 partials over groups, Kahan across groups.
+struct Acc
+{
+    float part = 0.f;
+    Kahan k;
+    __device__ __forceinline__ void add(float x) { part += x; }
+    __device__ __forceinline__ void flush()
+    {
+        k.add(part);
+        part = 0.f;
+    }
+    __device__ __forceinline__ float value() const { return k.value(); }
 };
 
 __host__ __device__ __forceinline__ uint32_t pack_cell(int cx, int cy, int cz)
@@ -75,15 +95,14 @@ struct MPConst
 
 struct MPFluid
 {
-    uint32_t *cell;
-    float *off, *off0, *vel, *force, *drho, *drho_dt, *p;
+    float4 *geo0, *dyn;
+    float *off, *force, *drho, *drho_dt, *drho_sum;
     uint32_t *id;
 };
 
 struct MPWall
 {
-    uint32_t *cell;
-    float *off, *n;
+    float4 *geo, *n;
     size_t nw;
 };
 
@@ -95,14 +114,14 @@ struct MPLists
 
 // ---------------------------------------------------------------- geometry helpers
 template <int D>
-__device__ __forceinline__ void pair_dx(const MPConst &k, const int *ci, const float *oi, uint32_t cell_j,
-                                        const float *off_j, size_t stride, size_t j, float *dx)
+__device__ __forceinline__ void geo_dx(const MPConst &k, const int *ci, const float *oi, float4 gj, float *dx)
 {
     int cj[3];
-    unpack_cell(cell_j, cj);
-#pragma unroll
-    for (int d = 0; d < D; ++d)
-        dx[d] = float(ci[d] - cj[d]) * k.gs_f + (oi[d] - off_j[d * stride + j]);
+    unpack_cell(__float_as_uint(gj.w), cj);
+    dx[0] = float(ci[0] - cj[0]) * k.gs_f + (oi[0] - gj.x);
+    dx[1] = float(ci[1] - cj[1]) * k.gs_f + (oi[1] - gj.y);
+    if (D == 3)
+        dx[2] = float(ci[2] - cj[2]) * k.gs_f + (oi[2] - gj.z);
 }
 
 template <int D>
@@ -152,9 +171,9 @@ template <int D, class F>
 __device__ __forceinline__ void for_each_candidate(const MeshDev &m, const uint32_t *offset, const int *c, F &&f)
 {
     int lo0 = max(c[0] - 1, 0), hi0 = min(c[0] + 1, m.all_cells[0] - 1);
+    int lo1 = max(c[1] - 1, 0), hi1 = min(c[1] + 1, m.all_cells[1] - 1);
     if (D == 2)
     {
-        int lo1 = max(c[1] - 1, 0), hi1 = min(c[1] + 1, m.all_cells[1] - 1);
         for (int x = lo0; x <= hi0; ++x)
         {
             uint32_t a = uint32_t(x) * uint32_t(m.all_cells[1]);
@@ -165,7 +184,6 @@ __device__ __forceinline__ void for_each_candidate(const MeshDev &m, const uint3
     }
     else
     {
-        int lo1 = max(c[1] - 1, 0), hi1 = min(c[1] + 1, m.all_cells[1] - 1);
         int lo2 = max(c[2] - 1, 0), hi2 = min(c[2] + 1, m.all_cells[2] - 1);
         for (int x = lo0; x <= hi0; ++x)
             for (int y = lo1; y <= hi1; ++y)
@@ -205,7 +223,7 @@ __global__ void k_mp_from_fp64(size_t n, const double *__restrict__ pos, MeshDev
 
 // From the current (cell, offset) state: FP64 reconstruction of the position.
 template <int D>
-__global__ void k_mp_rehash(size_t n, const uint32_t *__restrict__ cell, const float *__restrict__ off, MeshDev m,
+__global__ void k_mp_rehash(size_t n, const float4 *__restrict__ geo0, const float *__restrict__ off, MeshDev m,
                             uint32_t *__restrict__ ncell, float *__restrict__ noff, uint32_t *__restrict__ key,
                             uint32_t *__restrict__ rank, uint32_t *__restrict__ count)
 {
@@ -213,7 +231,7 @@ __global__ void k_mp_rehash(size_t n, const uint32_t *__restrict__ cell, const f
     if (i >= n)
         return;
     int c0[3];
-    unpack_cell(cell[i], c0);
+    unpack_cell(__float_as_uint(geo0[i].w), c0);
     double x[3] = {0, 0, 0};
 #pragma unroll
     for (int d = 0; d < D; ++d)
@@ -267,22 +285,22 @@ __global__ void k_mp_gather(size_t n, const uint32_t *__restrict__ perm, const u
     if (k >= n)
         return;
     uint32_t i = perm[k];
-    dst.cell[k] = ncell[i];
+    float o[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int d = 0; d < D; ++d)
     {
-        float o = noff[d * n + i];
-        dst.off[d * n + k] = o;
-        dst.off0[d * n + k] = o;
-        dst.vel[d * n + k] = src.vel[d * n + i];
+        o[d] = noff[d * n + i];
+        dst.off[d * n + k] = o[d];
         dst.force[d * n + k] = src.force[d * n + i];
     }
+    dst.geo0[k] = make_float4(o[0], o[1], o[2], __uint_as_float(ncell[i]));
+    dst.dyn[k] = src.dyn[i];
     dst.drho[k] = src.drho[i];
     dst.drho_dt[k] = src.drho_dt[i];
     dst.id[k] = src.id[i];
 }
 
-// ---------------------------------------------------------------- configuration + density
+// ---------------------------------------------------------------- configuration + density sums
 template <int D>
 __global__ void __launch_bounds__(256)
     k_mp_build(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
@@ -291,19 +309,17 @@ __global__ void __launch_bounds__(256)
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
+    float4 gi = f.geo0[i];
     int ci[3] = {0, 0, 0};
-    unpack_cell(f.cell[i], ci);
-    float oi[3] = {0, 0, 0};
-#pragma unroll
-    for (int d = 0; d < D; ++d)
-        oi[d] = f.off0[d * n + i];
+    unpack_cell(__float_as_uint(gi.w), ci);
+    const float oi[3] = {gi.x, gi.y, gi.z};
     Kahan sigma;
     unsigned cnt = 0;
     for_each_candidate<D>(k.m, f_offset, ci, [&](uint32_t j) {
         if (j == uint32_t(i))
             return;
         float dx[3];
-        pair_dx<D>(k, ci, oi, f.cell[j], f.off0, n, j, dx);
+        geo_dx<D>(k, ci, oi, f.geo0[j], dx);
         float r2 = sq<D>(dx);
         if (!(r2 < k.rc_sqr))
             return;
@@ -316,7 +332,7 @@ __global__ void __launch_bounds__(256)
     unsigned wc = 0;
     for_each_candidate<D>(k.m, w_offset, ci, [&](uint32_t j) {
         float dx[3];
-        pair_dx<D>(k, ci, oi, w.cell[j], w.off, w.nw, j, dx);
+        geo_dx<D>(k, ci, oi, w.geo[j], dx);
         float r2 = sq<D>(dx);
         if (!(r2 < k.rc_sqr))
             return;
@@ -329,22 +345,30 @@ __global__ void __launch_bounds__(256)
     wl.count[i] = wc;
     atomicMax(&max_counts[0], cnt);
     atomicMax(&max_counts[1], wc);
-    // rho_sum - rho0 = rho0 (W0 + sum W - sigma0) / sigma0 + wall term; FreeSurface: max(., 0)
+    // rho_sum - rho0 = rho0 (W0 + sum W - sigma0) / sigma0 + wall term
     double dsig = (double(sigma.s) - k.sigma0) - double(sigma.c) + double(k.fW);
-    float drho = float(dsig) * k.rho0_over_sigma0 + wsig.value() * k.wall_factor;
-    f.drho[i] = fmaxf(drho, 0.0f);
+    f.drho_sum[i] = float(dsig) * k.rho0_over_sigma0 + wsig.value() * k.wall_factor;
+}
+
+// DensitySummation update with the FreeSurface rule rho = max(rho_sum, rho0), at the
+// start of the advection step as in the reference loop.
+__global__ void k_mp_density(size_t n, const float *__restrict__ drho_sum, float *__restrict__ drho)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n)
+        drho[i] = fmaxf(drho_sum[i], 0.0f);
 }
 
 // ---------------------------------------------------------------- acoustic sub-step
 __global__ void k_mp_init1(size_t n, float *__restrict__ drho, const float *__restrict__ drho_dt,
-                           float *__restrict__ p, float p0_over_rho0, float half_dt)
+                           float4 *__restrict__ dyn, float p0_over_rho0, float half_dt)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
     float r = drho[i] + drho_dt[i] * half_dt;
     drho[i] = r;
-    p[i] = p0_over_rho0 * r;
+    reinterpret_cast<float *>(dyn)[4 * i + 3] = p0_over_rho0 * r;
 }
 
 template <int D, bool LISTS>
@@ -357,43 +381,80 @@ __global__ void __launch_bounds__(256)
     double vmax = -1.0e300;
     if (i < n)
     {
+        const float4 gi = f.geo0[i];
         int ci[3] = {0, 0, 0};
-        unpack_cell(f.cell[i], ci);
-        float oi[3] = {0, 0, 0};
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-            oi[d] = f.off0[d * n + i];
-        const float p_i = f.p[i];
+        unpack_cell(__float_as_uint(gi.w), ci);
+        const float oi[3] = {gi.x, gi.y, gi.z};
+        const float4 di = f.dyn[i];
+        const float p_i = di.w;
         const float rho_i = k.rho0 + f.drho[i];
-        Kahan force[3], rdis;
-        auto inner = [&](uint32_t j) {
+        Acc force[3], rdis;
+        int g = 0;
+        auto inner_pair = [&](uint32_t j, float4 gj, float p_j) {
             float dx[3];
-            pair_dx<D>(k, ci, oi, f.cell[j], f.off0, n, j, dx);
+            geo_dx<D>(k, ci, oi, gj, dx);
             float r2 = sq<D>(dx);
             if (!LISTS && (!(r2 < k.rc_sqr) || j == uint32_t(i)))
                 return;
             float r = sqrtf(r2);
             float inv = 1.0f / (r + kTinyF);
             float dWV = wendland_dW(k, r) * k.Vol;
-            float p_j = f.p[j];
             float sc = (p_i + p_j) * dWV * inv;
 #pragma unroll
             for (int d = 0; d < D; ++d)
                 force[d].add(-sc * dx[d]);
-            rdis.add((p_i - p_j) * k.inv_z * dWV);
+            rdis.add((p_i - p_j) * dWV);
+            if (++g == kGroup)
+            {
+#pragma unroll
+                for (int d = 0; d < D; ++d)
+                    force[d].flush();
+                rdis.flush();
+                g = 0;
+            }
         };
+        auto inner = [&](uint32_t j) { inner_pair(j, f.geo0[j], f.dyn[j].w); };
         if (LISTS)
         {
-            unsigned c = min(in.count[i], in.cap);
-            for (unsigned s = 0; s < c; ++s)
-                inner(in.J[size_t(s) * n + i]);
+            // kUnroll neighbours' indices and 16-byte records are in flight before any
+            // arithmetic; the summation order is the list order either way
+            const unsigned c = min(in.count[i], in.cap);
+            unsigned s = 0;
+            for (; s + kUnroll <= c; s += kUnroll)
+            {
+                uint32_t jj[kUnroll];
+                float4 gg[kUnroll];
+                float pp[kUnroll];
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u)
+                    jj[u] = in.J[size_t(s + u) * n + i];
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u)
+                {
+                    gg[u] = __ldg(&f.geo0[jj[u]]);
+                    pp[u] = __ldg(&f.dyn[jj[u]].w);
+                }
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u)
+                    inner_pair(jj[u], gg[u], pp[u]);
+            }
+            for (; s < c; ++s)
+            {
+                uint32_t j = in.J[size_t(s) * n + i];
+                inner_pair(j, __ldg(&f.geo0[j]), __ldg(&f.dyn[j].w));
+            }
         }
         else
             for_each_candidate<D>(k.m, f_offset, ci, inner);
-        Kahan wforce[3], wrdis;
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            force[d].flush();
+        rdis.flush();
+        Acc wforce[3], wrdis;
+        g = 0;
         auto wall = [&](uint32_t j) {
             float dx[3];
-            pair_dx<D>(k, ci, oi, w.cell[j], w.off, w.nw, j, dx);
+            geo_dx<D>(k, ci, oi, w.geo[j], dx);
             float r2 = sq<D>(dx);
             if (!LISTS && !(r2 < k.rc_sqr))
                 return;
@@ -409,7 +470,15 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
             for (int d = 0; d < D; ++d)
                 wforce[d].add(-sc * dx[d]);
-            wrdis.add((p_i - p_w) * k.inv_z * dWV);
+            wrdis.add((p_i - p_w) * dWV);
+            if (++g == kGroup)
+            {
+#pragma unroll
+                for (int d = 0; d < D; ++d)
+                    wforce[d].flush();
+                wrdis.flush();
+                g = 0;
+            }
         };
         if (LISTS)
         {
@@ -419,21 +488,28 @@ __global__ void __launch_bounds__(256)
         }
         else
             for_each_candidate<D>(k.m, w_offset, ci, wall);
-        f.drho_dt[i] = rdis.value() * rho_i + wrdis.value() * rho_i;
-        double v2 = 0;
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            wforce[d].flush();
+        wrdis.flush();
+        f.drho_dt[i] = (rdis.value() * k.inv_z) * rho_i + (wrdis.value() * k.inv_z) * rho_i;
+        float v2 = 0.f;
+        float vn[3] = {di.x, di.y, di.z};
+        const float dt_f = float(dt);
 #pragma unroll
         for (int d = 0; d < D; ++d)
         {
             float F = f.force[d * n + i] + force[d].value() * k.Vol + wforce[d].value() * k.Vol;
             f.force[d * n + i] = F;
-            float v = f.vel[d * n + i];
+            float v = vn[d];
             // position half-step in FP64 (initialization of the 1st half, old velocity)
             f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(v));
-            double vn = double(v) + (k.gd[d] + double(F) * double(k.inv_mass)) * dt;
-            f.vel[d * n + i] = float(vn);
-            v2 += double(float(vn)) * double(float(vn));
+            vn[d] = v + (k.g[d] + F * k.inv_mass) * dt_f;
+            v2 += vn[d] * vn[d];
         }
-        vmax = k.c0 + sqrt(v2);
+        // same pressure as read by the neighbours of this sweep
+        f.dyn[i] = make_float4(vn[0], vn[1], D == 3 ? vn[2] : 0.f, p_i);
+        vmax = k.c0 + double(sqrtf(v2));
     }
     block_max_slot(ac_slot, vmax);
 }
@@ -448,72 +524,106 @@ __global__ void __launch_bounds__(256)
     double amax = -1.0e300;
     if (i < n)
     {
+        const float4 gi = f.geo0[i];
         int ci[3] = {0, 0, 0};
-        unpack_cell(f.cell[i], ci);
-        float oi[3] = {0, 0, 0}, vi[3] = {0, 0, 0};
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-        {
-            oi[d] = f.off0[d * n + i];
-            vi[d] = f.vel[d * n + i];
-        }
+        unpack_cell(__float_as_uint(gi.w), ci);
+        const float oi[3] = {gi.x, gi.y, gi.z};
+        const float4 di = f.dyn[i];
+        const float vi[3] = {di.x, di.y, di.z};
         const float rho_i = k.rho0 + f.drho[i];
-        Kahan rate, pdis[3];
-        auto inner = [&](uint32_t j) {
+        Acc rate, pdis[3];
+        int g = 0;
+        auto inner_pair = [&](uint32_t j, float4 gj, float4 dj) {
             float dx[3];
-            pair_dx<D>(k, ci, oi, f.cell[j], f.off0, n, j, dx);
+            geo_dx<D>(k, ci, oi, gj, dx);
             float r2 = sq<D>(dx);
             if (!LISTS && (!(r2 < k.rc_sqr) || j == uint32_t(i)))
                 return;
             float r = sqrtf(r2);
             float inv = 1.0f / (r + kTinyF);
             float dWV = wendland_dW(k, r) * k.Vol;
-            float u = 0.f;
-#pragma unroll
-            for (int d = 0; d < D; ++d)
-                u += (vi[d] - f.vel[d * n + j]) * (dx[d] * inv);
+            float u = (vi[0] - dj.x) * dx[0] + (vi[1] - dj.y) * dx[1];
+            if (D == 3)
+                u += (vi[2] - dj.z) * dx[2];
+            u *= inv;
             rate.add(u * dWV);
             float sc = p_jump(k, u) * dWV * inv;
 #pragma unroll
             for (int d = 0; d < D; ++d)
                 pdis[d].add(sc * dx[d]);
+            if (++g == kGroup)
+            {
+                rate.flush();
+#pragma unroll
+                for (int d = 0; d < D; ++d)
+                    pdis[d].flush();
+                g = 0;
+            }
         };
+        auto inner = [&](uint32_t j) { inner_pair(j, f.geo0[j], f.dyn[j]); };
         if (LISTS)
         {
-            unsigned c = min(in.count[i], in.cap);
-            for (unsigned s = 0; s < c; ++s)
-                inner(in.J[size_t(s) * n + i]);
+            const unsigned c = min(in.count[i], in.cap);
+            unsigned s = 0;
+            for (; s + kUnroll <= c; s += kUnroll)
+            {
+                uint32_t jj[kUnroll];
+                float4 gg[kUnroll], dd[kUnroll];
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u)
+                    jj[u] = in.J[size_t(s + u) * n + i];
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u)
+                {
+                    gg[u] = __ldg(&f.geo0[jj[u]]);
+                    dd[u] = __ldg(&f.dyn[jj[u]]);
+                }
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u)
+                    inner_pair(jj[u], gg[u], dd[u]);
+            }
+            for (; s < c; ++s)
+            {
+                uint32_t j = in.J[size_t(s) * n + i];
+                inner_pair(j, __ldg(&f.geo0[j]), __ldg(&f.dyn[j]));
+            }
         }
         else
             for_each_candidate<D>(k.m, f_offset, ci, inner);
-        Kahan wrate, wdis[3];
+        rate.flush();
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            pdis[d].flush();
+        Acc wrate, wdis[3];
+        g = 0;
         auto wall = [&](uint32_t j) {
             float dx[3];
-            pair_dx<D>(k, ci, oi, w.cell[j], w.off, w.nw, j, dx);
+            geo_dx<D>(k, ci, oi, w.geo[j], dx);
             float r2 = sq<D>(dx);
             if (!LISTS && !(r2 < k.rc_sqr))
                 return;
             float r = sqrtf(r2);
             float inv = 1.0f / (r + kTinyF);
             float dWV = wendland_dW(k, r) * k.wall_Vol;
-            float en = 0.f, ve = 0.f, vn = 0.f, nj[3];
-#pragma unroll
-            for (int d = 0; d < D; ++d)
-            {
-                nj[d] = w.n[d * w.nw + j];
-                float e = dx[d] * inv;
-                en += e * nj[d];
-                ve += vi[d] * e;
-            }
+            const float4 nj = w.n[j];
+            float en = (dx[0] * nj.x + dx[1] * nj.y + (D == 3 ? dx[2] * nj.z : 0.f)) * inv;
+            float ve = (vi[0] * dx[0] + vi[1] * dx[1] + (D == 3 ? vi[2] * dx[2] : 0.f)) * inv;
             float sgn = en < 0.f ? -1.f : (en > 0.f ? 1.f : 0.f);
-#pragma unroll
-            for (int d = 0; d < D; ++d)
-                vn += vi[d] * (sgn * nj[d]);
+            float vn = sgn * (vi[0] * nj.x + vi[1] * nj.y + (D == 3 ? vi[2] * nj.z : 0.f));
             wrate.add(2.0f * ve * dWV); // (v_i - (2 v_wall - v_i)) . e with a static wall
-            float sc = p_jump(k, 2.0f * vn) * dWV;
+            float sc = p_jump(k, 2.0f * vn) * dWV * sgn;
+            wdis[0].add(sc * nj.x);
+            wdis[1].add(sc * nj.y);
+            if (D == 3)
+                wdis[2].add(sc * nj.z);
+            if (++g == kGroup)
+            {
+                wrate.flush();
 #pragma unroll
-            for (int d = 0; d < D; ++d)
-                wdis[d].add(sc * (sgn * nj[d]));
+                for (int d = 0; d < D; ++d)
+                    wdis[d].flush();
+                g = 0;
+            }
         };
         if (LISTS)
         {
@@ -523,21 +633,25 @@ __global__ void __launch_bounds__(256)
         }
         else
             for_each_candidate<D>(k.m, w_offset, ci, wall);
+        wrate.flush();
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            wdis[d].flush();
         float drho_dt = f.drho_dt[i] + rate.value() * rho_i + wrate.value() * rho_i;
         f.drho_dt[i] = drho_dt;
         f.drho[i] = f.drho[i] + drho_dt * float(0.5 * dt);
-        double v2 = 0, a2 = 0;
+        float v2 = 0.f, a2 = 0.f;
 #pragma unroll
         for (int d = 0; d < D; ++d)
         {
             float F = pdis[d].value() * k.Vol + wdis[d].value() * k.Vol;
             f.force[d * n + i] = F;
             f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vi[d]));
-            v2 += double(vi[d]) * double(vi[d]);
-            double ft = double(F) + double(k.mass) * k.gd[d];
+            v2 += vi[d] * vi[d];
+            float ft = F + k.mass * k.g[d];
             a2 += ft * ft;
         }
-        amax = fmax(v2, 4.0 * k.h * sqrt(a2) * double(k.inv_mass));
+        amax = double(fmaxf(v2, 4.0f * float(k.h) * sqrtf(a2) * k.inv_mass));
     }
     block_max_slot(adv_slot, amax);
 }
@@ -550,12 +664,13 @@ __global__ void k_mp_initial_max(size_t n, MPConst k, MPFluid f, unsigned long l
     double am = -1.0e300, vm = -1.0e300;
     if (i < n)
     {
+        float4 di = f.dyn[i];
+        const float v[3] = {di.x, di.y, di.z};
         double v2 = 0, a2 = 0;
 #pragma unroll
         for (int d = 0; d < D; ++d)
         {
-            double v = f.vel[d * n + i];
-            v2 += v * v;
+            v2 += double(v[d]) * double(v[d]);
             double ft = double(f.force[d * n + i]) + double(k.mass) * k.gd[d];
             a2 += ft * ft;
         }
@@ -566,7 +681,39 @@ __global__ void k_mp_initial_max(size_t n, MPConst k, MPFluid f, unsigned long l
     block_max_slot(adv_slot, am);
 }
 
+// ---------------------------------------------------------------- FP64 body -> FP32 state
+struct ImportArgs
+{
+    const double *vel, *force, *rho, *drho_dt;
+    double rho0, c0_sqr;
+};
+
+template <int D>
+__global__ void k_mp_import(size_t n, ImportArgs a, MPFluid f)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    float v[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        v[d] = a.vel ? float(a.vel[d * n + i]) : 0.f;
+        f.force[d * n + i] = a.force ? float(a.force[d * n + i]) : 0.f;
+    }
+    float dr = float(a.rho[i] - a.rho0);
+    f.drho[i] = dr;
+    f.drho_dt[i] = a.drho_dt ? float(a.drho_dt[i]) : 0.f;
+    f.dyn[i] = make_float4(v[0], v[1], v[2], float(a.c0_sqr) * dr);
+    f.id[i] = uint32_t(i);
+}
+
 // ---------------------------------------------------------------- outputs
+__device__ __forceinline__ double position(const MPConst &k, const MPFluid &f, size_t n, size_t i, int d, const int *c)
+{
+    return cell_corner(k.m, d, c[d]) + double(f.off[d * n + i]);
+}
+
 template <int D>
 __global__ void k_mp_download(size_t n, MPConst k, MPFluid f, double *__restrict__ pos, double *__restrict__ vel,
                               double *__restrict__ rho, double *__restrict__ p, double *__restrict__ force,
@@ -577,16 +724,18 @@ __global__ void k_mp_download(size_t n, MPConst k, MPFluid f, double *__restrict
         return;
     uint32_t o = f.id[i];
     int c[3];
-    unpack_cell(f.cell[i], c);
+    unpack_cell(__float_as_uint(f.geo0[i].w), c);
+    float4 di = f.dyn[i];
+    const float v[3] = {di.x, di.y, di.z};
 #pragma unroll
     for (int d = 0; d < D; ++d)
     {
-        pos[d * n + o] = cell_corner(k.m, d, c[d]) + double(f.off[d * n + i]);
-        vel[d * n + o] = f.vel[d * n + i];
+        pos[d * n + o] = position(k, f, n, i, d, c);
+        vel[d * n + o] = v[d];
         force[d * n + o] = f.force[d * n + i];
     }
     rho[o] = double(k.rho0) + double(f.drho[i]);
-    p[o] = double(k.p0_over_rho0) * double(f.drho[i]);
+    p[o] = di.w; // pressure of the last 1st-half initialisation, as the FP64 body holds it
     drho_dt[o] = f.drho_dt[i];
 }
 
@@ -597,17 +746,18 @@ __global__ void k_mp_conservation(size_t n, MPConst k, MPFluid f, double *__rest
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
     {
         int c[3];
-        unpack_cell(f.cell[i], c);
+        unpack_cell(__float_as_uint(f.geo0[i].w), c);
+        float4 di = f.dyn[i];
+        const float vv[3] = {di.x, di.y, di.z};
         double m = k.mass, v2 = 0, gx = 0;
         s[0] += m;
 #pragma unroll
         for (int d = 0; d < D; ++d)
         {
-            double v = f.vel[d * n + i];
+            double v = vv[d];
             s[1 + d] += m * v;
             v2 += v * v;
-            double x = cell_corner(k.m, d, c[d]) + double(f.off[d * n + i]);
-            gx += k.gd[d] * (-x);
+            gx += k.gd[d] * (-position(k, f, n, i, d, c));
         }
         s[4] += 0.5 * m * v2 + m * gx;
     }
@@ -636,13 +786,13 @@ __global__ void k_mp_upper_front(size_t n, MPConst k, MPFluid f, int axis, doubl
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
     {
         int c[3];
-        unpack_cell(f.cell[i], c);
+        unpack_cell(__float_as_uint(f.geo0[i].w), c);
         double x[3];
         bool in = true;
 #pragma unroll
         for (int d = 0; d < D; ++d)
         {
-            x[d] = cell_corner(k.m, d, c[d]) + double(f.off[d * n + i]);
+            x[d] = position(k, f, n, i, d, c);
             in = in && !(x[d] < lo[d] || x[d] > up[d]);
         }
         if (in)
@@ -653,8 +803,8 @@ __global__ void k_mp_upper_front(size_t n, MPConst k, MPFluid f, int axis, doubl
 
 template <int D>
 __global__ void k_wall_load(size_t nw, const uint32_t *__restrict__ perm, const double *__restrict__ pos,
-                            const double *__restrict__ nrm, MeshDev m, uint32_t *__restrict__ cell,
-                            float *__restrict__ off, float *__restrict__ n_out)
+                            const double *__restrict__ nrm, MeshDev m, float4 *__restrict__ geo,
+                            float4 *__restrict__ n_out)
 {
     size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (k >= nw)
@@ -666,13 +816,15 @@ __global__ void k_wall_load(size_t nw, const uint32_t *__restrict__ perm, const 
         x[d] = pos[d * nw + i];
     int c[3] = {0, 0, 0};
     cell_index<D>(m, x, c);
-    cell[k] = pack_cell(c[0], c[1], c[2]);
+    float o[3] = {0.f, 0.f, 0.f}, nn[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int d = 0; d < D; ++d)
     {
-        off[d * nw + k] = float(x[d] - cell_corner(m, d, c[d]));
-        n_out[d * nw + k] = float(nrm[d * nw + i]);
+        o[d] = float(x[d] - cell_corner(m, d, c[d]));
+        nn[d] = float(nrm[d * nw + i]);
     }
+    geo[k] = make_float4(o[0], o[1], o[2], __uint_as_float(pack_cell(c[0], c[1], c[2])));
+    n_out[k] = make_float4(nn[0], nn[1], nn[2], 0.f);
 }
 
 template <int D>
@@ -715,7 +867,7 @@ struct sphx_mp_s
     uint32_t *key = nullptr, *rank = nullptr, *perm = nullptr, *ncell = nullptr;
     float *noff = nullptr;
     MPLists in{}, wl{};
-    unsigned long long *slots = nullptr; // 0 acoustic, 1 advection, 2 misc, 3..4 build counts
+    unsigned long long *slots = nullptr; // 0 acoustic, 1 advection, 2 misc, 3 build counts
     unsigned long long *h_slots = nullptr;
     double physical_time = 0, acoustic_dt = 0;
     int block = 128, strategy = 0;
@@ -740,16 +892,15 @@ namespace
 int alloc_state(sphx_mp mp, MPFluid &s)
 {
     size_t n = mp->n, D = size_t(mp->dim);
-    s.cell = mp->alloc<uint32_t>(n);
+    s.geo0 = mp->alloc<float4>(n);
+    s.dyn = mp->alloc<float4>(n);
     s.off = mp->alloc<float>(D * n);
-    s.off0 = mp->alloc<float>(D * n);
-    s.vel = mp->alloc<float>(D * n);
     s.force = mp->alloc<float>(D * n);
     s.drho = mp->alloc<float>(n);
     s.drho_dt = mp->alloc<float>(n);
-    s.p = mp->alloc<float>(n);
+    s.drho_sum = mp->alloc<float>(n);
     s.id = mp->alloc<uint32_t>(n);
-    if (!s.cell || !s.off || !s.off0 || !s.vel || !s.force || !s.drho || !s.drho_dt || !s.p || !s.id)
+    if (!s.geo0 || !s.dyn || !s.off || !s.force || !s.drho || !s.drho_dt || !s.drho_sum || !s.id)
         return fail(SPHX_ERR_OUT_OF_MEMORY, "mixed-precision state allocation failed");
     return SPHX_OK;
 }
@@ -825,12 +976,14 @@ int configuration_update(sphx_mp mp, bool from_state)
     size_t n = mp->n;
     MeshDev m = mp->k.m;
     if (from_state)
-        SPHX_CUDA(cudaMemsetAsync(mp->count, 0, mp->ncells * sizeof(uint32_t), s));
-    if (n > 0 && from_state)
     {
-        k_mp_rehash<D><<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.cell, mp->a.off, m, mp->ncell, mp->noff, mp->key,
-                                                        mp->rank, mp->count);
-        SPHX_LAUNCHED(ctx);
+        SPHX_CUDA(cudaMemsetAsync(mp->count, 0, mp->ncells * sizeof(uint32_t), s));
+        if (n > 0)
+        {
+            k_mp_rehash<D><<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.geo0, mp->a.off, m, mp->ncell, mp->noff,
+                                                            mp->key, mp->rank, mp->count);
+            SPHX_LAUNCHED(ctx);
+        }
     }
     SPHX_TRY(sort_keys(mp, n, mp->f_offset));
     if (n > 0)
@@ -861,7 +1014,7 @@ int substep(sphx_mp mp, double dt)
     if (n == 0)
         return SPHX_OK;
     unsigned blk = unsigned(mp->block);
-    k_mp_init1<<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.drho, mp->a.drho_dt, mp->a.p, mp->k.p0_over_rho0,
+    k_mp_init1<<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.drho, mp->a.drho_dt, mp->a.dyn, mp->k.p0_over_rho0,
                                                 float(0.5 * dt));
     SPHX_LAUNCHED(ctx);
     SPHX_CUDA(cudaMemsetAsync(mp->slots, 0, 2 * sizeof(unsigned long long), s));
@@ -903,6 +1056,11 @@ int advection_step(sphx_mp mp, int loop_style, int *substeps, double *adv_dt)
     double adv_max;
     SPHX_TRY(read_slot(mp, 1, &adv_max));
     double Dt = mp->k.advection_cfl * mp->k.h / (std::max(std::sqrt(adv_max), mp->k.U_ref) + kTinyReal);
+    if (mp->n > 0)
+    {
+        k_mp_density<<<grid_for(mp->n, 256), 256, 0, mp->ctx->stream>>>(mp->n, mp->a.drho_sum, mp->a.drho);
+        SPHX_LAUNCHED(mp->ctx);
+    }
     double relaxation = 0, dt = mp->acoustic_dt;
     int count = 0;
     while (relaxation < Dt)
@@ -929,6 +1087,84 @@ int advection_step(sphx_mp mp, int loop_style, int *substeps, double *adv_dt)
         *substeps = count;
     if (adv_dt)
         *adv_dt = Dt;
+    return SPHX_OK;
+}
+
+// Folds the recorded event pairs into the running totals and frees the events.
+void collect_events(sphx_mp mp)
+{
+    auto fold = [](std::vector<cudaEvent_t> &ev, double &ms, long &cnt) {
+        for (size_t q = 0; q + 1 < ev.size(); q += 2)
+        {
+            float t = 0.f;
+            if (cudaEventElapsedTime(&t, ev[q], ev[q + 1]) == cudaSuccess)
+            {
+                ms += t;
+                ++cnt;
+            }
+            cudaEventDestroy(ev[q]);
+            cudaEventDestroy(ev[q + 1]);
+        }
+        ev.clear();
+    };
+    fold(mp->ev_first, mp->ms_first, mp->n_first);
+    fold(mp->ev_second, mp->ms_second, mp->n_second);
+}
+} // namespace
+
+namespace
+{
+// Loads the FP64 fluid body's state (any particle order) into the solver, re-sorts it into
+// cell order, rebuilds the neighbour lists and density sums, and primes the time-step
+// maxima: the set-up of sphx_mp_create and sphx_mp_upload.
+int import_fluid(sphx_mp mp, sphx_body fb, double rho0, double c0)
+{
+    const int D = mp->dim;
+    const size_t n = mp->n;
+    const size_t nc = mp->ncells;
+    sphx_ctx ctx = mp->ctx;
+    cudaStream_t s = ctx->stream;
+    MeshDev m = mp->k.m;
+    SPHX_CUDA(cudaStreamSynchronize(s));
+    // fluid: FP64 body state -> FP32 (body order) in `a`, then the first configuration
+    Field *pos = fb->find("Position"), *vel = fb->find("Velocity"), *force = fb->find("Force"),
+          *rho = fb->find("Density"), *drho = fb->find("DensityChangeRate");
+    if (!pos || !rho)
+        return fail(SPHX_ERR_NOT_FOUND, "fluid Position / Density missing");
+    if (n > 0)
+    {
+        ImportArgs ia{(const double *)(vel ? vel->dev : nullptr), (const double *)(force ? force->dev : nullptr),
+                      (const double *)rho->dev, (const double *)(drho ? drho->dev : nullptr), rho0, c0 * c0};
+        if (D == 2)
+            k_mp_import<2><<<grid_for(n, 256), 256, 0, s>>>(n, ia, mp->a);
+        else
+            k_mp_import<3><<<grid_for(n, 256), 256, 0, s>>>(n, ia, mp->a);
+        SPHX_LAUNCHED(ctx);
+    }
+    if (cudaMemsetAsync(mp->count, 0, nc * sizeof(uint32_t), s) != cudaSuccess)
+        return fail(SPHX_ERR_CUDA, "memset failed");
+    if (n > 0)
+    {
+        if (D == 2)
+            k_mp_from_fp64<2><<<grid_for(n, 256), 256, 0, s>>>(n, (const double *)pos->dev, m, mp->ncell, mp->noff,
+                                                               mp->key, mp->rank, mp->count);
+        else
+            k_mp_from_fp64<3><<<grid_for(n, 256), 256, 0, s>>>(n, (const double *)pos->dev, m, mp->ncell, mp->noff,
+                                                               mp->key, mp->rank, mp->count);
+        ctx->launches++;
+    }
+    SPHX_TRY(D == 2 ? configuration_update<2>(mp, false) : configuration_update<3>(mp, false));
+    // initial maxima for the first time steps
+    if (cudaMemsetAsync(mp->slots, 0, 2 * sizeof(unsigned long long), s) != cudaSuccess)
+        return fail(SPHX_ERR_CUDA, "memset failed");
+    if (n > 0)
+    {
+        if (D == 2)
+            k_mp_initial_max<2><<<grid_for(n, 256), 256, 0, s>>>(n, mp->k, mp->a, mp->slots, mp->slots + 1);
+        else
+            k_mp_initial_max<3><<<grid_for(n, 256), 256, 0, s>>>(n, mp->k, mp->a, mp->slots, mp->slots + 1);
+        ctx->launches++;
+    }
     return SPHX_OK;
 }
 } // namespace
@@ -1047,15 +1283,14 @@ extern "C" int sphx_mp_create(sphx_relation inner, sphx_relation wall, const sph
     mp->perm = mp->alloc<uint32_t>(big);
     mp->ncell = mp->alloc<uint32_t>(n);
     mp->noff = mp->alloc<float>(3 * n);
-    mp->w.cell = mp->alloc<uint32_t>(nw);
-    mp->w.off = mp->alloc<float>(3 * nw);
-    mp->w.n = mp->alloc<float>(3 * nw);
+    mp->w.geo = mp->alloc<float4>(nw);
+    mp->w.n = mp->alloc<float4>(nw);
     mp->w.nw = nw;
     mp->in.count = mp->alloc<uint32_t>(n);
     mp->wl.count = mp->alloc<uint32_t>(n);
     mp->slots = mp->alloc<unsigned long long>(8);
     if (!mp->f_offset || !mp->w_offset || !mp->count || !mp->key || !mp->rank || !mp->perm || !mp->ncell ||
-        !mp->noff || !mp->w.cell || !mp->w.off || !mp->w.n || !mp->in.count || !mp->wl.count || !mp->slots)
+        !mp->noff || !mp->w.geo || !mp->w.n || !mp->in.count || !mp->wl.count || !mp->slots)
         return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "mixed-precision allocation failed"));
     if (cudaMallocHost(&mp->h_slots, 8 * sizeof(unsigned long long)) != cudaSuccess)
         return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "pinned allocation failed"));
@@ -1087,98 +1322,29 @@ extern "C" int sphx_mp_create(sphx_relation inner, sphx_relation wall, const sph
     {
         if (D == 2)
             k_wall_load<2><<<grid_for(nw, 256), 256, 0, s>>>(nw, mp->perm, (const double *)wpos->dev,
-                                                              (const double *)wn->dev, m, mp->w.cell, mp->w.off,
-                                                              mp->w.n);
+                                                              (const double *)wn->dev, m, mp->w.geo, mp->w.n);
         else
             k_wall_load<3><<<grid_for(nw, 256), 256, 0, s>>>(nw, mp->perm, (const double *)wpos->dev,
-                                                              (const double *)wn->dev, m, mp->w.cell, mp->w.off,
-                                                              mp->w.n);
+                                                              (const double *)wn->dev, m, mp->w.geo, mp->w.n);
         ctx->launches++;
     }
-    // fluid: FP64 body state -> FP32 (body order) in `a`, then the first configuration
-    Field *pos = fb->find("Position"), *vel = fb->find("Velocity"), *force = fb->find("Force"),
-          *rho = fb->find("Density"), *drho = fb->find("DensityChangeRate");
-    if (!pos || !rho)
-        return bail(fail(SPHX_ERR_NOT_FOUND, "fluid Position / Density missing"));
-    {
-        std::vector<double> hv(n * D, 0.0), hf(n * D, 0.0), hr(n, p->rho0), hd(n, 0.0);
-        if (vel && cudaMemcpy(hv.data(), vel->dev, hv.size() * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
-            return bail(fail(SPHX_ERR_CUDA, "copy failed"));
-        if (force && cudaMemcpy(hf.data(), force->dev, hf.size() * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
-            return bail(fail(SPHX_ERR_CUDA, "copy failed"));
-        if (cudaMemcpy(hr.data(), rho->dev, hr.size() * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
-            return bail(fail(SPHX_ERR_CUDA, "copy failed"));
-        if (drho && cudaMemcpy(hd.data(), drho->dev, hd.size() * 8, cudaMemcpyDeviceToHost) != cudaSuccess)
-            return bail(fail(SPHX_ERR_CUDA, "copy failed"));
-        std::vector<float> fv(hv.begin(), hv.end()), ff(hf.begin(), hf.end()), fr(n), fd(hd.begin(), hd.end());
-        std::vector<uint32_t> ids(n);
-        for (size_t i = 0; i < n; ++i)
-        {
-            fr[i] = float(hr[i] - p->rho0);
-            ids[i] = uint32_t(i);
-        }
-        if (cudaMemcpy(mp->a.vel, fv.data(), fv.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(mp->a.force, ff.data(), ff.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(mp->a.drho, fr.data(), fr.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(mp->a.drho_dt, fd.data(), fd.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(mp->a.id, ids.data(), ids.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
-            return bail(fail(SPHX_ERR_CUDA, "copy failed"));
-    }
-    if (cudaMemsetAsync(mp->count, 0, nc * sizeof(uint32_t), s) != cudaSuccess)
-        return bail(fail(SPHX_ERR_CUDA, "memset failed"));
-    if (n > 0)
-    {
-        if (D == 2)
-            k_mp_from_fp64<2><<<grid_for(n, 256), 256, 0, s>>>(n, (const double *)pos->dev, m, mp->ncell, mp->noff,
-                                                               mp->key, mp->rank, mp->count);
-        else
-            k_mp_from_fp64<3><<<grid_for(n, 256), 256, 0, s>>>(n, (const double *)pos->dev, m, mp->ncell, mp->noff,
-                                                               mp->key, mp->rank, mp->count);
-        ctx->launches++;
-    }
-    st = D == 2 ? configuration_update<2>(mp, false) : configuration_update<3>(mp, false);
-    if (st != SPHX_OK)
+    if ((st = import_fluid(mp, fb, p->rho0, p->c0)) != SPHX_OK)
         return bail(st);
-    // initial maxima for the first time steps
-    if (cudaMemsetAsync(mp->slots, 0, 2 * sizeof(unsigned long long), s) != cudaSuccess)
-        return bail(fail(SPHX_ERR_CUDA, "memset failed"));
-    if (n > 0)
-    {
-        if (D == 2)
-            k_mp_initial_max<2><<<grid_for(n, 256), 256, 0, s>>>(n, mp->k, mp->a, mp->slots, mp->slots + 1);
-        else
-            k_mp_initial_max<3><<<grid_for(n, 256), 256, 0, s>>>(n, mp->k, mp->a, mp->slots, mp->slots + 1);
-        ctx->launches++;
-    }
     if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess)
         return bail(fail(SPHX_ERR_CUDA, "mixed-precision set-up failed"));
     *out = mp;
     return SPHX_OK;
 }
 
-namespace
+extern "C" int sphx_mp_upload(sphx_mp mp, sphx_body fb)
 {
-// Folds the recorded event pairs into the running totals and frees the events.
-void collect_events(sphx_mp mp)
-{
-    auto fold = [](std::vector<cudaEvent_t> &ev, double &ms, long &cnt) {
-        for (size_t q = 0; q + 1 < ev.size(); q += 2)
-        {
-            float t = 0.f;
-            if (cudaEventElapsedTime(&t, ev[q], ev[q + 1]) == cudaSuccess)
-            {
-                ms += t;
-                ++cnt;
-            }
-            cudaEventDestroy(ev[q]);
-            cudaEventDestroy(ev[q + 1]);
-        }
-        ev.clear();
-    };
-    fold(mp->ev_first, mp->ms_first, mp->n_first);
-    fold(mp->ev_second, mp->ms_second, mp->n_second);
+    if (!mp || !fb || fb->n != mp->n || fb->dim != mp->dim)
+        return fail(SPHX_ERR_INVALID_ARG, "body does not match the mixed-precision solver");
+    double rho0 = double(mp->k.rho0), c0 = mp->k.c0;
+    SPHX_TRY(import_fluid(mp, fb, rho0, c0));
+    SPHX_CUDA(cudaStreamSynchronize(mp->ctx->stream));
+    return SPHX_OK;
 }
-} // namespace
 
 extern "C" int sphx_mp_set_profiling(sphx_mp mp, int on)
 {
@@ -1245,6 +1411,109 @@ extern "C" int sphx_mp_destroy(sphx_mp mp)
         cudaFreeHost(mp->h_slots);
     delete mp;
     release(ctx);
+    return SPHX_OK;
+}
+
+namespace
+{
+// Snapshot of the variables a sub-step modifies (the configuration is untouched).
+struct Snapshot
+{
+    std::vector<void *> bufs;
+    int take(sphx_mp mp, bool restore)
+    {
+        size_t n = mp->n, D = size_t(mp->dim);
+        void *src[6] = {mp->a.dyn, mp->a.off, mp->a.force, mp->a.drho, mp->a.drho_dt, mp->slots};
+        size_t bytes[6] = {n * sizeof(float4), D * n * 4, D * n * 4, n * 4, n * 4, 2 * sizeof(unsigned long long)};
+        if (!restore)
+        {
+            bufs.assign(6, nullptr);
+            for (int q = 0; q < 6; ++q)
+                SPHX_CUDA(cudaMallocAsync(&bufs[q], std::max<size_t>(bytes[q], 1), mp->ctx->stream));
+        }
+        for (int q = 0; q < 6; ++q)
+        {
+            void *dst = restore ? src[q] : bufs[q];
+            const void *from = restore ? bufs[q] : src[q];
+            SPHX_CUDA(cudaMemcpyAsync(dst, from, bytes[q], cudaMemcpyDeviceToDevice, mp->ctx->stream));
+        }
+        return SPHX_OK;
+    }
+    void release(sphx_mp mp)
+    {
+        for (void *b : bufs)
+            if (b)
+                cudaFreeAsync(b, mp->ctx->stream);
+        bufs.clear();
+    }
+};
+} // namespace
+
+extern "C" int sphx_mp_autotune(sphx_mp mp, int reps, int *best_block, int *best_strategy, double *best_ms)
+{
+    if (!mp || reps < 1)
+        return fail(SPHX_ERR_INVALID_ARG, "invalid autotune arguments");
+    if (mp->n == 0)
+        return SPHX_OK;
+    double ac;
+    SPHX_TRY(read_slot(mp, 0, &ac));
+    double dt = mp->k.acoustic_cfl * mp->k.h / (ac + kTinyReal);
+    Snapshot snap;
+    SPHX_TRY(snap.take(mp, false));
+    const int blocks[3] = {64, 128, 256};
+    int keep_block = mp->block, keep_strategy = mp->strategy;
+    bool keep_prof = mp->profiling;
+    double best = 1e300;
+    int bb = keep_block, bs = keep_strategy;
+    cudaEvent_t e0, e1;
+    SPHX_CUDA(cudaEventCreate(&e0));
+    SPHX_CUDA(cudaEventCreate(&e1));
+    int st = SPHX_OK;
+    mp->profiling = false;
+    for (int strategy = 0; strategy < 2 && st == SPHX_OK; ++strategy)
+        for (int bi = 0; bi < 3 && st == SPHX_OK; ++bi)
+        {
+            mp->block = blocks[bi];
+            mp->strategy = strategy;
+            if ((st = snap.take(mp, true)) != SPHX_OK)
+                break;
+            if ((st = (mp->dim == 2 ? substep<2>(mp, dt) : substep<3>(mp, dt))) != SPHX_OK) // warm-up
+                break;
+            cudaEventRecord(e0, mp->ctx->stream);
+            for (int r = 0; r < reps && st == SPHX_OK; ++r)
+                st = mp->dim == 2 ? substep<2>(mp, dt) : substep<3>(mp, dt);
+            cudaEventRecord(e1, mp->ctx->stream);
+            if (cudaEventSynchronize(e1) != cudaSuccess)
+                st = fail(SPHX_ERR_CUDA, "autotune timing failed");
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (st == SPHX_OK && ms / reps < best)
+            {
+                best = ms / reps;
+                bb = blocks[bi];
+                bs = strategy;
+            }
+        }
+    int st2 = snap.take(mp, true);
+    snap.release(mp);
+    cudaStreamSynchronize(mp->ctx->stream);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    mp->profiling = keep_prof;
+    if (st != SPHX_OK || st2 != SPHX_OK)
+    {
+        mp->block = keep_block;
+        mp->strategy = keep_strategy;
+        return st != SPHX_OK ? st : st2;
+    }
+    mp->block = bb;
+    mp->strategy = bs;
+    if (best_block)
+        *best_block = bb;
+    if (best_strategy)
+        *best_strategy = bs;
+    if (best_ms)
+        *best_ms = best;
     return SPHX_OK;
 }
 

@@ -48,12 +48,6 @@ struct BuildArgs
     unsigned int *max_count;
 };
 
-__device__ __forceinline__ double pow4(double x)
-{
-    double x2 = x * x;
-    return x2 * x2;
-}
-
 template <int D, bool INNER>
 __global__ void __launch_bounds__(kBlock) k_build(BuildArgs a)
 {
@@ -110,17 +104,23 @@ __global__ void __launch_bounds__(kBlock) k_build(BuildArgs a)
                         r2 = __dadd_rn(r2, __dmul_rn(dx[2], dx[2]));
                     if (!(r2 < a.k.rc_sqr))
                         continue;
-                    double r = sqrt(r2);
+                    // one reciprocal square root gives r and 1/r; e = dx / (r + TinyReal) of
+                    // the reference differs from dx / r by TinyReal / r relative, far below
+                    // one rounding, except for coincident particles where e is zero
+                    double ri = rsqrt(r2);
+                    double r = r2 > 0.0 ? r2 * ri : 0.0;
+                    double inv = r2 > 0.0 ? ri : 1.0 / kTinyReal;
                     double q = r * a.k.inv_h;
-                    double W = a.k.factor_W * (pow4(1.0 - 0.5 * q) * (1.0 + 2.0 * q));
-                    double qm2 = q - 2.0;
-                    double dW = a.k.factor_dW * (0.625 * (qm2 * qm2 * qm2) * q);
+                    // Wendland C2 with t = 1 - q/2: W ~ t^4 (1 + 2q), dW ~ 0.625 (q - 2)^3 q = -5 t^3 q
+                    double t = 1.0 - 0.5 * q;
+                    double t2 = t * t, t3 = t2 * t;
+                    double W = a.k.factor_W * (t2 * t2 * (1.0 + 2.0 * q));
+                    double dW = a.k.factor_dW * (-5.0 * t3 * q);
                     if (cnt < unsigned(a.cap))
                     {
                         size_t slot = size_t(cnt) * a.n_src + i;
                         a.J[slot] = j;
                         a.DW[slot] = dW;
-                        double inv = 1.0 / (r + kTinyReal);
 #pragma unroll
                         for (int d = 0; d < D; ++d)
                             a.E[d * stride + slot] = dx[d] * inv;

@@ -167,6 +167,13 @@ class MixedPrecisionDamBreak:
         self.total_substeps += sub.value
         return sub.value, Dt.value
 
+    def autotune(self, reps: int = 3):
+        """Picks the fastest block size and neighbour strategy on the current state."""
+        C = self._C
+        b, st, ms = C.c_int(), C.c_int(), C.c_double()
+        self._N.call("sphx_mp_autotune", self.handle, int(reps), C.byref(b), C.byref(st), C.byref(ms))
+        return b.value, st.value, ms.value
+
     def set_profiling(self, on: bool) -> None:
         self._N.call("sphx_mp_set_profiling", self.handle, int(on))
 
@@ -183,6 +190,14 @@ class MixedPrecisionDamBreak:
         self._N.call("sphx_mp_list_sizes", self.handle, out.ctypes.data_as(C.POINTER(C.c_uint64)))
         return dict(n=int(out[0]), nw=int(out[1]), nnz_inner=int(out[2]), nnz_wall=int(out[3]),
                     cap_inner=int(out[4]), cap_wall=int(out[5]))
+
+    def upload(self, body) -> None:
+        """Reloads the solver from an FP64 fluid body (sphx_mp_upload)."""
+        self._N.call("sphx_mp_upload", self.handle, body.handle)
+
+    def download(self, body) -> None:
+        """Writes the solver state into an FP64 fluid body (sphx_mp_download)."""
+        self._N.call("sphx_mp_download", self.handle, body.handle)
 
     def sync_fp64(self) -> None:
         sim = self.fp64

@@ -81,10 +81,12 @@ SIGNATURES = {
     "sphx_mp_destroy": (_i, [_vp]),
     "sphx_mp_advection_step": (_i, [_vp, _i, C.POINTER(C.c_int), _pd, _pd]),
     "sphx_mp_download": (_i, [_vp, _vp]),
+    "sphx_mp_upload": (_i, [_vp, _vp]),
     "sphx_mp_conservation": (_i, [_vp, _pd]),
     "sphx_mp_upper_front": (_i, [_vp, _i, _pd, _pd, _pd]),
     "sphx_mp_set_tuning": (_i, [_vp, _i, _i]),
     "sphx_mp_set_profiling": (_i, [_vp, _i]),
+    "sphx_mp_autotune": (_i, [_vp, _i, C.POINTER(C.c_int), C.POINTER(C.c_int), _pd]),
     "sphx_mp_kernel_times": (_i, [_vp, _pd]),
     "sphx_mp_list_sizes": (_i, [_vp, _pu64]),
 }

@@ -79,3 +79,36 @@ def test_mixed_precision_upper_front_and_probe():
     ref.water_block.updateCellLinkedList()
     ref.fluid_observer_contact.updateConfiguration()
     assert np.allclose(mp.observe_pressure(), ref.recorded_pressure.exec(), rtol=1e-3, atol=1e-6)
+
+
+def test_upload_restores_downloaded_state():
+    """sphx_mp_upload of a state written by sphx_mp_download continues the same run."""
+    case = cases.dambreak_2d()
+    a = MixedPrecisionDamBreak(case)
+    b = MixedPrecisionDamBreak(case)
+    for _ in range(3):
+        a.advection_step()
+        b.advection_step()
+    a.sync_fp64()
+    b.upload(a.fp64.water_block)  # same state, re-imported
+    a.advection_step()
+    b.advection_step()
+    a.sync_fp64()
+    b.sync_fp64()
+    for name in ("Position", "Velocity"):
+        assert rel_err(b.fp64.water_block.download(name), a.fp64.water_block.download(name)) < 1e-6
+
+
+def test_autotune_keeps_state():
+    case = cases.dambreak_2d()
+    a = MixedPrecisionDamBreak(case)
+    b = MixedPrecisionDamBreak(case)
+    block, strategy, ms = b.autotune(reps=1)
+    assert block in (64, 128, 256) and strategy in (0, 1) and ms > 0
+    b.set_tuning(128, 0)
+    for _ in range(3):
+        a.advection_step()
+        b.advection_step()
+    a.sync_fp64()
+    b.sync_fp64()
+    assert np.array_equal(a.fp64.water_block.download("Position"), b.fp64.water_block.download("Position"))
