@@ -251,6 +251,57 @@ int sphx_mp_kernel_times(sphx_mp mp, double *out);
  * wall pairs, out[4] / out[5] list capacities (synchronises). */
 int sphx_mp_list_sizes(sphx_mp mp, uint64_t *out);
 
+/* ------------------------------------------------------------------ batched instances
+ * Many independent dam breaks of one dimension advanced together in mixed precision (the
+ * numerics of sphx_mp_*).  No single reference counterpart: each instance runs its own
+ * pass of the Dambreak.cpp:166-220 loop (own advection dt, own acoustic dt and sub-step
+ * count, own configuration update), and every kernel launch covers all instances.
+ * Particles of all instances are concatenated in one cell-ordered array over one cell
+ * index space in which each instance owns a disjoint range; per-instance time steps,
+ * relaxation times and sub-step counters stay on the device.
+ *
+ * Each instance: fluid at rest (rho = rho0) on the given positions, one static wall body
+ * with its normals, uniform masses and volumes, gravity as the only prior force, and a
+ * cell mesh with grid spacing 2h (at most 32768 cells per axis in 2D, 1024 in 3D). */
+typedef struct sphx_batch_s *sphx_batch;
+
+typedef struct
+{
+    sphx_mesh_desc mesh;     /* cell mesh of the instance (grid spacing = 2h) */
+    size_t n_fluid, n_wall;
+    const double *fluid_pos;   /* n_fluid x dim, AoS */
+    const double *wall_pos;    /* n_wall x dim, AoS */
+    const double *wall_normal; /* n_wall x dim, AoS (NormalDirectionFromBodyShape) */
+    double h;                  /* smoothing length */
+    double sigma0;             /* lattice number density (sphx_lattice_number_density) */
+    double rho0, c0, U_ref;
+    double fluid_mass, fluid_vol;
+    double wall_rho0, wall_mass, wall_vol;
+    double gravity[3];
+} sphx_batch_instance;
+
+/* Copies the descriptions (host arrays may be freed afterwards), sorts the walls, builds
+ * the first configuration and the initial time-step maxima (synchronises). */
+int sphx_batch_create(sphx_ctx ctx, int dim, int count, const sphx_batch_instance *instances, sphx_batch *out);
+int sphx_batch_destroy(sphx_batch batch);
+/* One advection step of every instance (the Dambreak.cpp loop order: acoustic dt taken
+ * before each relaxation).  use_graph 1: the step runs as one CUDA graph launch whose
+ * conditional WHILE node repeats the acoustic sub-step until no instance is active (the
+ * graph is built on first use and rebuilt when list storage grows); 0: the same kernels,
+ * with the host reading the loop flag after each sub-step.  An instance taking more than
+ * 2^20 sub-steps ends the step with SPHX_ERR_TIMEOUT.  Outputs (may be null, else count
+ * entries): acoustic sub-steps of this step and physical time per instance. */
+int sphx_batch_advection_step(sphx_batch batch, int use_graph, int *substeps, double *physical_time);
+/* Block size (64..256, multiple of 32) of the two sweep kernels. */
+int sphx_batch_set_tuning(sphx_batch batch, int block);
+/* Graph launches made so far. */
+int sphx_batch_graph_launches(sphx_batch batch, uint64_t *out);
+/* Fluid state of one instance in its input particle order (any output may be null):
+ * pos / vel n_fluid x dim AoS, rho and p n_fluid (synchronises). */
+int sphx_batch_download(sphx_batch batch, int instance, double *pos, double *vel, double *rho, double *p);
+/* Total fluid and wall particles over all instances. */
+int sphx_batch_size(sphx_batch batch, size_t *fluid_particles, size_t *wall_particles);
+
 #ifdef __cplusplus
 }
 #endif

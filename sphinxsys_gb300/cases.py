@@ -123,3 +123,101 @@ def dambreak_3d(dp: float = 0.0075) -> DamBreakCase:
         inner_center=inner_hs, inner_halfsize=inner_hs,
         rho0=rho0, c0=c0, U_ref=U_ref, gravity=(0.0, 0.0, -g),
         observers=[(DL, 0.5, 0.2)], loop_style=0, vertical_axis=2)
+
+
+class MT19937_64:
+    """64-bit Mersenne Twister (Matsumoto & Nishimura, 2000) as std::mt19937_64 defines it,
+    so batch draws follow the stated seed exactly."""
+
+    N, M = 312, 156
+    MATRIX_A = 0xB5026F5AA96619E9
+    UPPER, LOWER = 0xFFFFFFFF80000000, 0x7FFFFFFF
+    MASK = (1 << 64) - 1
+
+    def __init__(self, seed: int = 5489):
+        self.mt = [0] * self.N
+        self.mt[0] = seed & self.MASK
+        for i in range(1, self.N):
+            prev = self.mt[i - 1]
+            self.mt[i] = (6364136223846793005 * (prev ^ (prev >> 62)) + i) & self.MASK
+        self.idx = self.N
+
+    def _twist(self):
+        mt = self.mt
+        for i in range(self.N):
+            x = (mt[i] & self.UPPER) | (mt[(i + 1) % self.N] & self.LOWER)
+            xa = x >> 1
+            if x & 1:
+                xa ^= self.MATRIX_A
+            mt[i] = mt[(i + self.M) % self.N] ^ xa
+        self.idx = 0
+
+    def __call__(self) -> int:
+        if self.idx >= self.N:
+            self._twist()
+        y = self.mt[self.idx]
+        self.idx += 1
+        y ^= (y >> 29) & 0x5555555555555555
+        y ^= (y << 17) & 0x71D67FFFEDA60000
+        y ^= (y << 37) & 0xFFF7EEE000000000
+        y ^= y >> 43
+        return y & self.MASK
+
+    def uniform(self) -> float:
+        """std::generate_canonical<double, 53> over one 64-bit draw (libstdc++)."""
+        return self() / 18446744073709551616.0
+
+
+def batch_instances(count: int = 64, seed: int = 0, n_min: float = 2e4, n_max: float = 5e5):
+    """Independent dam breaks for the batched solver: per instance, fluid particle count
+    N log-uniform in [n_min, n_max], column aspect H/L uniform in [0.25, 1], and the
+    dimension (2D if the draw is below 0.5) from one std::mt19937_64(seed) stream.
+
+    Geometry per instance: water column H = 1 (as Dambreak.cpp), L = H / aspect (and width
+    W = L / 2 in 3D); dp from N and the column volume; tank DL = 2.683 L, DH = 5.366 H (the
+    Dambreak.cpp tank-to-column ratios), DW = W in 3D; U_ref = 2 sqrt(g H), c0 = 10 U_ref."""
+    rng = MT19937_64(seed)
+    out = []
+    for k in range(count):
+        n = round(math.exp(math.log(n_min) + rng.uniform() * (math.log(n_max) - math.log(n_min))))
+        aspect = 0.25 + 0.75 * rng.uniform()
+        dim = 2 if rng.uniform() < 0.5 else 3
+        H = 1.0
+        L = H / aspect
+        if dim == 2:
+            dp = math.sqrt(L * H / n)
+            case = _column_case(f"batch{k}_2d", 2, L, H, 0.0, dp)
+        else:
+            W = 0.5 * L
+            dp = (L * H * W / n) ** (1.0 / 3.0)
+            case = _column_case(f"batch{k}_3d", 3, L, H, W, dp)
+        out.append(case)
+    return out
+
+
+def _column_case(name: str, dim: int, L: float, H: float, W: float, dp: float) -> DamBreakCase:
+    DL, DH = 2.683 * L, 5.366 * H
+    BW = 4 * dp
+    g = 1.0
+    U_ref = 2.0 * math.sqrt(g * H)
+    c0 = 10.0 * U_ref
+    if dim == 2:
+        water_hs = (0.5 * L, 0.5 * H)
+        outer_hs = (0.5 * DL + BW, 0.5 * DH + BW)
+        inner_hs = (0.5 * DL, 0.5 * DH)
+        return DamBreakCase(
+            name=name, dim=2, sys_lower=_pad((-BW, -BW)), sys_upper=_pad((DL + BW, DH + BW)), dp=dp,
+            water_center=_pad(water_hs), water_halfsize=_pad(water_hs),
+            outer_center=_pad(inner_hs), outer_halfsize=_pad(outer_hs),
+            inner_center=_pad(inner_hs), inner_halfsize=_pad(inner_hs),
+            rho0=1.0, c0=c0, U_ref=U_ref, gravity=_pad((0.0, -g)), observers=[_pad((DL, 0.2 * H))],
+            loop_style=0, vertical_axis=1)
+    DW = W
+    water_hs = (0.5 * L, 0.5 * W, 0.5 * H)
+    inner_hs = (0.5 * DL, 0.5 * DW, 0.5 * DH)
+    outer_hs = (0.5 * DL + BW, 0.5 * DW + BW, 0.5 * DH + BW)
+    return DamBreakCase(
+        name=name, dim=3, sys_lower=(-BW, -BW, -BW), sys_upper=(DL + BW, DW + BW, DH + BW), dp=dp,
+        water_center=water_hs, water_halfsize=water_hs, outer_center=inner_hs, outer_halfsize=outer_hs,
+        inner_center=inner_hs, inner_halfsize=inner_hs, rho0=1.0, c0=c0, U_ref=U_ref, gravity=(0.0, 0.0, -g),
+        observers=[(DL, 0.5 * DW, 0.2 * H)], loop_style=0, vertical_axis=2)

@@ -272,6 +272,25 @@ int exclusive_scan(sphx_ctx ctx, const uint32_t *d_in, uint32_t *d_out, size_t n
     return SPHX_OK;
 }
 
+size_t scan_scratch_entries(size_t n) { return (n + kScanTile - 1) / kScanTile + 1; }
+
+// The same three passes on a stream with caller-owned tile scratch of
+// scan_scratch_entries(n) entries; enqueues only (no allocation, no synchronisation), so a
+// stream capture may record it.
+int exclusive_scan_into(cudaStream_t s, const uint32_t *d_in, uint32_t *d_out, size_t n, uint32_t *tiles)
+{
+    if (n == 0)
+        return SPHX_OK;
+    size_t ntiles = (n + kScanTile - 1) / kScanTile;
+    k_scan_tile_sums<<<unsigned(ntiles), kBlock, 0, s>>>(d_in, n, tiles);
+    SPHX_CUDA(cudaGetLastError());
+    k_scan_tile_prefix<<<1, 1024, 0, s>>>(tiles, ntiles, tiles + ntiles);
+    SPHX_CUDA(cudaGetLastError());
+    k_scan_apply<<<unsigned(ntiles), kBlock, 0, s>>>(d_in, d_out, n, tiles);
+    SPHX_CUDA(cudaGetLastError());
+    return SPHX_OK;
+}
+
 // Stable counting sort of n keys in [0, nkeys): d_offset[nkeys+1] gets the key offsets,
 // d_perm[k] the index of the k-th particle in key order (ascending index within a key).
 int counting_sort_by_key(sphx_ctx ctx, const uint32_t *d_key, size_t n, uint32_t nkeys, uint32_t *d_offset,

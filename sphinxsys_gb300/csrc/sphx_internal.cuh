@@ -158,4 +158,8 @@ namespace sphx
 int counting_sort_by_key(sphx_ctx ctx, const uint32_t *d_key, size_t n, uint32_t nkeys, uint32_t *d_offset,
                          uint32_t *d_count, uint32_t *d_rank, uint32_t *d_perm);
 int exclusive_scan(sphx_ctx ctx, const uint32_t *d_in, uint32_t *d_out, size_t n);
+// Scan with caller-owned scratch (scan_scratch_entries(n) uint32 entries); 3 launches, no
+// allocation or synchronisation.
+size_t scan_scratch_entries(size_t n);
+int exclusive_scan_into(cudaStream_t s, const uint32_t *d_in, uint32_t *d_out, size_t n, uint32_t *tiles);
 } // namespace sphx

@@ -89,6 +89,13 @@ SIGNATURES = {
     "sphx_mp_autotune": (_i, [_vp, _i, C.POINTER(C.c_int), C.POINTER(C.c_int), _pd]),
     "sphx_mp_kernel_times": (_i, [_vp, _pd]),
     "sphx_mp_list_sizes": (_i, [_vp, _pu64]),
+    "sphx_batch_create": (_i, [_vp, _i, _i, _vp, _pvp]),
+    "sphx_batch_destroy": (_i, [_vp]),
+    "sphx_batch_advection_step": (_i, [_vp, _i, C.POINTER(C.c_int), _pd]),
+    "sphx_batch_set_tuning": (_i, [_vp, _i]),
+    "sphx_batch_graph_launches": (_i, [_vp, _pu64]),
+    "sphx_batch_download": (_i, [_vp, _i, _pd, _pd, _pd, _pd]),
+    "sphx_batch_size": (_i, [_vp, _psz, _psz]),
 }
 
 _lib: Optional[C.CDLL] = None

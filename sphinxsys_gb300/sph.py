@@ -156,6 +156,9 @@ def lattice_positions(dim: int, lower, upper, dp: float, shape) -> np.ndarray:
     up = np.asarray(upper[:dim], dtype=np.float64)
     n = [int(math.ceil((up[a] + 0.0 - lo[a]) / dp)) for a in range(dim)]
     axes = [(lo[a] + np.arange(n[a], dtype=np.float64) * dp) + 0.5 * dp for a in range(dim)]
+    parts = getattr(shape, "parts", None)
+    if parts and all(isinstance(p, GeometricShapeBox) for p, _ in parts):
+        return _box_lattice(dim, axes, parts)
     out = []
     for x0 in axes[0]:  # slab by slab to bound memory
         if dim == 2:
@@ -166,6 +169,31 @@ def lattice_positions(dim: int, lower, upper, dp: float, shape) -> np.ndarray:
         keep = shape.contain(pts)
         if np.any(keep):
             out.append(pts[keep])
+    return np.concatenate(out) if out else np.zeros((0, dim))
+
+
+def _box_lattice(dim: int, axes, parts) -> np.ndarray:
+    """lattice_positions for unions / differences of boxes: a box holds a lattice point
+    exactly when every axis passes |x_a - c_a| <= hs_a, so the per-axis tests are taken
+    once and combined slab by slab (same points, same order, without testing the points
+    outside every box)."""
+    masks = [[np.abs(axes[a] - box.c[a]) <= box.hs[a] for a in range(dim)] for box, _ in parts]
+    rest = (len(axes[1]),) if dim == 2 else (len(axes[1]), len(axes[2]))
+    planes = [m[1] if dim == 2 else (m[1][:, None] & m[2][None, :]) for m in masks]
+    out = []
+    for ix, x0 in enumerate(axes[0]):
+        exist = np.zeros(rest, dtype=bool)
+        for (box, add), m, plane in zip(parts, masks, planes):
+            inside = plane if m[0][ix] else np.zeros(rest, dtype=bool)
+            exist = (exist | inside) if add else (exist & ~inside)
+        if not exist.any():
+            continue
+        if dim == 2:
+            y = axes[1][exist]
+            out.append(np.stack([np.full(len(y), x0), y], axis=1))
+        else:
+            j, k = np.nonzero(exist)
+            out.append(np.stack([np.full(len(j), x0), axes[1][j], axes[2][k]], axis=1))
     return np.concatenate(out) if out else np.zeros((0, dim))
 
 
