@@ -268,6 +268,85 @@ def fp64_leg(args, torch, local):
     return out
 
 
+def batch_leg(args, torch, local):
+    """Seeded batch of independent 2D / 3D dam breaks (N log-uniform in [2e4, 5e5], aspect
+    H/L uniform in [0.25, 1], std::mt19937_64 seed 0), one BatchDamBreak per dimension,
+    each advection step one CUDA graph launch.  Aggregate particle-steps/s = sum over
+    instances of fluid particles x acoustic sub-steps / time, against the same instances
+    run one after another through the FP64 drop-in path (a bounded sample of steps)."""
+    from sphinxsys_gb300 import cases
+    from sphinxsys_gb300.batch import BatchDamBreak
+    from sphinxsys_gb300.dambreak import DamBreak
+    insts = cases.batch_instances(args.batch_count, seed=0)
+    groups = {}
+    ps_graph = el_graph = ps_host = el_host = 0.0
+    launches = 0
+    for d in (2, 3):
+        cs = [c for c in insts if c.dim == d]
+        if not cs:
+            continue
+        b = BatchDamBreak(cs, device=local)
+        nq = np.asarray(b.n_fluid, dtype=np.float64)
+        stream = torch.cuda.ExternalStream(b.ctx.stream())
+
+        def run(k, use_graph):
+            b.ctx.synchronize()
+            l0 = b.ctx.launch_count()
+            with torch.cuda.stream(stream):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+            ps = 0.0
+            for _ in range(k):
+                ps += float(np.dot(nq, b.advection_step(use_graph)))
+            with torch.cuda.stream(stream):
+                e1.record()
+            b.ctx.synchronize()
+            torch.cuda.synchronize()
+            return ps, e0.elapsed_time(e1) / 1e3, b.ctx.launch_count() - l0
+
+        tune = {}
+        for blk in (64, 128, 256):  # block-size autotune, one step each after a graph build
+            b.set_tuning(blk)
+            b.advection_step()
+            ps, el, _ = run(1, True)
+            tune[blk] = el / max(ps, 1.0)
+        blk = min(tune, key=tune.get)
+        b.set_tuning(blk)
+        for _ in range(max(args.warmup - 3, 1)):
+            b.advection_step()
+        ps, el, ln = run(args.batch_steps, True)
+        ps_graph += ps
+        el_graph += el
+        launches += ln
+        hps, hel, _ = run(args.batch_steps, False)
+        ps_host += hps
+        el_host += hel
+        nf, nw = b.size()
+        groups[f"{d}d"] = {"instances": len(cs), "n_fluid": int(nf), "n_wall": int(nw), "block": blk,
+                           "graph": {"value": ps / el, "ms_per_step": 1e3 * el / args.batch_steps},
+                           "host_loop": {"value": hps / hel, "ms_per_step": 1e3 * hel / args.batch_steps}}
+        del b
+    # the same instances, one after another, through the FP64 drop-in path
+    fp_ps = fp_el = 0.0
+    for c in insts:
+        sim = DamBreak(c, device=local)
+        n = sim.water_block.n
+        for _ in range(args.batch_fp64_warmup):
+            sim.advection_step()
+        el, subs, _, _ = timed_steps(torch, sim.ctx, lambda: sim.advection_step()[:2], args.batch_fp64_steps, 0)
+        fp_ps += n * subs
+        fp_el += el
+        del sim
+    value = ps_graph / el_graph
+    return {"workload": f"batch{len(insts)}_seed0", "instances": len(insts), "value": value, "unit": UNIT,
+            "steps": args.batch_steps, "gpu_launches": int(launches), "groups": groups,
+            "host_loop_value": ps_host / el_host,
+            "fp64_sequential": {"value": fp_ps / fp_el, "steps_per_instance": args.batch_fp64_steps,
+                                "sample": f"{args.batch_fp64_steps} advection steps of each instance"},
+            "speedup_vs_fp64_sequential": value / (fp_ps / fp_el)}
+
+
 def run_cpu_sample(case, threads: int):
     """One advection step of the oracle (OpenMP FP64 restatement) on the same case."""
     from oracle import oracle as O
@@ -325,6 +404,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--autotune", type=int, default=1)
+    ap.add_argument("--batch-count", type=int, default=64, help="instances of the batched leg (0 = skip)")
+    ap.add_argument("--batch-steps", type=int, default=5)
+    ap.add_argument("--batch-fp64-steps", type=int, default=1)
+    ap.add_argument("--batch-fp64-warmup", type=int, default=1)
     args = ap.parse_args()
     rank, world, local = dist_info()
 
@@ -350,6 +433,7 @@ def main():
         dist.all_reduce(m, op=dist.ReduceOp.MAX)
         ps, el = float(t[0]), float(m[0])
     fp64 = None if args.no_fp64 else fp64_leg(args, torch, local)
+    batch = batch_leg(args, torch, local) if args.batch_count > 0 else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -375,6 +459,7 @@ def main():
                                 "fp64_same_case": mixed["fp64_same_case"],
                                 "errors_vs_fp64": mixed["errors_vs_fp64"], "lists": mixed["lists"]},
             "fp64_drop_in": fp64,
+            "batch": batch,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
