@@ -207,7 +207,7 @@ int sphx_upper_front_in_axis_direction(sphx_body fluid, int axis, const double *
  *
  * Requirements checked at creation: uniform particle mass and volume in each body, a
  * static wall (zero wall velocity and acceleration), gravity as the only prior force,
- * at most 1024 cells per mesh axis. */
+ * at most 32768 cells per mesh axis in 2D and 1024 in 3D. */
 typedef struct sphx_mp_s *sphx_mp;
 
 /* Builds the solver from the current FP64 state of the relations' bodies. */

@@ -14,9 +14,8 @@
 // CUDA graph whose conditional WHILE node repeats the sub-step until no instance is active.
 // A per-instance cap on sub-steps per advection step ends the loop with an error flag.
 //
-// Numerics and precision are those of the single-case mixed solver (mixed.cu): FP32 pair
-// arithmetic with compensated sums, positions as an FP32 offset from an integer cell,
-// FP64 position half-steps, time-step reductions and conservation sums.
+// The per-particle arithmetic is the single-case mixed solver's (mp_common.cuh), so an
+// instance advances exactly as sphx_mp_* advances that case alone.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -31,42 +30,14 @@ namespace
 {
 constexpr int kMaxSubsteps = 1 << 20; // cap of acoustic sub-steps per advection step
 
-// cell coordinates packed into 30 bits: 15 per axis in 2D, 10 per axis in 3D
-template <int D>
-__host__ __device__ __forceinline__ uint32_t bpack(const int *c)
-{
-    if (D == 2)
-        return uint32_t(c[0]) | (uint32_t(c[1]) << 15);
-    return uint32_t(c[0]) | (uint32_t(c[1]) << 10) | (uint32_t(c[2]) << 20);
-}
-template <int D>
-__device__ __forceinline__ void bunpack(uint32_t p, int *c)
-{
-    if (D == 2)
-    {
-        c[0] = int(p & 32767u);
-        c[1] = int((p >> 15) & 32767u);
-        c[2] = 0;
-    }
-    else
-    {
-        c[0] = int(p & 1023u);
-        c[1] = int((p >> 10) & 1023u);
-        c[2] = int((p >> 20) & 1023u);
-    }
-}
-
 struct BInst
 {
     MeshDev m;
+    MPParams p;
+    double gd[3];
     uint32_t cell_base, ncells;
     uint32_t p_start, p_count, w_start, w_count;
-    float gs_f, rc_sqr, inv_h, fW, fdW;
-    float rho0, p0_over_rho0, Vol, mass, inv_mass, rho0_over_sigma0, wall_factor, wall_Vol;
-    float inv_z, zgeo, inv_c0, slope;
-    float g[3];
-    double gd[3];
-    double sigma0, h, c0, acoustic_cfl, advection_cfl, U_ref;
+    double acoustic_cfl, advection_cfl, U_ref;
 };
 
 struct BRun
@@ -74,24 +45,6 @@ struct BRun
     double dt, Dt, relax, time;
     unsigned long long ac, adv;
     int active, substeps, iter, error;
-};
-
-struct BState
-{
-    float4 *geo0, *dyn;
-    float *off, *force, *drho, *drho_dt, *drho_sum;
-    uint32_t *id; // index inside the instance's input order
-};
-
-struct BWall
-{
-    float4 *geo, *n;
-};
-
-struct BLists
-{
-    uint32_t *count, *J;
-    unsigned cap;
 };
 
 __device__ __forceinline__ int find_instance(const uint32_t *starts, int count, uint32_t i)
@@ -106,59 +59,6 @@ __device__ __forceinline__ int find_instance(const uint32_t *starts, int count, 
             hi = mid - 1;
     }
     return lo;
-}
-
-template <int D>
-__device__ __forceinline__ void bgeo_dx(const BInst &k, const int *ci, const float *oi, float4 gj, float *dx)
-{
-    int cj[3];
-    bunpack<D>(__float_as_uint(gj.w), cj);
-    dx[0] = float(ci[0] - cj[0]) * k.gs_f + (oi[0] - gj.x);
-    dx[1] = float(ci[1] - cj[1]) * k.gs_f + (oi[1] - gj.y);
-    if (D == 3)
-        dx[2] = float(ci[2] - cj[2]) * k.gs_f + (oi[2] - gj.z);
-}
-
-template <int D>
-__device__ __forceinline__ float bsq(const float *dx)
-{
-    float s = dx[0] * dx[0] + dx[1] * dx[1];
-    if (D == 3)
-        s += dx[2] * dx[2];
-    return s;
-}
-
-// Candidates of the 3^D cells around local cell c of an instance (columns along the last axis
-// are contiguous in the cell order).
-template <int D, class F>
-__device__ __forceinline__ void bfor_each_candidate(const BInst &k, const uint32_t *offset, const int *c, F &&f)
-{
-    const MeshDev &m = k.m;
-    int lo0 = max(c[0] - 1, 0), hi0 = min(c[0] + 1, m.all_cells[0] - 1);
-    int lo1 = max(c[1] - 1, 0), hi1 = min(c[1] + 1, m.all_cells[1] - 1);
-    if (D == 2)
-    {
-        for (int x = lo0; x <= hi0; ++x)
-        {
-            uint32_t a = k.cell_base + uint32_t(x) * uint32_t(m.all_cells[1]);
-            uint32_t b = offset[a + uint32_t(lo1)], e = offset[a + uint32_t(hi1) + 1];
-            for (uint32_t j = b; j < e; ++j)
-                f(j);
-        }
-    }
-    else
-    {
-        int lo2 = max(c[2] - 1, 0), hi2 = min(c[2] + 1, m.all_cells[2] - 1);
-        for (int x = lo0; x <= hi0; ++x)
-            for (int y = lo1; y <= hi1; ++y)
-            {
-                uint32_t a = k.cell_base +
-                             (uint32_t(x) * uint32_t(m.all_cells[1]) + uint32_t(y)) * uint32_t(m.all_cells[2]);
-                uint32_t b = offset[a + uint32_t(lo2)], e = offset[a + uint32_t(hi2) + 1];
-                for (uint32_t j = b; j < e; ++j)
-                    f(j);
-            }
-    }
 }
 
 // Per-instance max of one lane value: a warp reduction when the warp holds one instance,
@@ -178,6 +78,21 @@ __device__ __forceinline__ void instance_max(BRun *run, int b, bool lane_active,
 
 // ---------------------------------------------------------------- hashing and sorting
 template <int D>
+__device__ __forceinline__ void hash_position(const BInst &k, const double *x, uint32_t *ncell, float *noff, size_t n,
+                                              size_t i, uint32_t *key, uint32_t *rank, uint32_t *cnt)
+{
+    int c[3] = {0, 0, 0};
+    cell_index<D>(k.m, x, c);
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        noff[d * n + i] = float(x[d] - cell_corner(k.m, d, c[d]));
+    ncell[i] = pack_cell<D>(c);
+    uint32_t key_i = k.cell_base + linear_cell<D>(k.m, c);
+    key[i] = key_i;
+    rank[i] = atomicAdd(&cnt[key_i], 1u);
+}
+
+template <int D>
 __global__ void k_b_from_fp64(size_t n, const double *__restrict__ pos, const uint32_t *__restrict__ starts,
                               int count, const BInst *__restrict__ inst, uint32_t *__restrict__ ncell,
                               float *__restrict__ noff, uint32_t *__restrict__ key, uint32_t *__restrict__ rank,
@@ -191,15 +106,7 @@ __global__ void k_b_from_fp64(size_t n, const double *__restrict__ pos, const ui
 #pragma unroll
     for (int d = 0; d < D; ++d)
         x[d] = pos[d * n + i];
-    int c[3] = {0, 0, 0};
-    cell_index<D>(k.m, x, c);
-#pragma unroll
-    for (int d = 0; d < D; ++d)
-        noff[d * n + i] = float(x[d] - cell_corner(k.m, d, c[d]));
-    ncell[i] = bpack<D>(c);
-    uint32_t key_i = k.cell_base + linear_cell<D>(k.m, c);
-    key[i] = key_i;
-    rank[i] = atomicAdd(&cnt[key_i], 1u);
+    hash_position<D>(k, x, ncell, noff, n, i, key, rank, cnt);
 }
 
 template <int D>
@@ -213,20 +120,12 @@ __global__ void k_b_rehash(size_t n, const float4 *__restrict__ geo0, const floa
         return;
     const BInst &k = inst[find_instance(starts, count, uint32_t(i))];
     int c0[3];
-    bunpack<D>(__float_as_uint(geo0[i].w), c0);
+    unpack_cell<D>(__float_as_uint(geo0[i].w), c0);
     double x[3] = {0, 0, 0};
 #pragma unroll
     for (int d = 0; d < D; ++d)
         x[d] = cell_corner(k.m, d, c0[d]) + double(off[d * n + i]);
-    int c[3] = {0, 0, 0};
-    cell_index<D>(k.m, x, c);
-#pragma unroll
-    for (int d = 0; d < D; ++d)
-        noff[d * n + i] = float(x[d] - cell_corner(k.m, d, c[d]));
-    ncell[i] = bpack<D>(c);
-    uint32_t key_i = k.cell_base + linear_cell<D>(k.m, c);
-    key[i] = key_i;
-    rank[i] = atomicAdd(&cnt[key_i], 1u);
+    hash_position<D>(k, x, ncell, noff, n, i, key, rank, cnt);
 }
 
 __global__ void k_b_scatter(size_t n, const uint32_t *__restrict__ key, const uint32_t *__restrict__ rank,
@@ -260,7 +159,7 @@ __global__ void k_b_set_total(uint32_t *offset, size_t ncells, uint32_t total) {
 
 template <int D>
 __global__ void k_b_gather(size_t n, const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ncell,
-                           const float *__restrict__ noff, BState src, BState dst)
+                           const float *__restrict__ noff, MPState src, MPState dst)
 {
     size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (k >= n)
@@ -304,7 +203,7 @@ __global__ void k_b_wall_load(size_t nw, const uint32_t *__restrict__ perm, cons
         o[d] = float(x[d] - cell_corner(b.m, d, c[d]));
         nn[d] = float(nrm[d * nw + i]);
     }
-    geo[k] = make_float4(o[0], o[1], o[2], __uint_as_float(bpack<D>(c)));
+    geo[k] = make_float4(o[0], o[1], o[2], __uint_as_float(pack_cell<D>(c)));
     n_out[k] = make_float4(nn[0], nn[1], nn[2], 0.f);
 }
 
@@ -330,53 +229,15 @@ __global__ void k_b_wall_hash(size_t nw, const double *__restrict__ pos, const u
 
 // ---------------------------------------------------------------- configuration + density sums
 template <int D>
-__global__ void __launch_bounds__(256)
-    k_b_build(size_t n, const uint32_t *__restrict__ starts, int count, const BInst *__restrict__ inst, BState f,
-              const uint32_t *__restrict__ f_offset, BWall w, const uint32_t *__restrict__ w_offset, BLists in,
-              BLists wl, unsigned int *max_counts)
+__global__ void k_b_build(size_t n, const uint32_t *__restrict__ starts, int count, const BInst *__restrict__ inst, MPState f,
+              const uint32_t *__restrict__ f_offset, MPWallData w, const uint32_t *__restrict__ w_offset,
+              MPNeighbors in, MPNeighbors wl, unsigned int *max_counts)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
     const BInst &k = inst[find_instance(starts, count, uint32_t(i))];
-    float4 gi = f.geo0[i];
-    int ci[3] = {0, 0, 0};
-    bunpack<D>(__float_as_uint(gi.w), ci);
-    const float oi[3] = {gi.x, gi.y, gi.z};
-    Kahan sigma;
-    unsigned cnt = 0;
-    bfor_each_candidate<D>(k, f_offset, ci, [&](uint32_t j) {
-        if (j == uint32_t(i))
-            return;
-        float dx[3];
-        bgeo_dx<D>(k, ci, oi, f.geo0[j], dx);
-        float r2 = bsq<D>(dx);
-        if (!(r2 < k.rc_sqr))
-            return;
-        if (cnt < in.cap)
-            in.J[size_t(cnt) * n + i] = j;
-        ++cnt;
-        sigma.add(wc2_W(k.fW, k.inv_h, sqrtf(r2)));
-    });
-    Kahan wsig;
-    unsigned wc = 0;
-    bfor_each_candidate<D>(k, w_offset, ci, [&](uint32_t j) {
-        float dx[3];
-        bgeo_dx<D>(k, ci, oi, w.geo[j], dx);
-        float r2 = bsq<D>(dx);
-        if (!(r2 < k.rc_sqr))
-            return;
-        if (wc < wl.cap)
-            wl.J[size_t(wc) * n + i] = j;
-        ++wc;
-        wsig.add(wc2_W(k.fW, k.inv_h, sqrtf(r2)));
-    });
-    in.count[i] = cnt;
-    wl.count[i] = wc;
-    atomicMax(&max_counts[0], cnt);
-    atomicMax(&max_counts[1], wc);
-    double dsig = (double(sigma.s) - k.sigma0) - double(sigma.c) + double(k.fW);
-    f.drho_sum[i] = float(dsig) * k.rho0_over_sigma0 + wsig.value() * k.wall_factor;
+    build_particle<D>(i, n, k.p, Visit{k.m, k.cell_base, f_offset, w_offset}, f, w, in, wl, max_counts);
 }
 
 __global__ void k_b_density(size_t n, const float *__restrict__ drho_sum, float *__restrict__ drho)
@@ -396,8 +257,8 @@ __global__ void k_b_begin(int count, const BInst *__restrict__ inst, BRun *run)
     const BInst &k = inst[b];
     BRun &r = run[b];
     double adv = from_ordered_bits(r.adv), ac = from_ordered_bits(r.ac);
-    r.Dt = k.advection_cfl * k.h / (fmax(sqrt(adv), k.U_ref) + kTinyReal);
-    r.dt = k.acoustic_cfl * k.h / (ac + kTinyReal);
+    r.Dt = k.advection_cfl * k.p.h / (fmax(sqrt(adv), k.U_ref) + kTinyReal);
+    r.dt = k.acoustic_cfl * k.p.h / (ac + kTinyReal);
     r.relax = 0.0;
     r.active = 1;
     r.substeps = 0;
@@ -419,13 +280,12 @@ __global__ void k_b_init1(size_t n, const uint32_t *__restrict__ starts, int cou
         return;
     float r = drho[i] + drho_dt[i] * float(0.5 * run[b].dt);
     drho[i] = r;
-    reinterpret_cast<float *>(dyn)[4 * i + 3] = inst[b].p0_over_rho0 * r;
+    reinterpret_cast<float *>(dyn)[4 * i + 3] = inst[b].p.p0_over_rho0 * r;
 }
 
 template <int D>
-__global__ void __launch_bounds__(256)
-    k_b_first(size_t n, const uint32_t *__restrict__ starts, int count, const BInst *__restrict__ inst, BRun *run,
-              BState f, BWall w, BLists in, BLists wl)
+__global__ void k_b_first(size_t n, const uint32_t *__restrict__ starts, int count, const BInst *__restrict__ inst, BRun *run,
+              MPState f, MPWallData w, MPNeighbors in, MPNeighbors wl)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int b = find_instance(starts, count, uint32_t(i < n ? i : n - 1));
@@ -434,123 +294,15 @@ __global__ void __launch_bounds__(256)
     if (active)
     {
         const BInst &k = inst[b];
-        const double dt = run[b].dt;
-        const float4 gi = f.geo0[i];
-        int ci[3] = {0, 0, 0};
-        bunpack<D>(__float_as_uint(gi.w), ci);
-        const float oi[3] = {gi.x, gi.y, gi.z};
-        const float4 di = f.dyn[i];
-        const float p_i = di.w;
-        const float rho_i = k.rho0 + f.drho[i];
-        Acc force[3], rdis;
-        int g = 0;
-        auto inner_pair = [&](float4 gj, float p_j) {
-            float dx[3];
-            bgeo_dx<D>(k, ci, oi, gj, dx);
-            float r = sqrtf(bsq<D>(dx));
-            float inv = 1.0f / (r + kTinyF);
-            float dWV = wc2_dW(k.fdW, k.inv_h, r) * k.Vol;
-            float sc = (p_i + p_j) * dWV * inv;
-#pragma unroll
-            for (int d = 0; d < D; ++d)
-                force[d].add(-sc * dx[d]);
-            rdis.add((p_i - p_j) * dWV);
-            if (++g == kGroup)
-            {
-#pragma unroll
-                for (int d = 0; d < D; ++d)
-                    force[d].flush();
-                rdis.flush();
-                g = 0;
-            }
-        };
-        const unsigned c = min(in.count[i], in.cap);
-        unsigned s = 0;
-        for (; s + kUnroll <= c; s += kUnroll)
-        {
-            uint32_t jj[kUnroll];
-            float4 gg[kUnroll];
-            float pp[kUnroll];
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u)
-                jj[u] = in.J[size_t(s + u) * n + i];
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u)
-            {
-                gg[u] = __ldg(&f.geo0[jj[u]]);
-                pp[u] = __ldg(&f.dyn[jj[u]].w);
-            }
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u)
-                inner_pair(gg[u], pp[u]);
-        }
-        for (; s < c; ++s)
-        {
-            uint32_t j = in.J[size_t(s) * n + i];
-            inner_pair(__ldg(&f.geo0[j]), __ldg(&f.dyn[j].w));
-        }
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-            force[d].flush();
-        rdis.flush();
-        Acc wforce[3], wrdis;
-        g = 0;
-        const unsigned wc = min(wl.count[i], wl.cap);
-        for (unsigned q = 0; q < wc; ++q)
-        {
-            uint32_t j = wl.J[size_t(q) * n + i];
-            float dx[3];
-            bgeo_dx<D>(k, ci, oi, __ldg(&w.geo[j]), dx);
-            float r = sqrtf(bsq<D>(dx));
-            float inv = 1.0f / (r + kTinyF);
-            float dWV = wc2_dW(k.fdW, k.inv_h, r) * k.wall_Vol;
-            float face = 0.f;
-#pragma unroll
-            for (int d = 0; d < D; ++d)
-                face -= k.g[d] * (dx[d] * inv);
-            float p_w = p_i + rho_i * r * fmaxf(0.0f, face);
-            float sc = (p_i + p_w) * dWV * inv;
-#pragma unroll
-            for (int d = 0; d < D; ++d)
-                wforce[d].add(-sc * dx[d]);
-            wrdis.add((p_i - p_w) * dWV);
-            if (++g == kGroup)
-            {
-#pragma unroll
-                for (int d = 0; d < D; ++d)
-                    wforce[d].flush();
-                wrdis.flush();
-                g = 0;
-            }
-        }
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-            wforce[d].flush();
-        wrdis.flush();
-        f.drho_dt[i] = (rdis.value() * k.inv_z) * rho_i + (wrdis.value() * k.inv_z) * rho_i;
-        float v2 = 0.f;
-        float vn[3] = {di.x, di.y, di.z};
-        const float dt_f = float(dt);
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-        {
-            float F = f.force[d * n + i] + force[d].value() * k.Vol + wforce[d].value() * k.Vol;
-            f.force[d * n + i] = F;
-            float v = vn[d];
-            f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(v));
-            vn[d] = v + (k.g[d] + F * k.inv_mass) * dt_f;
-            v2 += vn[d] * vn[d];
-        }
-        f.dyn[i] = make_float4(vn[0], vn[1], D == 3 ? vn[2] : 0.f, p_i);
-        vmax = k.c0 + double(sqrtf(v2));
+        vmax = first_particle<D, true>(i, n, k.p, Visit{k.m, k.cell_base, nullptr, nullptr}, run[b].dt, f, w, in,
+                                       wl);
     }
     instance_max(run, b, active, vmax, false);
 }
 
 template <int D>
-__global__ void __launch_bounds__(256)
-    k_b_second(size_t n, const uint32_t *__restrict__ starts, int count, const BInst *__restrict__ inst, BRun *run,
-               BState f, BWall w, BLists in, BLists wl)
+__global__ void k_b_second(size_t n, const uint32_t *__restrict__ starts, int count, const BInst *__restrict__ inst, BRun *run,
+               MPState f, MPWallData w, MPNeighbors in, MPNeighbors wl)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     int b = find_instance(starts, count, uint32_t(i < n ? i : n - 1));
@@ -559,118 +311,8 @@ __global__ void __launch_bounds__(256)
     if (active)
     {
         const BInst &k = inst[b];
-        const double dt = run[b].dt;
-        const float4 gi = f.geo0[i];
-        int ci[3] = {0, 0, 0};
-        bunpack<D>(__float_as_uint(gi.w), ci);
-        const float oi[3] = {gi.x, gi.y, gi.z};
-        const float4 di = f.dyn[i];
-        const float vi[3] = {di.x, di.y, di.z};
-        const float rho_i = k.rho0 + f.drho[i];
-        Acc rate, pdis[3];
-        int g = 0;
-        auto inner_pair = [&](float4 gj, float4 dj) {
-            float dx[3];
-            bgeo_dx<D>(k, ci, oi, gj, dx);
-            float r = sqrtf(bsq<D>(dx));
-            float inv = 1.0f / (r + kTinyF);
-            float dWV = wc2_dW(k.fdW, k.inv_h, r) * k.Vol;
-            float u = (vi[0] - dj.x) * dx[0] + (vi[1] - dj.y) * dx[1];
-            if (D == 3)
-                u += (vi[2] - dj.z) * dx[2];
-            u *= inv;
-            rate.add(u * dWV);
-            float sc = p_jump(k.zgeo, k.inv_c0, k.slope, u) * dWV * inv;
-#pragma unroll
-            for (int d = 0; d < D; ++d)
-                pdis[d].add(sc * dx[d]);
-            if (++g == kGroup)
-            {
-                rate.flush();
-#pragma unroll
-                for (int d = 0; d < D; ++d)
-                    pdis[d].flush();
-                g = 0;
-            }
-        };
-        const unsigned c = min(in.count[i], in.cap);
-        unsigned s = 0;
-        for (; s + kUnroll <= c; s += kUnroll)
-        {
-            uint32_t jj[kUnroll];
-            float4 gg[kUnroll], dd[kUnroll];
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u)
-                jj[u] = in.J[size_t(s + u) * n + i];
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u)
-            {
-                gg[u] = __ldg(&f.geo0[jj[u]]);
-                dd[u] = __ldg(&f.dyn[jj[u]]);
-            }
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u)
-                inner_pair(gg[u], dd[u]);
-        }
-        for (; s < c; ++s)
-        {
-            uint32_t j = in.J[size_t(s) * n + i];
-            inner_pair(__ldg(&f.geo0[j]), __ldg(&f.dyn[j]));
-        }
-        rate.flush();
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-            pdis[d].flush();
-        Acc wrate, wdis[3];
-        g = 0;
-        const unsigned wc = min(wl.count[i], wl.cap);
-        for (unsigned q = 0; q < wc; ++q)
-        {
-            uint32_t j = wl.J[size_t(q) * n + i];
-            float dx[3];
-            bgeo_dx<D>(k, ci, oi, __ldg(&w.geo[j]), dx);
-            float r = sqrtf(bsq<D>(dx));
-            float inv = 1.0f / (r + kTinyF);
-            float dWV = wc2_dW(k.fdW, k.inv_h, r) * k.wall_Vol;
-            const float4 nj = __ldg(&w.n[j]);
-            float en = (dx[0] * nj.x + dx[1] * nj.y + (D == 3 ? dx[2] * nj.z : 0.f)) * inv;
-            float ve = (vi[0] * dx[0] + vi[1] * dx[1] + (D == 3 ? vi[2] * dx[2] : 0.f)) * inv;
-            float sgn = en < 0.f ? -1.f : (en > 0.f ? 1.f : 0.f);
-            float vnn = sgn * (vi[0] * nj.x + vi[1] * nj.y + (D == 3 ? vi[2] * nj.z : 0.f));
-            wrate.add(2.0f * ve * dWV);
-            float sc = p_jump(k.zgeo, k.inv_c0, k.slope, 2.0f * vnn) * dWV * sgn;
-            wdis[0].add(sc * nj.x);
-            wdis[1].add(sc * nj.y);
-            if (D == 3)
-                wdis[2].add(sc * nj.z);
-            if (++g == kGroup)
-            {
-                wrate.flush();
-#pragma unroll
-                for (int d = 0; d < D; ++d)
-                    wdis[d].flush();
-                g = 0;
-            }
-        }
-        wrate.flush();
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-            wdis[d].flush();
-        float drho_dt = f.drho_dt[i] + rate.value() * rho_i + wrate.value() * rho_i;
-        f.drho_dt[i] = drho_dt;
-        f.drho[i] = f.drho[i] + drho_dt * float(0.5 * dt);
-        float v2 = 0.f, a2 = 0.f;
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-        {
-            float F = pdis[d].value() * k.Vol + wdis[d].value() * k.Vol;
-            f.force[d * n + i] = F;
-            f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vi[d]));
-            v2 += vi[d] * vi[d];
-            float ft = F + k.mass * k.g[d];
-            a2 += ft * ft;
-        }
-        amax = double(fmaxf(v2, 4.0f * float(k.h) * sqrtf(a2) * k.inv_mass));
+        amax = second_particle<D, true>(i, n, k.p, Visit{k.m, k.cell_base, nullptr, nullptr}, run[b].dt, f, w, in,
+                                        wl);
     }
     instance_max(run, b, active, amax, true);
 }
@@ -703,7 +345,7 @@ __global__ void k_b_control(int count, const BInst *__restrict__ inst, BRun *run
         }
         if (more)
         {
-            r.dt = k.acoustic_cfl * k.h / (from_ordered_bits(r.ac) + kTinyReal);
+            r.dt = k.acoustic_cfl * k.p.h / (from_ordered_bits(r.ac) + kTinyReal);
             r.ac = 0ull;
             r.adv = 0ull;
             atomicOr(&any, 1);
@@ -723,33 +365,24 @@ __global__ void k_b_control(int count, const BInst *__restrict__ inst, BRun *run
 // Initial maxima for the first time steps (all instances).
 template <int D>
 __global__ void k_b_initial_max(size_t n, const uint32_t *__restrict__ starts, int count,
-                                const BInst *__restrict__ inst, BRun *run, BState f)
+                                const BInst *__restrict__ inst, BRun *run, MPState f)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
     int b = find_instance(starts, count, uint32_t(i));
-    const BInst &k = inst[b];
-    float4 di = f.dyn[i];
-    const float v[3] = {di.x, di.y, di.z};
-    double v2 = 0, a2 = 0;
-#pragma unroll
-    for (int d = 0; d < D; ++d)
-    {
-        v2 += double(v[d]) * double(v[d]);
-        double ft = double(f.force[d * n + i]) + double(k.mass) * k.gd[d];
-        a2 += ft * ft;
-    }
-    atomicMax(&run[b].ac, ordered_bits(k.c0 + sqrt(v2)));
-    atomicMax(&run[b].adv, ordered_bits(fmax(v2, 4.0 * k.h * sqrt(a2) * double(k.inv_mass))));
+    double vm, am;
+    initial_max<D>(i, n, inst[b].p, inst[b].gd, f, &vm, &am);
+    atomicMax(&run[b].ac, ordered_bits(vm));
+    atomicMax(&run[b].adv, ordered_bits(am));
 }
 
 template <int D>
 __global__ void k_b_download(size_t n, const uint32_t *__restrict__ starts, int count,
-                             const BInst *__restrict__ inst, BState f, double *__restrict__ out, size_t stride)
+                             const BInst *__restrict__ inst, MPState f, double *__restrict__ out, size_t stride)
 {
     // out rows (SoA, stride = total particles): pos (D), vel (D), rho, p; row index = the
-    // particle's input position start + id
+    // instance's first particle + the particle's index in the instance's input order
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
@@ -757,7 +390,7 @@ __global__ void k_b_download(size_t n, const uint32_t *__restrict__ starts, int 
     const BInst &k = inst[b];
     size_t o = size_t(k.p_start) + f.id[i];
     int c[3];
-    bunpack<D>(__float_as_uint(f.geo0[i].w), c);
+    unpack_cell<D>(__float_as_uint(f.geo0[i].w), c);
     float4 di = f.dyn[i];
     const float v[3] = {di.x, di.y, di.z};
 #pragma unroll
@@ -766,7 +399,7 @@ __global__ void k_b_download(size_t n, const uint32_t *__restrict__ starts, int 
         out[d * stride + o] = cell_corner(k.m, d, c[d]) + double(f.off[d * n + i]);
         out[(D + d) * stride + o] = v[d];
     }
-    out[(2 * D) * stride + o] = double(k.rho0) + double(f.drho[i]);
+    out[(2 * D) * stride + o] = double(k.p.rho0) + double(f.drho[i]);
     out[(2 * D + 1) * stride + o] = di.w;
 }
 
@@ -791,13 +424,13 @@ struct sphx_batch_s
     BRun *h_run = nullptr; // pinned mirror, refreshed after every advection step
     uint32_t *starts = nullptr, *wstarts = nullptr;
     // two state buffers: the configuration update gathers st[parity] into st[parity ^ 1]
-    BState st[2]{};
+    MPState st[2]{};
     int parity = 0;
-    BWall w{};
+    MPWallData w{};
     uint32_t *f_offset = nullptr, *w_offset = nullptr, *cnt = nullptr, *scan_tiles = nullptr;
     uint32_t *key = nullptr, *rank = nullptr, *perm = nullptr, *ncell = nullptr;
     float *noff = nullptr;
-    BLists in{}, wl{};
+    MPNeighbors in{}, wl{};
     unsigned int *d_max = nullptr, *h_max = nullptr;
     int *d_any = nullptr, *h_any = nullptr;
     int block = 128;
@@ -807,7 +440,7 @@ struct sphx_batch_s
     cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
     uint64_t graph_launches = 0;
     std::vector<void *> owned;
-    BState &cur() { return st[parity]; }
+    MPState &cur() { return st[parity]; }
     void invalidate_graphs()
     {
         for (int q = 0; q < 2; ++q)
@@ -833,7 +466,7 @@ namespace
 // sort, gather, build) and by the start of an advection step (density, step start)
 constexpr uint64_t kConfigLaunches = 9, kBeginLaunches = 2, kSubstepLaunches = 4;
 
-int b_alloc_state(sphx_batch bt, BState &s)
+int b_alloc_state(sphx_batch bt, MPState &s)
 {
     size_t n = bt->n, D = size_t(bt->dim);
     s.geo0 = bt->alloc<float4>(n);
@@ -849,7 +482,7 @@ int b_alloc_state(sphx_batch bt, BState &s)
     return SPHX_OK;
 }
 
-int b_alloc_lists(sphx_batch bt, BLists &l, unsigned cap)
+int b_alloc_lists(sphx_batch bt, MPNeighbors &l, unsigned cap)
 {
     if (l.J)
     {
@@ -881,7 +514,7 @@ int b_enqueue_sort(sphx_batch bt, cudaStream_t s, size_t n, uint32_t *offset)
 }
 
 template <int D>
-int b_enqueue_build(sphx_batch bt, cudaStream_t s, const BState &dst)
+int b_enqueue_build(sphx_batch bt, cudaStream_t s, const MPState &dst)
 {
     SPHX_CUDA(cudaMemsetAsync(bt->d_max, 0, 2 * sizeof(unsigned int), s));
     k_b_build<D><<<grid_for(bt->n, 256), 256, 0, s>>>(bt->n, bt->starts, bt->count, bt->inst, dst, bt->f_offset,
@@ -894,7 +527,7 @@ int b_enqueue_build(sphx_batch bt, cudaStream_t s, const BState &dst)
 // Configuration update from src into dst: re-hash (or the hash left by creation), sort,
 // gather, neighbour lists and density sums.  Enqueues only.
 template <int D>
-int b_enqueue_configuration(sphx_batch bt, cudaStream_t s, const BState &src, const BState &dst, bool rehash)
+int b_enqueue_configuration(sphx_batch bt, cudaStream_t s, const MPState &src, const MPState &dst, bool rehash)
 {
     size_t n = bt->n;
     if (rehash)
@@ -939,7 +572,7 @@ int b_check_lists(sphx_batch bt)
 }
 
 template <int D>
-int b_enqueue_begin(sphx_batch bt, cudaStream_t s, const BState &cur)
+int b_enqueue_begin(sphx_batch bt, cudaStream_t s, const MPState &cur)
 {
     size_t n = bt->n;
     k_b_density<<<grid_for(n, 256), 256, 0, s>>>(n, cur.drho_sum, cur.drho);
@@ -950,7 +583,7 @@ int b_enqueue_begin(sphx_batch bt, cudaStream_t s, const BState &cur)
 }
 
 template <int D>
-int b_enqueue_substep(sphx_batch bt, cudaStream_t s, const BState &cur, int use_graph,
+int b_enqueue_substep(sphx_batch bt, cudaStream_t s, const MPState &cur, int use_graph,
                       cudaGraphConditionalHandle handle)
 {
     size_t n = bt->n;
@@ -984,7 +617,7 @@ int capture_into(cudaStream_t s, cudaGraph_t *out, F &&enqueue)
 template <int D>
 int b_build_graph(sphx_batch bt, int q)
 {
-    const BState src = bt->st[q], dst = bt->st[q ^ 1];
+    const MPState src = bt->st[q], dst = bt->st[q ^ 1];
     cudaStream_t s = bt->capture;
     cudaGraph_t g = nullptr, pre = nullptr, post = nullptr;
     auto done = [&](int code) {
@@ -1045,7 +678,7 @@ int b_advection_step(sphx_batch bt, int use_graph)
     sphx_ctx ctx = bt->ctx;
     cudaStream_t s = ctx->stream;
     const int q = bt->parity;
-    const BState src = bt->st[q], dst = bt->st[q ^ 1];
+    const MPState src = bt->st[q], dst = bt->st[q ^ 1];
     uint64_t loops = 0;
     if (use_graph)
     {
@@ -1152,7 +785,7 @@ extern "C" int sphx_batch_create(sphx_ctx ctx, int dim, int count, const sphx_ba
         size_t cells = 1;
         for (int a = 0; a < D; ++a)
         {
-            int lim = D == 2 ? 32768 : 1024;
+            int lim = D == 2 ? CellLanes<2>::max_cells : CellLanes<3>::max_cells;
             if (d.mesh.all_cells[a] < 1 || d.mesh.all_cells[a] > lim)
                 return bail(fail(SPHX_ERR_INVALID_ARG, "instance %d: %d cells on axis %d (at most %d)", q,
                                  d.mesh.all_cells[a], a, lim));
@@ -1167,33 +800,10 @@ extern "C" int sphx_batch_create(sphx_ctx ctx, int dim, int count, const sphx_ba
         k.p_count = uint32_t(d.n_fluid);
         k.w_start = uint32_t(nw);
         k.w_count = uint32_t(d.n_wall);
-        WendlandC2 wk = wendland(D, d.h);
-        k.gs_f = float(d.mesh.grid_spacing);
-        k.rc_sqr = float(wk.rc_sqr);
-        k.inv_h = float(wk.inv_h);
-        k.fW = float(wk.factor_W);
-        k.fdW = float(wk.factor_dW);
-        k.rho0 = float(d.rho0);
-        k.p0_over_rho0 = float(d.rho0 * d.c0 * d.c0 / d.rho0);
-        k.Vol = float(d.fluid_vol);
-        k.mass = float(d.fluid_mass);
-        k.inv_mass = float(1.0 / d.fluid_mass);
-        k.sigma0 = d.sigma0;
-        k.rho0_over_sigma0 = float(d.rho0 / d.sigma0);
-        k.wall_factor = float(1.0 / d.wall_rho0 * d.wall_mass * d.rho0 * d.rho0 / (d.sigma0 * d.fluid_mass));
-        k.wall_Vol = float(d.wall_vol);
-        double Z = d.rho0 * d.c0;
-        k.inv_z = float((Z + Z) / (Z * Z + Z * Z));
-        k.zgeo = float(2.0 * Z * Z / (Z + Z));
-        k.inv_c0 = float(0.5 * (d.rho0 + d.rho0) * double(k.inv_z));
-        k.slope = 3.0f;
         for (int a = 0; a < 3; ++a)
-        {
             k.gd[a] = a < D ? d.gravity[a] : 0.0;
-            k.g[a] = float(k.gd[a]);
-        }
-        k.h = d.h;
-        k.c0 = d.c0;
+        k.p = make_params(D, d.mesh.grid_spacing, d.h, d.rho0, d.c0, d.fluid_vol, d.fluid_mass, d.sigma0,
+                          1.0 / d.wall_rho0 * d.wall_mass, d.wall_vol, 3.0, k.gd);
         k.acoustic_cfl = 0.6;
         k.advection_cfl = 0.25;
         k.U_ref = d.U_ref;
@@ -1282,7 +892,7 @@ extern "C" int sphx_batch_create(sphx_ctx ctx, int dim, int count, const sphx_ba
         return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "staging allocation failed"));
     }
     cudaStream_t s = ctx->stream;
-    const BState &a0 = bt->st[0];
+    const MPState &a0 = bt->st[0];
     bool ok =
         cudaMemcpy(d_fpos, fpos.data(), fpos.size() * 8, cudaMemcpyHostToDevice) == cudaSuccess &&
         (wpos.empty() || cudaMemcpy(d_wpos, wpos.data(), wpos.size() * 8, cudaMemcpyHostToDevice) == cudaSuccess) &&

@@ -8,7 +8,8 @@
 //
 // Layout (cell order, re-sorted at every configuration update):
 //   geo0   float4  {offset from the cell's lower corner at the last configuration
-//                   update (x, y, z), packed integer cell coordinates (10 bits per axis)}
+//                   update (x, y, z), packed integer cell coordinates (15 bits per axis
+//                   in 2D, 10 in 3D)}
 //   dyn    float4  {velocity (x, y, z), pressure}
 //   off    float3  current offset from the same cell corner (SoA)
 //   force  float3 (SoA); drho = rho - rho0, drho_dt, drho_sum (density summation) float
@@ -25,176 +26,28 @@
 #include <cmath>
 #include <vector>
 
+#include "mp_common.cuh"
 #include "sphx_device.cuh"
 #include "sphx_internal.cuh"
 
 using namespace sphx;
+using namespace sphx::mpc;
 
 namespace
 {
-constexpr float kTinyF = 2.71051e-20f;
-constexpr int kGroup = 8;  // neighbours per plain partial sum
-constexpr int kUnroll = 4; // neighbour records in flight per thread in the list sweeps
-
-struct Kahan
-{
-    float s = 0.f, c = 0.f;
-    __device__ __forceinline__ void add(float x)
-    {
-        float y = x - c;
-        float t = s + y;
-        c = (t - s) - y;
-        s = t;
-    }
-    __device__ __forceinline__ float value() const { return s - c; }
-};
-
-// Compensated neighbour sum: plain FP32 partials over groups, Kahan across groups.
-struct Acc
-{
-    float part = 0.f;
-    Kahan k;
-    __device__ __forceinline__ void add(float x) { part += x; }
-    __device__ __forceinline__ void flush()
-    {
-        k.add(part);
-        part = 0.f;
-    }
-    __device__ __forceinline__ float value() const { return k.value(); }
-};
-
-__host__ __device__ __forceinline__ uint32_t pack_cell(int cx, int cy, int cz)
-{
-    return uint32_t(cx) | (uint32_t(cy) << 10) | (uint32_t(cz) << 20);
-}
-__device__ __forceinline__ void unpack_cell(uint32_t p, int *c)
-{
-    c[0] = int(p & 1023u);
-    c[1] = int((p >> 10) & 1023u);
-    c[2] = int((p >> 20) & 1023u);
-}
-
 struct MPConst
 {
     MeshDev m;
-    float gs_f;
-    // kernel
-    float rc_sqr, inv_h, fW, fdW;
-    // fluid
-    float rho0, p0_over_rho0, Vol, mass, inv_mass;
-    double sigma0;
-    float rho0_over_sigma0, wall_factor; // wall_factor = rho0^2 / (sigma0 m) * (m_w / rho0_w)
-    float wall_Vol;
-    // Riemann solver
-    float inv_z, zgeo, inv_c0, slope;
-    float g[3];
+    MPParams p;
     double gd[3];
-    // time steps
-    double h, c0, acoustic_cfl, advection_cfl, U_ref;
+    double acoustic_cfl, advection_cfl, U_ref;
 };
-
-struct MPFluid
+using MPFluid = MPState;
+using MPLists = MPNeighbors;
+struct MPWall : MPWallData
 {
-    float4 *geo0, *dyn;
-    float *off, *force, *drho, *drho_dt, *drho_sum;
-    uint32_t *id;
-};
-
-struct MPWall
-{
-    float4 *geo, *n;
     size_t nw;
 };
-
-struct MPLists
-{
-    uint32_t *count, *J;
-    unsigned cap;
-};
-
-// ---------------------------------------------------------------- geometry helpers
-template <int D>
-__device__ __forceinline__ void geo_dx(const MPConst &k, const int *ci, const float *oi, float4 gj, float *dx)
-{
-    int cj[3];
-    unpack_cell(__float_as_uint(gj.w), cj);
-    dx[0] = float(ci[0] - cj[0]) * k.gs_f + (oi[0] - gj.x);
-    dx[1] = float(ci[1] - cj[1]) * k.gs_f + (oi[1] - gj.y);
-    if (D == 3)
-        dx[2] = float(ci[2] - cj[2]) * k.gs_f + (oi[2] - gj.z);
-}
-
-template <int D>
-__device__ __forceinline__ float sq(const float *dx)
-{
-    float s = dx[0] * dx[0] + dx[1] * dx[1];
-    if (D == 3)
-        s += dx[2] * dx[2];
-    return s;
-}
-
-__device__ __forceinline__ float wendland_W(const MPConst &k, float r)
-{
-    float q = r * k.inv_h;
-    float t = 1.0f - 0.5f * q;
-    float t2 = t * t;
-    return k.fW * (t2 * t2 * (1.0f + 2.0f * q));
-}
-__device__ __forceinline__ float wendland_dW(const MPConst &k, float r)
-{
-    float q = r * k.inv_h;
-    float t = q - 2.0f;
-    return k.fdW * (0.625f * (t * t * t) * q);
-}
-
-__device__ __forceinline__ float p_jump(const MPConst &k, float u)
-{
-    return k.zgeo * u * fminf(k.slope * (k.inv_c0 * fmaxf(u, 0.0f)), 1.0f);
-}
-
-__device__ __forceinline__ void block_max_slot(unsigned long long *slot, double v)
-{
-    unsigned long long b = ordered_bits(v);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-    {
-        unsigned long long y = __shfl_down_sync(0xffffffffu, b, o);
-        b = y > b ? y : b;
-    }
-    if ((threadIdx.x & 31u) == 0)
-        atomicMax(slot, b);
-}
-
-// Visits the candidate particles of the 3^D cells around cell c: along the last axis the
-// cells are consecutive in linear order, so each (x[, y]) column is one contiguous range.
-template <int D, class F>
-__device__ __forceinline__ void for_each_candidate(const MeshDev &m, const uint32_t *offset, const int *c, F &&f)
-{
-    int lo0 = max(c[0] - 1, 0), hi0 = min(c[0] + 1, m.all_cells[0] - 1);
-    int lo1 = max(c[1] - 1, 0), hi1 = min(c[1] + 1, m.all_cells[1] - 1);
-    if (D == 2)
-    {
-        for (int x = lo0; x <= hi0; ++x)
-        {
-            uint32_t a = uint32_t(x) * uint32_t(m.all_cells[1]);
-            uint32_t b = offset[a + uint32_t(lo1)], e = offset[a + uint32_t(hi1) + 1];
-            for (uint32_t j = b; j < e; ++j)
-                f(j);
-        }
-    }
-    else
-    {
-        int lo2 = max(c[2] - 1, 0), hi2 = min(c[2] + 1, m.all_cells[2] - 1);
-        for (int x = lo0; x <= hi0; ++x)
-            for (int y = lo1; y <= hi1; ++y)
-            {
-                uint32_t a = (uint32_t(x) * uint32_t(m.all_cells[1]) + uint32_t(y)) * uint32_t(m.all_cells[2]);
-                uint32_t b = offset[a + uint32_t(lo2)], e = offset[a + uint32_t(hi2) + 1];
-                for (uint32_t j = b; j < e; ++j)
-                    f(j);
-            }
-    }
-}
 
 // ---------------------------------------------------------------- (re)hash + sort
 // From FP64 body positions (creation).
@@ -215,7 +68,7 @@ __global__ void k_mp_from_fp64(size_t n, const double *__restrict__ pos, MeshDev
 #pragma unroll
     for (int d = 0; d < D; ++d)
         noff[d * n + i] = float(x[d] - cell_corner(m, d, c[d]));
-    ncell[i] = pack_cell(c[0], c[1], c[2]);
+    ncell[i] = pack_cell<D>(c);
     uint32_t lc = linear_cell<D>(m, c);
     key[i] = lc;
     rank[i] = atomicAdd(&count[lc], 1u);
@@ -231,7 +84,7 @@ __global__ void k_mp_rehash(size_t n, const float4 *__restrict__ geo0, const flo
     if (i >= n)
         return;
     int c0[3];
-    unpack_cell(__float_as_uint(geo0[i].w), c0);
+    unpack_cell<D>(__float_as_uint(geo0[i].w), c0);
     double x[3] = {0, 0, 0};
 #pragma unroll
     for (int d = 0; d < D; ++d)
@@ -241,7 +94,7 @@ __global__ void k_mp_rehash(size_t n, const float4 *__restrict__ geo0, const flo
 #pragma unroll
     for (int d = 0; d < D; ++d)
         noff[d * n + i] = float(x[d] - cell_corner(m, d, c[d]));
-    ncell[i] = pack_cell(c[0], c[1], c[2]);
+    ncell[i] = pack_cell<D>(c);
     uint32_t lc = linear_cell<D>(m, c);
     key[i] = lc;
     rank[i] = atomicAdd(&count[lc], 1u);
@@ -302,52 +155,12 @@ __global__ void k_mp_gather(size_t n, const uint32_t *__restrict__ perm, const u
 
 // ---------------------------------------------------------------- configuration + density sums
 template <int D>
-__global__ void __launch_bounds__(256)
-    k_mp_build(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
+__global__ void k_mp_build(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
                const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, unsigned int *max_counts)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n)
-        return;
-    float4 gi = f.geo0[i];
-    int ci[3] = {0, 0, 0};
-    unpack_cell(__float_as_uint(gi.w), ci);
-    const float oi[3] = {gi.x, gi.y, gi.z};
-    Kahan sigma;
-    unsigned cnt = 0;
-    for_each_candidate<D>(k.m, f_offset, ci, [&](uint32_t j) {
-        if (j == uint32_t(i))
-            return;
-        float dx[3];
-        geo_dx<D>(k, ci, oi, f.geo0[j], dx);
-        float r2 = sq<D>(dx);
-        if (!(r2 < k.rc_sqr))
-            return;
-        if (cnt < in.cap)
-            in.J[size_t(cnt) * n + i] = j;
-        ++cnt;
-        sigma.add(wendland_W(k, sqrtf(r2)));
-    });
-    Kahan wsig;
-    unsigned wc = 0;
-    for_each_candidate<D>(k.m, w_offset, ci, [&](uint32_t j) {
-        float dx[3];
-        geo_dx<D>(k, ci, oi, w.geo[j], dx);
-        float r2 = sq<D>(dx);
-        if (!(r2 < k.rc_sqr))
-            return;
-        if (wc < wl.cap)
-            wl.J[size_t(wc) * n + i] = j;
-        ++wc;
-        wsig.add(wendland_W(k, sqrtf(r2)));
-    });
-    in.count[i] = cnt;
-    wl.count[i] = wc;
-    atomicMax(&max_counts[0], cnt);
-    atomicMax(&max_counts[1], wc);
-    // rho_sum - rho0 = rho0 (W0 + sum W - sigma0) / sigma0 + wall term
-    double dsig = (double(sigma.s) - k.sigma0) - double(sigma.c) + double(k.fW);
-    f.drho_sum[i] = float(dsig) * k.rho0_over_sigma0 + wsig.value() * k.wall_factor;
+    if (i < n)
+        build_particle<D>(i, n, k.p, Visit{k.m, 0u, f_offset, w_offset}, f, w, in, wl, max_counts);
 }
 
 // DensitySummation update with the FreeSurface rule rho = max(rho_sum, rho0), at the
@@ -372,288 +185,27 @@ __global__ void k_mp_init1(size_t n, float *__restrict__ drho, const float *__re
 }
 
 template <int D, bool LISTS>
-__global__ void __launch_bounds__(256)
-    k_mp_first(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
+__global__ void k_mp_first(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
                const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, double dt,
                unsigned long long *ac_slot)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     double vmax = -1.0e300;
     if (i < n)
-    {
-        const float4 gi = f.geo0[i];
-        int ci[3] = {0, 0, 0};
-        unpack_cell(__float_as_uint(gi.w), ci);
-        const float oi[3] = {gi.x, gi.y, gi.z};
-        const float4 di = f.dyn[i];
-        const float p_i = di.w;
-        const float rho_i = k.rho0 + f.drho[i];
-        Acc force[3], rdis;
-        int g = 0;
-        auto inner_pair = [&](uint32_t j, float4 gj, float p_j) {
-            float dx[3];
-            geo_dx<D>(k, ci, oi, gj, dx);
-            float r2 = sq<D>(dx);
-            if (!LISTS && (!(r2 < k.rc_sqr) || j == uint32_t(i)))
-                return;
-            float r = sqrtf(r2);
-            float inv = 1.0f / (r + kTinyF);
-            float dWV = wendland_dW(k, r) * k.Vol;
-            float sc = (p_i + p_j) * dWV * inv;
-#pragma unroll
-            for (int d = 0; d < D; ++d)
-                force[d].add(-sc * dx[d]);
-            rdis.add((p_i - p_j) * dWV);
-            if (++g == kGroup)
-            {
-#pragma unroll
-                for (int d = 0; d < D; ++d)
-                    force[d].flush();
-                rdis.flush();
-                g = 0;
-            }
-        };
-        auto inner = [&](uint32_t j) { inner_pair(j, f.geo0[j], f.dyn[j].w); };
-        if (LISTS)
-        {
-            // kUnroll neighbours' indices and 16-byte records are in flight before any
-            // arithmetic; the summation order is the list order either way
-            const unsigned c = min(in.count[i], in.cap);
-            unsigned s = 0;
-            for (; s + kUnroll <= c; s += kUnroll)
-            {
-                uint32_t jj[kUnroll];
-                float4 gg[kUnroll];
-                float pp[kUnroll];
-#pragma unroll
-                for (int u = 0; u < kUnroll; ++u)
-                    jj[u] = in.J[size_t(s + u) * n + i];
-#pragma unroll
-                for (int u = 0; u < kUnroll; ++u)
-                {
-                    gg[u] = __ldg(&f.geo0[jj[u]]);
-                    pp[u] = __ldg(&f.dyn[jj[u]].w);
-                }
-#pragma unroll
-                for (int u = 0; u < kUnroll; ++u)
-                    inner_pair(jj[u], gg[u], pp[u]);
-            }
-            for (; s < c; ++s)
-            {
-                uint32_t j = in.J[size_t(s) * n + i];
-                inner_pair(j, __ldg(&f.geo0[j]), __ldg(&f.dyn[j].w));
-            }
-        }
-        else
-            for_each_candidate<D>(k.m, f_offset, ci, inner);
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-            force[d].flush();
-        rdis.flush();
-        Acc wforce[3], wrdis;
-        g = 0;
-        auto wall = [&](uint32_t j) {
-            float dx[3];
-            geo_dx<D>(k, ci, oi, w.geo[j], dx);
-            float r2 = sq<D>(dx);
-            if (!LISTS && !(r2 < k.rc_sqr))
-                return;
-            float r = sqrtf(r2);
-            float inv = 1.0f / (r + kTinyF);
-            float dWV = wendland_dW(k, r) * k.wall_Vol;
-            float face = 0.f; // (F_prior/m - a_wall) . (-e), static wall
-#pragma unroll
-            for (int d = 0; d < D; ++d)
-                face -= k.g[d] * (dx[d] * inv);
-            float p_w = p_i + rho_i * r * fmaxf(0.0f, face);
-            float sc = (p_i + p_w) * dWV * inv;
-#pragma unroll
-            for (int d = 0; d < D; ++d)
-                wforce[d].add(-sc * dx[d]);
-            wrdis.add((p_i - p_w) * dWV);
-            if (++g == kGroup)
-            {
-#pragma unroll
-                for (int d = 0; d < D; ++d)
-                    wforce[d].flush();
-                wrdis.flush();
-                g = 0;
-            }
-        };
-        if (LISTS)
-        {
-            unsigned c = min(wl.count[i], wl.cap);
-            for (unsigned s = 0; s < c; ++s)
-                wall(wl.J[size_t(s) * n + i]);
-        }
-        else
-            for_each_candidate<D>(k.m, w_offset, ci, wall);
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-            wforce[d].flush();
-        wrdis.flush();
-        f.drho_dt[i] = (rdis.value() * k.inv_z) * rho_i + (wrdis.value() * k.inv_z) * rho_i;
-        float v2 = 0.f;
-        float vn[3] = {di.x, di.y, di.z};
-        const float dt_f = float(dt);
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-        {
-            float F = f.force[d * n + i] + force[d].value() * k.Vol + wforce[d].value() * k.Vol;
-            f.force[d * n + i] = F;
-            float v = vn[d];
-            // position half-step in FP64 (initialization of the 1st half, old velocity)
-            f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(v));
-            vn[d] = v + (k.g[d] + F * k.inv_mass) * dt_f;
-            v2 += vn[d] * vn[d];
-        }
-        // same pressure as read by the neighbours of this sweep
-        f.dyn[i] = make_float4(vn[0], vn[1], D == 3 ? vn[2] : 0.f, p_i);
-        vmax = k.c0 + double(sqrtf(v2));
-    }
-    block_max_slot(ac_slot, vmax);
+        vmax = first_particle<D, LISTS>(i, n, k.p, Visit{k.m, 0u, f_offset, w_offset}, dt, f, w, in, wl);
+    warp_max_to(ac_slot, vmax);
 }
 
 template <int D, bool LISTS>
-__global__ void __launch_bounds__(256)
-    k_mp_second(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
+__global__ void k_mp_second(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
                 const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, double dt,
                 unsigned long long *adv_slot)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     double amax = -1.0e300;
     if (i < n)
-    {
-        const float4 gi = f.geo0[i];
-        int ci[3] = {0, 0, 0};
-        unpack_cell(__float_as_uint(gi.w), ci);
-        const float oi[3] = {gi.x, gi.y, gi.z};
-        const float4 di = f.dyn[i];
-        const float vi[3] = {di.x, di.y, di.z};
-        const float rho_i = k.rho0 + f.drho[i];
-        Acc rate, pdis[3];
-        int g = 0;
-        auto inner_pair = [&](uint32_t j, float4 gj, float4 dj) {
-            float dx[3];
-            geo_dx<D>(k, ci, oi, gj, dx);
-            float r2 = sq<D>(dx);
-            if (!LISTS && (!(r2 < k.rc_sqr) || j == uint32_t(i)))
-                return;
-            float r = sqrtf(r2);
-            float inv = 1.0f / (r + kTinyF);
-            float dWV = wendland_dW(k, r) * k.Vol;
-            float u = (vi[0] - dj.x) * dx[0] + (vi[1] - dj.y) * dx[1];
-            if (D == 3)
-                u += (vi[2] - dj.z) * dx[2];
-            u *= inv;
-            rate.add(u * dWV);
-            float sc = p_jump(k, u) * dWV * inv;
-#pragma unroll
-            for (int d = 0; d < D; ++d)
-                pdis[d].add(sc * dx[d]);
-            if (++g == kGroup)
-            {
-                rate.flush();
-#pragma unroll
-                for (int d = 0; d < D; ++d)
-                    pdis[d].flush();
-                g = 0;
-            }
-        };
-        auto inner = [&](uint32_t j) { inner_pair(j, f.geo0[j], f.dyn[j]); };
-        if (LISTS)
-        {
-            const unsigned c = min(in.count[i], in.cap);
-            unsigned s = 0;
-            for (; s + kUnroll <= c; s += kUnroll)
-            {
-                uint32_t jj[kUnroll];
-                float4 gg[kUnroll], dd[kUnroll];
-#pragma unroll
-                for (int u = 0; u < kUnroll; ++u)
-                    jj[u] = in.J[size_t(s + u) * n + i];
-#pragma unroll
-                for (int u = 0; u < kUnroll; ++u)
-                {
-                    gg[u] = __ldg(&f.geo0[jj[u]]);
-                    dd[u] = __ldg(&f.dyn[jj[u]]);
-                }
-#pragma unroll
-                for (int u = 0; u < kUnroll; ++u)
-                    inner_pair(jj[u], gg[u], dd[u]);
-            }
-            for (; s < c; ++s)
-            {
-                uint32_t j = in.J[size_t(s) * n + i];
-                inner_pair(j, __ldg(&f.geo0[j]), __ldg(&f.dyn[j]));
-            }
-        }
-        else
-            for_each_candidate<D>(k.m, f_offset, ci, inner);
-        rate.flush();
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-            pdis[d].flush();
-        Acc wrate, wdis[3];
-        g = 0;
-        auto wall = [&](uint32_t j) {
-            float dx[3];
-            geo_dx<D>(k, ci, oi, w.geo[j], dx);
-            float r2 = sq<D>(dx);
-            if (!LISTS && !(r2 < k.rc_sqr))
-                return;
-            float r = sqrtf(r2);
-            float inv = 1.0f / (r + kTinyF);
-            float dWV = wendland_dW(k, r) * k.wall_Vol;
-            const float4 nj = w.n[j];
-            float en = (dx[0] * nj.x + dx[1] * nj.y + (D == 3 ? dx[2] * nj.z : 0.f)) * inv;
-            float ve = (vi[0] * dx[0] + vi[1] * dx[1] + (D == 3 ? vi[2] * dx[2] : 0.f)) * inv;
-            float sgn = en < 0.f ? -1.f : (en > 0.f ? 1.f : 0.f);
-            float vn = sgn * (vi[0] * nj.x + vi[1] * nj.y + (D == 3 ? vi[2] * nj.z : 0.f));
-            wrate.add(2.0f * ve * dWV); // (v_i - (2 v_wall - v_i)) . e with a static wall
-            float sc = p_jump(k, 2.0f * vn) * dWV * sgn;
-            wdis[0].add(sc * nj.x);
-            wdis[1].add(sc * nj.y);
-            if (D == 3)
-                wdis[2].add(sc * nj.z);
-            if (++g == kGroup)
-            {
-                wrate.flush();
-#pragma unroll
-                for (int d = 0; d < D; ++d)
-                    wdis[d].flush();
-                g = 0;
-            }
-        };
-        if (LISTS)
-        {
-            unsigned c = min(wl.count[i], wl.cap);
-            for (unsigned s = 0; s < c; ++s)
-                wall(wl.J[size_t(s) * n + i]);
-        }
-        else
-            for_each_candidate<D>(k.m, w_offset, ci, wall);
-        wrate.flush();
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-            wdis[d].flush();
-        float drho_dt = f.drho_dt[i] + rate.value() * rho_i + wrate.value() * rho_i;
-        f.drho_dt[i] = drho_dt;
-        f.drho[i] = f.drho[i] + drho_dt * float(0.5 * dt);
-        float v2 = 0.f, a2 = 0.f;
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-        {
-            float F = pdis[d].value() * k.Vol + wdis[d].value() * k.Vol;
-            f.force[d * n + i] = F;
-            f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vi[d]));
-            v2 += vi[d] * vi[d];
-            float ft = F + k.mass * k.g[d];
-            a2 += ft * ft;
-        }
-        amax = double(fmaxf(v2, 4.0f * float(k.h) * sqrtf(a2) * k.inv_mass));
-    }
-    block_max_slot(adv_slot, amax);
+        amax = second_particle<D, LISTS>(i, n, k.p, Visit{k.m, 0u, f_offset, w_offset}, dt, f, w, in, wl);
+    warp_max_to(adv_slot, amax);
 }
 
 template <int D>
@@ -663,22 +215,9 @@ __global__ void k_mp_initial_max(size_t n, MPConst k, MPFluid f, unsigned long l
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     double am = -1.0e300, vm = -1.0e300;
     if (i < n)
-    {
-        float4 di = f.dyn[i];
-        const float v[3] = {di.x, di.y, di.z};
-        double v2 = 0, a2 = 0;
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-        {
-            v2 += double(v[d]) * double(v[d]);
-            double ft = double(f.force[d * n + i]) + double(k.mass) * k.gd[d];
-            a2 += ft * ft;
-        }
-        vm = k.c0 + sqrt(v2);
-        am = fmax(v2, 4.0 * k.h * sqrt(a2) * double(k.inv_mass));
-    }
-    block_max_slot(ac_slot, vm);
-    block_max_slot(adv_slot, am);
+        initial_max<D>(i, n, k.p, k.gd, f, &vm, &am);
+    warp_max_to(ac_slot, vm);
+    warp_max_to(adv_slot, am);
 }
 
 // ---------------------------------------------------------------- FP64 body -> FP32 state
@@ -724,7 +263,7 @@ __global__ void k_mp_download(size_t n, MPConst k, MPFluid f, double *__restrict
         return;
     uint32_t o = f.id[i];
     int c[3];
-    unpack_cell(__float_as_uint(f.geo0[i].w), c);
+    unpack_cell<D>(__float_as_uint(f.geo0[i].w), c);
     float4 di = f.dyn[i];
     const float v[3] = {di.x, di.y, di.z};
 #pragma unroll
@@ -734,7 +273,7 @@ __global__ void k_mp_download(size_t n, MPConst k, MPFluid f, double *__restrict
         vel[d * n + o] = v[d];
         force[d * n + o] = f.force[d * n + i];
     }
-    rho[o] = double(k.rho0) + double(f.drho[i]);
+    rho[o] = double(k.p.rho0) + double(f.drho[i]);
     p[o] = di.w; // pressure of the last 1st-half initialisation, as the FP64 body holds it
     drho_dt[o] = f.drho_dt[i];
 }
@@ -746,10 +285,10 @@ __global__ void k_mp_conservation(size_t n, MPConst k, MPFluid f, double *__rest
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
     {
         int c[3];
-        unpack_cell(__float_as_uint(f.geo0[i].w), c);
+        unpack_cell<D>(__float_as_uint(f.geo0[i].w), c);
         float4 di = f.dyn[i];
         const float vv[3] = {di.x, di.y, di.z};
-        double m = k.mass, v2 = 0, gx = 0;
+        double m = k.p.mass, v2 = 0, gx = 0;
         s[0] += m;
 #pragma unroll
         for (int d = 0; d < D; ++d)
@@ -786,7 +325,7 @@ __global__ void k_mp_upper_front(size_t n, MPConst k, MPFluid f, int axis, doubl
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
     {
         int c[3];
-        unpack_cell(__float_as_uint(f.geo0[i].w), c);
+        unpack_cell<D>(__float_as_uint(f.geo0[i].w), c);
         double x[3];
         bool in = true;
 #pragma unroll
@@ -798,7 +337,7 @@ __global__ void k_mp_upper_front(size_t n, MPConst k, MPFluid f, int axis, doubl
         if (in)
             m = fmax(m, x[axis]);
     }
-    block_max_slot(slot, m);
+    warp_max_to(slot, m);
 }
 
 template <int D>
@@ -823,7 +362,7 @@ __global__ void k_wall_load(size_t nw, const uint32_t *__restrict__ perm, const 
         o[d] = float(x[d] - cell_corner(m, d, c[d]));
         nn[d] = float(nrm[d * nw + i]);
     }
-    geo[k] = make_float4(o[0], o[1], o[2], __uint_as_float(pack_cell(c[0], c[1], c[2])));
+    geo[k] = make_float4(o[0], o[1], o[2], __uint_as_float(pack_cell<D>(c)));
     n_out[k] = make_float4(nn[0], nn[1], nn[2], 0.f);
 }
 
@@ -1014,7 +553,7 @@ int substep(sphx_mp mp, double dt)
     if (n == 0)
         return SPHX_OK;
     unsigned blk = unsigned(mp->block);
-    k_mp_init1<<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.drho, mp->a.drho_dt, mp->a.dyn, mp->k.p0_over_rho0,
+    k_mp_init1<<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.drho, mp->a.drho_dt, mp->a.dyn, mp->k.p.p0_over_rho0,
                                                 float(0.5 * dt));
     SPHX_LAUNCHED(ctx);
     SPHX_CUDA(cudaMemsetAsync(mp->slots, 0, 2 * sizeof(unsigned long long), s));
@@ -1055,7 +594,7 @@ int advection_step(sphx_mp mp, int loop_style, int *substeps, double *adv_dt)
 {
     double adv_max;
     SPHX_TRY(read_slot(mp, 1, &adv_max));
-    double Dt = mp->k.advection_cfl * mp->k.h / (std::max(std::sqrt(adv_max), mp->k.U_ref) + kTinyReal);
+    double Dt = mp->k.advection_cfl * mp->k.p.h / (std::max(std::sqrt(adv_max), mp->k.U_ref) + kTinyReal);
     if (mp->n > 0)
     {
         k_mp_density<<<grid_for(mp->n, 256), 256, 0, mp->ctx->stream>>>(mp->n, mp->a.drho_sum, mp->a.drho);
@@ -1069,13 +608,13 @@ int advection_step(sphx_mp mp, int loop_style, int *substeps, double *adv_dt)
         if (loop_style == 0) // AcousticTimeStep before the relaxation (Dambreak.cpp:184)
         {
             SPHX_TRY(read_slot(mp, 0, &ac));
-            dt = mp->k.acoustic_cfl * mp->k.h / (ac + kTinyReal);
+            dt = mp->k.acoustic_cfl * mp->k.p.h / (ac + kTinyReal);
         }
         SPHX_TRY(substep<D>(mp, dt));
         if (loop_style == 1) // after it (test_3d_dambreak/dambreak.cpp:197)
         {
             SPHX_TRY(read_slot(mp, 0, &ac));
-            dt = mp->k.acoustic_cfl * mp->k.h / (ac + kTinyReal);
+            dt = mp->k.acoustic_cfl * mp->k.p.h / (ac + kTinyReal);
         }
         relaxation += dt;
         mp->physical_time += dt;
@@ -1178,10 +717,11 @@ extern "C" int sphx_mp_create(sphx_relation inner, sphx_relation wall, const sph
     const int D = fb->dim;
     sphx_ctx ctx = fb->ctx;
     const sphx_mesh_desc &mesh = inner->cl->mesh;
+    const int max_cells = D == 2 ? CellLanes<2>::max_cells : CellLanes<3>::max_cells;
     for (int a = 0; a < D; ++a)
-        if (mesh.all_cells[a] > 1024)
-            return fail(SPHX_ERR_INVALID_ARG, "mixed precision packs 10 bits per cell axis; axis %d has %d cells", a,
-                        mesh.all_cells[a]);
+        if (mesh.all_cells[a] > max_cells)
+            return fail(SPHX_ERR_INVALID_ARG, "mixed precision packs %d bits per cell axis; axis %d has %d cells",
+                        D == 2 ? CellLanes<2>::bits : CellLanes<3>::bits, a, mesh.all_cells[a]);
     if (std::abs(wall->cl->mesh.grid_spacing - mesh.grid_spacing) > 0 ||
         std::abs(2.0 * p->h - mesh.grid_spacing) > 1e-12 * mesh.grid_spacing)
         return fail(SPHX_ERR_INVALID_ARG, "mixed precision needs one mesh with grid spacing equal to the cut-off");
@@ -1235,34 +775,11 @@ extern "C" int sphx_mp_create(sphx_relation inner, sphx_relation wall, const sph
     mp->ncells = nc;
     MPConst &k = mp->k;
     k.m = mesh_dev(mesh);
-    k.gs_f = float(mesh.grid_spacing);
-    WendlandC2 wk = wendland(D, p->h);
-    k.rc_sqr = float(wk.rc_sqr);
-    k.inv_h = float(wk.inv_h);
-    k.fW = float(wk.factor_W);
-    k.fdW = float(wk.factor_dW);
-    k.rho0 = float(p->rho0);
-    k.p0_over_rho0 = float(p->rho0 * p->c0 * p->c0 / p->rho0);
-    k.Vol = float(vol[0]);
-    k.mass = float(mass[0]);
-    k.inv_mass = float(1.0 / mass[0]);
-    k.sigma0 = p->sigma0;
-    k.rho0_over_sigma0 = float(p->rho0 / p->sigma0);
     double wm = wmass.empty() ? 0.0 : wmass[0];
-    k.wall_factor = float(wall->tgt_inv_rho0 * wm * p->rho0 * p->rho0 / (p->sigma0 * mass[0]));
-    k.wall_Vol = float(wvol.empty() ? 0.0 : wvol[0]);
-    double Z = p->rho0 * p->c0;
-    k.inv_z = float((Z + Z) / (Z * Z + Z * Z));
-    k.zgeo = float(2.0 * Z * Z / (Z + Z));
-    k.inv_c0 = float(0.5 * (p->rho0 + p->rho0) * double(k.inv_z));
-    k.slope = float(p->limiter_slope);
     for (int d = 0; d < 3; ++d)
-    {
         k.gd[d] = d < D ? gravity[d] : 0.0;
-        k.g[d] = float(k.gd[d]);
-    }
-    k.h = p->h;
-    k.c0 = p->c0;
+    k.p = make_params(D, mesh.grid_spacing, p->h, p->rho0, p->c0, vol[0], mass[0], p->sigma0, wall->tgt_inv_rho0 * wm,
+                      wvol.empty() ? 0.0 : wvol[0], p->limiter_slope, k.gd);
     k.acoustic_cfl = p->acoustic_cfl;
     k.advection_cfl = p->advection_cfl;
     k.U_ref = p->U_ref;
@@ -1340,7 +857,7 @@ extern "C" int sphx_mp_upload(sphx_mp mp, sphx_body fb)
 {
     if (!mp || !fb || fb->n != mp->n || fb->dim != mp->dim)
         return fail(SPHX_ERR_INVALID_ARG, "body does not match the mixed-precision solver");
-    double rho0 = double(mp->k.rho0), c0 = mp->k.c0;
+    double rho0 = double(mp->k.p.rho0), c0 = mp->k.p.c0;
     SPHX_TRY(import_fluid(mp, fb, rho0, c0));
     SPHX_CUDA(cudaStreamSynchronize(mp->ctx->stream));
     return SPHX_OK;
@@ -1457,7 +974,7 @@ extern "C" int sphx_mp_autotune(sphx_mp mp, int reps, int *best_block, int *best
         return SPHX_OK;
     double ac;
     SPHX_TRY(read_slot(mp, 0, &ac));
-    double dt = mp->k.acoustic_cfl * mp->k.h / (ac + kTinyReal);
+    double dt = mp->k.acoustic_cfl * mp->k.p.h / (ac + kTinyReal);
     Snapshot snap;
     SPHX_TRY(snap.take(mp, false));
     const int blocks[3] = {64, 128, 256};

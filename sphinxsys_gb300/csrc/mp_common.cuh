@@ -1,7 +1,19 @@
-// Device helpers shared by the mixed-precision solvers (single case and batch).
+// Per-particle physics of the mixed-precision solvers, shared by the single-case solver
+// (mixed.cu) and the batched solver (batch.cu) so both run the same arithmetic.
+//
+// The sweeps follow Integration1stHalfWithWallRiemann / Integration2ndHalfWithWallRiemann
+// (fluid_integration.hpp:49-113,166-231) with the AcousticRiemannSolver and the
+// TruncatedLinear limiter (riemann_solver.h), the wall terms of fluid_integration.hpp
+// (static wall: zero wall velocity and acceleration), and the configuration build with
+// the sums of DensitySummationComplexFreeSurface (density_summation.cpp:74-82,124-144).
+//
+// Precision: FP32 pair arithmetic; neighbour sums are compensated (plain FP32 partials over
+// groups of kGroup neighbours, Kahan-added); positions are FP32 offsets from the lower
+// corner of an integer cell; position half-steps and the time-step maxima are FP64.
 #pragma once
 
 #include "sphx_device.cuh"
+#include "sphx_internal.cuh"
 
 namespace sphx
 {
@@ -10,6 +22,97 @@ namespace mpc
 constexpr float kTinyF = 2.71051e-20f; // TinyReal of the reference, base_data_type.h:207
 constexpr int kGroup = 8;             // neighbours per plain partial sum
 constexpr int kUnroll = 4;            // neighbour records in flight per thread in list sweeps
+constexpr int kCellBias = 4;          // |c_i - c_j| per axis handled by the packed difference
+
+// Cell coordinates packed into 30 bits: 15 per axis in 2D, 10 per axis in 3D.
+template <int D>
+struct CellLanes
+{
+    static constexpr int bits = D == 2 ? 15 : 10;
+    static constexpr uint32_t mask = (1u << bits) - 1u;
+    static constexpr int max_cells = 1 << bits;
+    static constexpr uint32_t bias = D == 2 ? (uint32_t(kCellBias) | (uint32_t(kCellBias) << 15))
+                                            : (uint32_t(kCellBias) | (uint32_t(kCellBias) << 10) |
+                                               (uint32_t(kCellBias) << 20));
+};
+
+template <int D>
+__host__ __device__ __forceinline__ uint32_t pack_cell(const int *c)
+{
+    uint32_t p = 0;
+    for (int d = 0; d < D; ++d)
+        p |= uint32_t(c[d]) << (d * CellLanes<D>::bits);
+    return p;
+}
+template <int D>
+__host__ __device__ __forceinline__ void unpack_cell(uint32_t p, int *c)
+{
+    c[0] = c[1] = c[2] = 0;
+    for (int d = 0; d < D; ++d)
+        c[d] = int((p >> (d * CellLanes<D>::bits)) & CellLanes<D>::mask);
+}
+
+struct MPParams
+{
+    float gs_f, rc_sqr, inv_h, fW;
+    float cW, cWw; // Wendland dW prefactor x 5/8 x particle volume (fluid, wall)
+    float rho0, p0_over_rho0, Vol, mass, inv_mass;
+    float rho0_over_sigma0, wall_factor; // wall_factor = rho0^2 m_w / (sigma0 m rho0_w)
+    float inv_z, zgeo, s_lim;            // acoustic Riemann solver; s_lim = limiter slope / c0
+    float g[3];
+    double sigma0, c0, h;
+};
+
+// Constants of one fluid body against one static wall (same rounding for every solver).
+inline MPParams make_params(int dim, double grid_spacing, double h, double rho0, double c0, double vol, double mass,
+                            double sigma0, double wall_mass_over_rho0, double wall_vol, double limiter_slope,
+                            const double *gravity)
+{
+    WendlandC2 wk = wendland(dim, h);
+    MPParams k{};
+    k.gs_f = float(grid_spacing);
+    k.rc_sqr = float(wk.rc_sqr);
+    k.inv_h = float(wk.inv_h);
+    k.fW = float(wk.factor_W);
+    k.cW = float(wk.factor_dW * 0.625 * vol);
+    k.cWw = float(wk.factor_dW * 0.625 * wall_vol);
+    k.rho0 = float(rho0);
+    k.p0_over_rho0 = float(rho0 * c0 * c0 / rho0);
+    k.Vol = float(vol);
+    k.mass = float(mass);
+    k.inv_mass = float(1.0 / mass);
+    k.sigma0 = sigma0;
+    k.rho0_over_sigma0 = float(rho0 / sigma0);
+    k.wall_factor = float(wall_mass_over_rho0 * rho0 * rho0 / (sigma0 * mass));
+    double Z = rho0 * c0;
+    double inv_z = (Z + Z) / (Z * Z + Z * Z);
+    k.inv_z = float(inv_z);
+    k.zgeo = float(2.0 * Z * Z / (Z + Z));
+    k.s_lim = float(limiter_slope * (0.5 * (rho0 + rho0) * inv_z));
+    for (int d = 0; d < 3; ++d)
+        k.g[d] = d < dim ? float(gravity[d]) : 0.f;
+    k.c0 = c0;
+    k.h = h;
+    return k;
+}
+
+struct MPState
+{
+    float4 *geo0, *dyn; // {offset at the last configuration update, packed cell}; {velocity, pressure}
+    float *off, *force, *drho, *drho_dt, *drho_sum;
+    uint32_t *id;
+};
+
+struct MPWallData
+{
+    float4 *geo, *n;
+};
+
+struct MPNeighbors
+{
+    uint32_t *count, *J; // slot-major: slot s of particle i at J[s * n + i]
+    unsigned cap;
+};
 
 struct Kahan
 {
@@ -52,7 +155,46 @@ __device__ __forceinline__ void warp_max_to(unsigned long long *slot, double v)
         atomicMax(slot, b);
 }
 
-// Wendland C2 in FP32 with t = 1 - q/2: W = fW t^4 (1 + 2q), dW = fdW 0.625 (q - 2)^3 q.
+// x_i - x_j from the packed cells and cell offsets.  pib = packed cell of i plus the lane
+// bias: the 32-bit difference pib - p_j holds c_i - c_j + kCellBias in every lane (no
+// borrow while |c_i - c_j| <= kCellBias), and each lane becomes an exact float through the
+// 2^23 exponent pattern.
+template <int D>
+__device__ __forceinline__ void geo_dx(float gs, uint32_t pib, const float *oi, float4 gj, float *dx)
+{
+    const uint32_t dl = pib - __float_as_uint(gj.w);
+    const float oj[3] = {gj.x, gj.y, gj.z};
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        uint32_t lane = (dl >> (d * CellLanes<D>::bits)) & CellLanes<D>::mask;
+        float dc = __uint_as_float(0x4B000000u | lane) - (8388608.0f + float(kCellBias));
+        dx[d] = fmaf(dc, gs, oi[d] - oj[d]);
+    }
+}
+
+template <int D>
+__device__ __forceinline__ float sq(const float *dx)
+{
+    float s = dx[0] * dx[0] + dx[1] * dx[1];
+    if (D == 3)
+        s += dx[2] * dx[2];
+    return s;
+}
+
+template <int D>
+__device__ __forceinline__ float dot(const float *a, const float *b)
+{
+    float s = a[0] * b[0] + a[1] * b[1];
+    if (D == 3)
+        s += a[2] * b[2];
+    return s;
+}
+
+// 1 / r (0 for coincident particles, whose kernel gradient is zero).
+__device__ __forceinline__ float inv_dist(float r2) { return r2 > 0.f ? rsqrtf(r2) : 0.f; }
+
+// Wendland C2 W(r) = fW t^4 (1 + 2q), t = 1 - q/2.
 __device__ __forceinline__ float wc2_W(float fW, float inv_h, float r)
 {
     float q = r * inv_h;
@@ -60,17 +202,374 @@ __device__ __forceinline__ float wc2_W(float fW, float inv_h, float r)
     float t2 = t * t;
     return fW * (t2 * t2 * (1.0f + 2.0f * q));
 }
-__device__ __forceinline__ float wc2_dW(float fdW, float inv_h, float r)
+// dW(r) V = c (q - 2)^3 q with c = fdW 5/8 V.
+__device__ __forceinline__ float wc2_dWV(float c, float inv_h, float r)
 {
     float q = r * inv_h;
     float t = q - 2.0f;
-    return fdW * (0.625f * (t * t * t) * q);
+    return c * (t * t * t) * q;
 }
 
-// DissipativePJump of AcousticRiemannSolver with the TruncatedLinear limiter.
-__device__ __forceinline__ float p_jump(float zgeo, float inv_c0, float slope, float u)
+// DissipativePJump of the AcousticRiemannSolver with the TruncatedLinear limiter.
+__device__ __forceinline__ float p_jump(const MPParams &k, float u)
 {
-    return zgeo * u * fminf(slope * (inv_c0 * fmaxf(u, 0.0f)), 1.0f);
+    return k.zgeo * u * fminf(k.s_lim * fmaxf(u, 0.0f), 1.0f);
+}
+
+// Candidates of the 3^D cells around cell c; cells of one instance start at cell_base
+// (columns along the last axis are contiguous in the linear cell order).
+template <int D, class F>
+__device__ __forceinline__ void for_each_candidate(const MeshDev &m, uint32_t cell_base, const uint32_t *offset,
+                                                   const int *c, F &&f)
+{
+    int lo0 = max(c[0] - 1, 0), hi0 = min(c[0] + 1, m.all_cells[0] - 1);
+    int lo1 = max(c[1] - 1, 0), hi1 = min(c[1] + 1, m.all_cells[1] - 1);
+    if (D == 2)
+    {
+        for (int x = lo0; x <= hi0; ++x)
+        {
+            uint32_t a = cell_base + uint32_t(x) * uint32_t(m.all_cells[1]);
+            uint32_t b = offset[a + uint32_t(lo1)], e = offset[a + uint32_t(hi1) + 1];
+            for (uint32_t j = b; j < e; ++j)
+                f(j);
+        }
+    }
+    else
+    {
+        int lo2 = max(c[2] - 1, 0), hi2 = min(c[2] + 1, m.all_cells[2] - 1);
+        for (int x = lo0; x <= hi0; ++x)
+            for (int y = lo1; y <= hi1; ++y)
+            {
+                uint32_t a = cell_base +
+                             (uint32_t(x) * uint32_t(m.all_cells[1]) + uint32_t(y)) * uint32_t(m.all_cells[2]);
+                uint32_t b = offset[a + uint32_t(lo2)], e = offset[a + uint32_t(hi2) + 1];
+                for (uint32_t j = b; j < e; ++j)
+                    f(j);
+            }
+    }
+}
+
+// Neighbour visits of one particle: stored lists (LISTS) or a sweep of the 3^D cells with
+// the same membership test as the build, in the same order, so both give the same sums.
+struct Visit
+{
+    MeshDev m;
+    uint32_t cell_base;
+    const uint32_t *f_offset, *w_offset;
+};
+
+// Calls pair(x) for every stored neighbour of i, with kUnroll neighbour records loaded
+// before the arithmetic, and flush() after every kGroup neighbours; load(j) fetches what
+// pair() consumes.
+template <class Load, class Pair, class Flush>
+__device__ __forceinline__ void list_sweep(size_t i, size_t n, const MPNeighbors &l, Load &&load, Pair &&pair,
+                                           Flush &&flush)
+{
+    const unsigned c = min(l.count[i], l.cap);
+    unsigned s = 0;
+    for (; s + kGroup <= c; s += kGroup)
+    {
+#pragma unroll
+        for (int h = 0; h < kGroup; h += kUnroll)
+        {
+            uint32_t jj[kUnroll];
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u)
+                jj[u] = __ldg(&l.J[size_t(s + h + u) * n + i]);
+            decltype(load(0u)) rec[kUnroll];
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u)
+                rec[u] = load(jj[u]);
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u)
+                pair(rec[u]);
+        }
+        flush();
+    }
+    for (; s < c; ++s)
+        pair(load(__ldg(&l.J[size_t(s) * n + i])));
+    flush();
+}
+
+// Same visits by cell sweep: accepts the candidates the build accepted.
+template <int D, class Load, class Pair, class Flush>
+__device__ __forceinline__ void cell_sweep(const Visit &v, const uint32_t *offset, const int *ci, float gs, uint32_t pib,
+                                           const float *oi, float rc_sqr, size_t self, const float4 *geo, Load &&load,
+                                           Pair &&pair, Flush &&flush)
+{
+    int g = 0;
+    for_each_candidate<D>(v.m, v.cell_base, offset, ci, [&](uint32_t j) {
+        if (size_t(j) == self)
+            return;
+        float dx[3];
+        geo_dx<D>(gs, pib, oi, geo[j], dx);
+        if (!(sq<D>(dx) < rc_sqr))
+            return;
+        pair(load(j));
+        if (++g == kGroup)
+        {
+            flush();
+            g = 0;
+        }
+    });
+    flush();
+}
+
+struct FirstRec
+{
+    float4 g;
+    float p;
+};
+struct SecondRec
+{
+    float4 g, v;
+};
+
+// 1st half of one particle: pressure force and density-rate dissipation against fluid and
+// wall neighbours, velocity update and the first position half-step.  Returns the
+// acoustic-time-step candidate c0 + |v|.
+template <int D, bool LISTS>
+__device__ __forceinline__ double first_particle(size_t i, size_t n, const MPParams &k, const Visit &v, double dt,
+                                                 const MPState &f, const MPWallData &w, const MPNeighbors &in,
+                                                 const MPNeighbors &wl)
+{
+    const float4 gi = f.geo0[i];
+    const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
+    int ci[3] = {0, 0, 0};
+    if (!LISTS)
+        unpack_cell<D>(__float_as_uint(gi.w), ci);
+    const float oi[3] = {gi.x, gi.y, gi.z};
+    const float4 di = f.dyn[i];
+    const float p_i = di.w;
+    const float rho_i = k.rho0 + f.drho[i];
+    Acc force[3], rdis;
+    auto pair = [&](const FirstRec &r) {
+        float dx[3];
+        geo_dx<D>(k.gs_f, pib, oi, r.g, dx);
+        float r2 = sq<D>(dx);
+        float inv = inv_dist(r2);
+        float dWV = wc2_dWV(k.cW, k.inv_h, r2 * inv);
+        float sc = (p_i + r.p) * (dWV * inv);
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            force[d].add(-sc * dx[d]);
+        rdis.add((p_i - r.p) * dWV);
+    };
+    auto flush = [&]() {
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            force[d].flush();
+        rdis.flush();
+    };
+    auto load = [&](uint32_t j) { return FirstRec{__ldg(&f.geo0[j]), __ldg(&f.dyn[j].w)}; };
+    if (LISTS)
+        list_sweep(i, n, in, load, pair, flush);
+    else
+        cell_sweep<D>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, i, f.geo0, load, pair, flush);
+
+    Acc wforce[3], wrdis;
+    auto wpair = [&](const float4 &gj) {
+        float dx[3];
+        geo_dx<D>(k.gs_f, pib, oi, gj, dx);
+        float r2 = sq<D>(dx);
+        float inv = inv_dist(r2);
+        float dWV = wc2_dWV(k.cWw, k.inv_h, r2 * inv);
+        // wall pressure p_i + rho_i r max(0, (F_prior / m - a_wall) . (-e)), static wall
+        float p_w = p_i + rho_i * fmaxf(0.0f, -dot<D>(k.g, dx));
+        float sc = (p_i + p_w) * (dWV * inv);
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            wforce[d].add(-sc * dx[d]);
+        wrdis.add((p_i - p_w) * dWV);
+    };
+    auto wflush = [&]() {
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            wforce[d].flush();
+        wrdis.flush();
+    };
+    auto wload = [&](uint32_t j) { return __ldg(&w.geo[j]); };
+    if (LISTS)
+        list_sweep(i, n, wl, wload, wpair, wflush);
+    else
+        cell_sweep<D>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, ~size_t(0), w.geo, wload, wpair, wflush);
+
+    f.drho_dt[i] = (rdis.value() * k.inv_z) * rho_i + (wrdis.value() * k.inv_z) * rho_i;
+    float v2 = 0.f;
+    float vn[3] = {di.x, di.y, di.z};
+    const float dt_f = float(dt);
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        float F = f.force[d * n + i] + force[d].value() * k.Vol + wforce[d].value() * k.Vol;
+        f.force[d * n + i] = F;
+        float vo = vn[d];
+        // position half-step in FP64 (initialisation of the 1st half, old velocity)
+        f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vo));
+        vn[d] = vo + (k.g[d] + F * k.inv_mass) * dt_f;
+        v2 += vn[d] * vn[d];
+    }
+    // the pressure stays the one the neighbours of this sweep read
+    f.dyn[i] = make_float4(vn[0], vn[1], D == 3 ? vn[2] : 0.f, p_i);
+    return k.c0 + double(sqrtf(v2));
+}
+
+// 2nd half of one particle: the second position half-step, density rate and pressure
+// dissipation against fluid and wall neighbours, density update.  Returns the
+// advection-time-step candidate max(|v|^2, 4 h |F + F_prior| / m).
+template <int D, bool LISTS>
+__device__ __forceinline__ double second_particle(size_t i, size_t n, const MPParams &k, const Visit &v, double dt,
+                                                  const MPState &f, const MPWallData &w, const MPNeighbors &in,
+                                                  const MPNeighbors &wl)
+{
+    const float4 gi = f.geo0[i];
+    const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
+    int ci[3] = {0, 0, 0};
+    if (!LISTS)
+        unpack_cell<D>(__float_as_uint(gi.w), ci);
+    const float oi[3] = {gi.x, gi.y, gi.z};
+    const float4 di = f.dyn[i];
+    const float vi[3] = {di.x, di.y, di.z};
+    const float rho_i = k.rho0 + f.drho[i];
+    Acc rate, pdis[3];
+    auto pair = [&](const SecondRec &r) {
+        float dx[3];
+        geo_dx<D>(k.gs_f, pib, oi, r.g, dx);
+        float r2 = sq<D>(dx);
+        float inv = inv_dist(r2);
+        float dWV = wc2_dWV(k.cW, k.inv_h, r2 * inv);
+        const float dv[3] = {vi[0] - r.v.x, vi[1] - r.v.y, vi[2] - r.v.z};
+        float u = dot<D>(dv, dx) * inv;
+        rate.add(u * dWV);
+        float sc = p_jump(k, u) * (dWV * inv);
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            pdis[d].add(sc * dx[d]);
+    };
+    auto flush = [&]() {
+        rate.flush();
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            pdis[d].flush();
+    };
+    auto load = [&](uint32_t j) { return SecondRec{__ldg(&f.geo0[j]), __ldg(&f.dyn[j])}; };
+    if (LISTS)
+        list_sweep(i, n, in, load, pair, flush);
+    else
+        cell_sweep<D>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, i, f.geo0, load, pair, flush);
+
+    Acc wrate, wdis[3];
+    auto wpair = [&](const SecondRec &r) {
+        float dx[3];
+        geo_dx<D>(k.gs_f, pib, oi, r.g, dx);
+        float r2 = sq<D>(dx);
+        float inv = inv_dist(r2);
+        float dWV = wc2_dWV(k.cWw, k.inv_h, r2 * inv);
+        const float nj[3] = {r.v.x, r.v.y, r.v.z};
+        float en = dot<D>(dx, nj);
+        float sgn = en < 0.f ? -1.f : (en > 0.f ? 1.f : 0.f);
+        // (v_i - (2 v_wall - v_i)) . e with a static wall; face velocity jump along n
+        wrate.add(2.0f * (dot<D>(vi, dx) * inv) * dWV);
+        float sc = p_jump(k, 2.0f * sgn * dot<D>(vi, nj)) * dWV * sgn;
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            wdis[d].add(sc * nj[d]);
+    };
+    auto wflush = [&]() {
+        wrate.flush();
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            wdis[d].flush();
+    };
+    auto wload = [&](uint32_t j) { return SecondRec{__ldg(&w.geo[j]), __ldg(&w.n[j])}; };
+    if (LISTS)
+        list_sweep(i, n, wl, wload, wpair, wflush);
+    else
+        cell_sweep<D>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, ~size_t(0), w.geo, wload, wpair, wflush);
+
+    float drho_dt = f.drho_dt[i] + rate.value() * rho_i + wrate.value() * rho_i;
+    f.drho_dt[i] = drho_dt;
+    f.drho[i] = f.drho[i] + drho_dt * float(0.5 * dt);
+    float v2 = 0.f, a2 = 0.f;
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        float F = pdis[d].value() * k.Vol + wdis[d].value() * k.Vol;
+        f.force[d * n + i] = F;
+        f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vi[d]));
+        v2 += vi[d] * vi[d];
+        float ft = F + k.mass * k.g[d];
+        a2 += ft * ft;
+    }
+    return double(fmaxf(v2, 4.0f * float(k.h) * sqrtf(a2) * k.inv_mass));
+}
+
+// Configuration of one particle: fluid and wall neighbour lists (candidate order of the
+// 3^D cells) and the density-summation sum drho_sum = rho_sum - rho0.
+template <int D>
+__device__ __forceinline__ void build_particle(size_t i, size_t n, const MPParams &k, const Visit &v,
+                                               const MPState &f, const MPWallData &w, const MPNeighbors &in,
+                                               const MPNeighbors &wl, unsigned int *max_counts)
+{
+    const float4 gi = f.geo0[i];
+    const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
+    int ci[3] = {0, 0, 0};
+    unpack_cell<D>(__float_as_uint(gi.w), ci);
+    const float oi[3] = {gi.x, gi.y, gi.z};
+    Kahan sigma;
+    unsigned cnt = 0;
+    for_each_candidate<D>(v.m, v.cell_base, v.f_offset, ci, [&](uint32_t j) {
+        if (j == uint32_t(i))
+            return;
+        float dx[3];
+        geo_dx<D>(k.gs_f, pib, oi, f.geo0[j], dx);
+        float r2 = sq<D>(dx);
+        if (!(r2 < k.rc_sqr))
+            return;
+        if (cnt < in.cap)
+            in.J[size_t(cnt) * n + i] = j;
+        ++cnt;
+        sigma.add(wc2_W(k.fW, k.inv_h, sqrtf(r2)));
+    });
+    Kahan wsig;
+    unsigned wc = 0;
+    for_each_candidate<D>(v.m, v.cell_base, v.w_offset, ci, [&](uint32_t j) {
+        float dx[3];
+        geo_dx<D>(k.gs_f, pib, oi, w.geo[j], dx);
+        float r2 = sq<D>(dx);
+        if (!(r2 < k.rc_sqr))
+            return;
+        if (wc < wl.cap)
+            wl.J[size_t(wc) * n + i] = j;
+        ++wc;
+        wsig.add(wc2_W(k.fW, k.inv_h, sqrtf(r2)));
+    });
+    in.count[i] = cnt;
+    wl.count[i] = wc;
+    atomicMax(&max_counts[0], cnt);
+    atomicMax(&max_counts[1], wc);
+    // rho_sum - rho0 = rho0 (W0 + sum W - sigma0) / sigma0 + wall term
+    double dsig = (double(sigma.s) - k.sigma0) - double(sigma.c) + double(k.fW);
+    f.drho_sum[i] = float(dsig) * k.rho0_over_sigma0 + wsig.value() * k.wall_factor;
+}
+
+// Acoustic and advection maxima of the initial state (FP64).
+template <int D>
+__device__ __forceinline__ void initial_max(size_t i, size_t n, const MPParams &k, const double *gd, const MPState &f,
+                                            double *vm, double *am)
+{
+    float4 di = f.dyn[i];
+    const float vv[3] = {di.x, di.y, di.z};
+    double v2 = 0, a2 = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        v2 += double(vv[d]) * double(vv[d]);
+        double ft = double(f.force[d * n + i]) + double(k.mass) * gd[d];
+        a2 += ft * ft;
+    }
+    *vm = k.c0 + sqrt(v2);
+    *am = fmax(v2, 4.0 * k.h * sqrt(a2) * double(k.inv_mass));
 }
 } // namespace mpc
 } // namespace sphx
