@@ -207,7 +207,8 @@ int sphx_upper_front_in_axis_direction(sphx_body fluid, int axis, const double *
  *
  * Requirements checked at creation: uniform particle mass and volume in each body, a
  * static wall (zero wall velocity and acceleration), gravity as the only prior force,
- * at most 32768 cells per mesh axis in 2D and 1024 in 3D. */
+ * at most 16384 cells per mesh axis in 2D and 512 in 3D (the solver searches sub-cells of
+ * half the spacing, packed 15 / 10 bits per axis). */
 typedef struct sphx_mp_s *sphx_mp;
 
 /* Builds the solver from the current FP64 state of the relations' bodies. */
@@ -262,7 +263,7 @@ int sphx_mp_list_sizes(sphx_mp mp, uint64_t *out);
  *
  * Each instance: fluid at rest (rho = rho0) on the given positions, one static wall body
  * with its normals, uniform masses and volumes, gravity as the only prior force, and a
- * cell mesh with grid spacing 2h (at most 32768 cells per axis in 2D, 1024 in 3D). */
+ * cell mesh with grid spacing 2h (at most 16384 cells per axis in 2D, 512 in 3D). */
 typedef struct sphx_batch_s *sphx_batch;
 
 typedef struct

@@ -782,18 +782,19 @@ extern "C" int sphx_batch_create(sphx_ctx ctx, int dim, int count, const sphx_ba
             return bail(fail(SPHX_ERR_INVALID_ARG, "instance %d: invalid description", q));
         if (std::abs(d.mesh.grid_spacing - 2.0 * d.h) > 1e-12 * d.mesh.grid_spacing)
             return bail(fail(SPHX_ERR_INVALID_ARG, "instance %d: grid spacing must equal the cut-off radius 2h", q));
+        const sphx_mesh_desc mesh = sub_mesh(d.mesh);
         size_t cells = 1;
         for (int a = 0; a < D; ++a)
         {
             int lim = D == 2 ? CellLanes<2>::max_cells : CellLanes<3>::max_cells;
-            if (d.mesh.all_cells[a] < 1 || d.mesh.all_cells[a] > lim)
+            if (mesh.all_cells[a] < 1 || mesh.all_cells[a] > lim)
                 return bail(fail(SPHX_ERR_INVALID_ARG, "instance %d: %d cells on axis %d (at most %d)", q,
-                                 d.mesh.all_cells[a], a, lim));
-            cells *= size_t(d.mesh.all_cells[a]);
+                                 mesh.all_cells[a], a, lim));
+            cells *= size_t(mesh.all_cells[a]);
         }
         BInst &k = bt->h_inst[q];
         k = BInst{};
-        k.m = mesh_dev(d.mesh);
+        k.m = mesh_dev(mesh);
         k.cell_base = uint32_t(nc);
         k.ncells = uint32_t(cells);
         k.p_start = uint32_t(n);
@@ -802,7 +803,7 @@ extern "C" int sphx_batch_create(sphx_ctx ctx, int dim, int count, const sphx_ba
         k.w_count = uint32_t(d.n_wall);
         for (int a = 0; a < 3; ++a)
             k.gd[a] = a < D ? d.gravity[a] : 0.0;
-        k.p = make_params(D, d.mesh.grid_spacing, d.h, d.rho0, d.c0, d.fluid_vol, d.fluid_mass, d.sigma0,
+        k.p = make_params(D, mesh.grid_spacing, d.h, d.rho0, d.c0, d.fluid_vol, d.fluid_mass, d.sigma0,
                           1.0 / d.wall_rho0 * d.wall_mass, d.wall_vol, 3.0, k.gd);
         k.acoustic_cfl = 0.6;
         k.advection_cfl = 0.25;

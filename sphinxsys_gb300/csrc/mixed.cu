@@ -716,14 +716,15 @@ extern "C" int sphx_mp_create(sphx_relation inner, sphx_relation wall, const sph
     sphx_body fb = inner->src, wb = wall->tgt;
     const int D = fb->dim;
     sphx_ctx ctx = fb->ctx;
-    const sphx_mesh_desc &mesh = inner->cl->mesh;
+    const sphx_mesh_desc &body_mesh = inner->cl->mesh;
+    const sphx_mesh_desc mesh = sub_mesh(body_mesh);
     const int max_cells = D == 2 ? CellLanes<2>::max_cells : CellLanes<3>::max_cells;
     for (int a = 0; a < D; ++a)
         if (mesh.all_cells[a] > max_cells)
             return fail(SPHX_ERR_INVALID_ARG, "mixed precision packs %d bits per cell axis; axis %d has %d cells",
                         D == 2 ? CellLanes<2>::bits : CellLanes<3>::bits, a, mesh.all_cells[a]);
-    if (std::abs(wall->cl->mesh.grid_spacing - mesh.grid_spacing) > 0 ||
-        std::abs(2.0 * p->h - mesh.grid_spacing) > 1e-12 * mesh.grid_spacing)
+    if (std::abs(wall->cl->mesh.grid_spacing - body_mesh.grid_spacing) > 0 ||
+        std::abs(2.0 * p->h - body_mesh.grid_spacing) > 1e-12 * body_mesh.grid_spacing)
         return fail(SPHX_ERR_INVALID_ARG, "mixed precision needs one mesh with grid spacing equal to the cut-off");
     // host checks of uniform mass / volume and a static wall (after the queued work)
     SPHX_CUDA(cudaStreamSynchronize(ctx->stream));

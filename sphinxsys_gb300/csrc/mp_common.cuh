@@ -9,7 +9,7 @@
 //
 // Precision: FP32 pair arithmetic; neighbour sums are compensated (plain FP32 partials over
 // groups of kGroup neighbours, Kahan-added); positions are FP32 offsets from the lower
-// corner of an integer cell; position half-steps and the time-step maxima are FP64.
+// corner of an integer sub-cell; position half-steps and the time-step maxima are FP64.
 #pragma once
 
 #include "sphx_device.cuh"
@@ -23,6 +23,19 @@ constexpr float kTinyF = 2.71051e-20f; // TinyReal of the reference, base_data_t
 constexpr int kGroup = 8;             // neighbours per plain partial sum
 constexpr int kUnroll = 4;            // neighbour records in flight per thread in list sweeps
 constexpr int kCellBias = 4;          // |c_i - c_j| per axis handled by the packed difference
+constexpr int kReach = 2;             // neighbour search reach in sub-cells (cut-off = 2 sub-cells)
+
+// The solvers order and search particles on sub-cells of half the cell-linked-list spacing
+// (spacing h for the cut-off 2h): the 5^D sub-cells around a particle hold about 42%
+// fewer candidates than the 3^D cells of spacing 2h in 3D (31% in 2D).
+inline sphx_mesh_desc sub_mesh(const sphx_mesh_desc &m)
+{
+    sphx_mesh_desc s = m;
+    s.grid_spacing = 0.5 * m.grid_spacing;
+    for (int a = 0; a < m.dim; ++a)
+        s.all_cells[a] = 2 * m.all_cells[a];
+    return s;
+}
 
 // Cell coordinates packed into 30 bits: 15 per axis in 2D, 10 per axis in 3D.
 template <int D>
@@ -216,14 +229,15 @@ __device__ __forceinline__ float p_jump(const MPParams &k, float u)
     return k.zgeo * u * fminf(k.s_lim * fmaxf(u, 0.0f), 1.0f);
 }
 
-// Candidates of the 3^D cells around cell c; cells of one instance start at cell_base
-// (columns along the last axis are contiguous in the linear cell order).
+// Candidates of the (2 kReach + 1)^D sub-cells around sub-cell c; the cells of one
+// instance start at cell_base (columns along the last axis are contiguous in the linear
+// cell order).
 template <int D, class F>
 __device__ __forceinline__ void for_each_candidate(const MeshDev &m, uint32_t cell_base, const uint32_t *offset,
                                                    const int *c, F &&f)
 {
-    int lo0 = max(c[0] - 1, 0), hi0 = min(c[0] + 1, m.all_cells[0] - 1);
-    int lo1 = max(c[1] - 1, 0), hi1 = min(c[1] + 1, m.all_cells[1] - 1);
+    int lo0 = max(c[0] - kReach, 0), hi0 = min(c[0] + kReach, m.all_cells[0] - 1);
+    int lo1 = max(c[1] - kReach, 0), hi1 = min(c[1] + kReach, m.all_cells[1] - 1);
     if (D == 2)
     {
         for (int x = lo0; x <= hi0; ++x)
@@ -236,7 +250,7 @@ __device__ __forceinline__ void for_each_candidate(const MeshDev &m, uint32_t ce
     }
     else
     {
-        int lo2 = max(c[2] - 1, 0), hi2 = min(c[2] + 1, m.all_cells[2] - 1);
+        int lo2 = max(c[2] - kReach, 0), hi2 = min(c[2] + kReach, m.all_cells[2] - 1);
         for (int x = lo0; x <= hi0; ++x)
             for (int y = lo1; y <= hi1; ++y)
             {
@@ -249,7 +263,7 @@ __device__ __forceinline__ void for_each_candidate(const MeshDev &m, uint32_t ce
     }
 }
 
-// Neighbour visits of one particle: stored lists (LISTS) or a sweep of the 3^D cells with
+// Neighbour visits of one particle: stored lists (LISTS) or a sweep of the sub-cells with
 // the same membership test as the build, in the same order, so both give the same sums.
 struct Visit
 {
@@ -505,7 +519,7 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
 }
 
 // Configuration of one particle: fluid and wall neighbour lists (candidate order of the
-// 3^D cells) and the density-summation sum drho_sum = rho_sum - rho0.
+// surrounding sub-cells) and the density-summation sum drho_sum = rho_sum - rho0.
 template <int D>
 __device__ __forceinline__ void build_particle(size_t i, size_t n, const MPParams &k, const Visit &v,
                                                const MPState &f, const MPWallData &w, const MPNeighbors &in,
