@@ -283,8 +283,9 @@ __global__ void k_b_init1(size_t n, const uint32_t *__restrict__ starts, int cou
     reinterpret_cast<float *>(dyn)[4 * i + 3] = inst[b].p.p0_over_rho0 * r;
 }
 
+// at most 64 registers: 4 blocks of 256 threads per SM
 template <int D>
-__global__ void k_b_first(size_t n, const uint32_t *__restrict__ starts, int count, const BInst *__restrict__ inst, BRun *run,
+__global__ void __launch_bounds__(256, 4) k_b_first(size_t n, const uint32_t *__restrict__ starts, int count, const BInst *__restrict__ inst, BRun *run,
               MPState f, MPWallData w, MPNeighbors in, MPNeighbors wl)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;

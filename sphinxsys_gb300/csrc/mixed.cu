@@ -184,8 +184,9 @@ __global__ void k_mp_init1(size_t n, float *__restrict__ drho, const float *__re
     reinterpret_cast<float *>(dyn)[4 * i + 3] = p0_over_rho0 * r;
 }
 
+// at most 64 registers: 4 blocks of 256 threads per SM
 template <int D, bool LISTS>
-__global__ void k_mp_first(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
+__global__ void __launch_bounds__(256, 4) k_mp_first(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
                const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, double dt,
                unsigned long long *ac_slot)
 {

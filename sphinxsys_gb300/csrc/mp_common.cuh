@@ -274,22 +274,48 @@ struct Visit
 
 // Calls pair(x) for every stored neighbour of i, with kUnroll neighbour records loaded
 // before the arithmetic, and flush() after every kGroup neighbours; load(j) fetches what
-// pair() consumes.
-template <class Load, class Pair, class Flush>
+// pair() consumes.  PREFETCH also loads the next kUnroll list entries before the current
+// records are used (one list read in flight behind the record gathers); it pays where the
+// records are small (1st half), not where the extra registers cost occupancy (2nd half).
+template <bool PREFETCH, class Load, class Pair, class Flush>
 __device__ __forceinline__ void list_sweep(size_t i, size_t n, const MPNeighbors &l, Load &&load, Pair &&pair,
                                            Flush &&flush)
 {
     const unsigned c = min(l.count[i], l.cap);
+    const uint32_t *J = l.J + i;
     unsigned s = 0;
+    uint32_t jn[kUnroll];
+    if (PREFETCH && c >= kUnroll)
+    {
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u)
+            jn[u] = __ldg(&J[size_t(u) * n]);
+    }
     for (; s + kGroup <= c; s += kGroup)
     {
 #pragma unroll
         for (int h = 0; h < kGroup; h += kUnroll)
         {
             uint32_t jj[kUnroll];
+            if (PREFETCH)
+            {
 #pragma unroll
-            for (int u = 0; u < kUnroll; ++u)
-                jj[u] = __ldg(&l.J[size_t(s + h + u) * n + i]);
+                for (int u = 0; u < kUnroll; ++u)
+                    jj[u] = jn[u];
+                const unsigned nx = s + h + kUnroll;
+                if (nx + kUnroll <= c)
+                {
+#pragma unroll
+                    for (int u = 0; u < kUnroll; ++u)
+                        jn[u] = __ldg(&J[size_t(nx + u) * n]);
+                }
+            }
+            else
+            {
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u)
+                    jj[u] = __ldg(&J[size_t(s + h + u) * n]);
+            }
             decltype(load(0u)) rec[kUnroll];
 #pragma unroll
             for (int u = 0; u < kUnroll; ++u)
@@ -301,7 +327,7 @@ __device__ __forceinline__ void list_sweep(size_t i, size_t n, const MPNeighbors
         flush();
     }
     for (; s < c; ++s)
-        pair(load(__ldg(&l.J[size_t(s) * n + i])));
+        pair(load(__ldg(&J[size_t(s) * n])));
     flush();
 }
 
@@ -377,7 +403,7 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
     };
     auto load = [&](uint32_t j) { return FirstRec{__ldg(&f.geo0[j]), __ldg(&f.dyn[j].w)}; };
     if (LISTS)
-        list_sweep(i, n, in, load, pair, flush);
+        list_sweep<true>(i, n, in, load, pair, flush);
     else
         cell_sweep<D>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, i, f.geo0, load, pair, flush);
 
@@ -404,7 +430,7 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
     };
     auto wload = [&](uint32_t j) { return __ldg(&w.geo[j]); };
     if (LISTS)
-        list_sweep(i, n, wl, wload, wpair, wflush);
+        list_sweep<true>(i, n, wl, wload, wpair, wflush);
     else
         cell_sweep<D>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, ~size_t(0), w.geo, wload, wpair, wflush);
 
@@ -468,7 +494,7 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
     };
     auto load = [&](uint32_t j) { return SecondRec{__ldg(&f.geo0[j]), __ldg(&f.dyn[j])}; };
     if (LISTS)
-        list_sweep(i, n, in, load, pair, flush);
+        list_sweep<false>(i, n, in, load, pair, flush);
     else
         cell_sweep<D>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, i, f.geo0, load, pair, flush);
 
@@ -497,7 +523,7 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
     };
     auto wload = [&](uint32_t j) { return SecondRec{__ldg(&w.geo[j]), __ldg(&w.n[j])}; };
     if (LISTS)
-        list_sweep(i, n, wl, wload, wpair, wflush);
+        list_sweep<false>(i, n, wl, wload, wpair, wflush);
     else
         cell_sweep<D>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, ~size_t(0), w.geo, wload, wpair, wflush);
 
