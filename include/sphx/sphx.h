@@ -78,6 +78,12 @@ int sphx_body_register(sphx_body body, const char *name, sphx_dtype dtype, int n
 int sphx_body_upload(sphx_body body, const char *name, sphx_dtype dtype, int ncomp, const void *host, size_t n);
 /* Device SoA -> host AoS (n x ncomp); synchronises the stream. */
 int sphx_body_download(sphx_body body, const char *name, void *host, size_t n);
+/* Rows [first, first + count) of a registered variable from / to a host AoS buffer of
+ * count x ncomp values (the ghost-layer exchange of a slab decomposition refreshes a block
+ * of rows; the reference's host-side counterpart is a loop over the variable's data).
+ * Synchronous; a pinned host buffer is copied at full link speed. */
+int sphx_body_upload_rows(sphx_body body, const char *name, const void *host, size_t first, size_t count);
+int sphx_body_download_rows(sphx_body body, const char *name, void *host, size_t first, size_t count);
 /* DelegatedData(CudaDevicePolicy): device base pointer of a variable (SoA). */
 int sphx_body_device_ptr(sphx_body body, const char *name, void **dev, sphx_dtype *dtype, int *ncomp);
 

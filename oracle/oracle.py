@@ -56,6 +56,7 @@ def lib() -> C.CDLL:
         L.orc_case_destroy.argtypes = [vp]
         L.orc_num_particles.restype = sz
         L.orc_num_particles.argtypes = [vp, i]
+        L.orc_body_resize.argtypes = [vp, i, sz]
         L.orc_constant.restype = d
         L.orc_constant.argtypes = [vp, i]
         L.orc_get.restype = i
@@ -144,6 +145,10 @@ class OracleCase:
         if getattr(self, "h", None):
             lib().orc_case_destroy(self.h)
             self.h = None
+
+    def resize(self, body: int, n: int) -> None:
+        """Zeroed body of n particles (set its variables, then rebuild lists and relations)."""
+        lib().orc_body_resize(self.h, body, int(n))
 
     def n(self, body: int = FLUID) -> int:
         return int(lib().orc_num_particles(self.h, body))

@@ -361,6 +361,123 @@ struct CellList
     }
 };
 
+//------------------------------------------------------------------------------
+// CK numerics: KernelTabulatedCK (kernel_tabulated_ck.h:37-62, .cpp:5-25) evaluated as
+// Neighbor<SPHAdaptation, SPHAdaptation>::SmoothingKernel does (neighbor_method.hpp:66-142)
+//------------------------------------------------------------------------------
+struct TabKernel
+{
+    static constexpr int resolution = 20, size = resolution + 4;
+    int D = 2;
+    Real inv_h = 1, inv_h2 = 1, inv_h3 = 1, inv_h4 = 1, dim_factor = 1;
+    Real dq = 0.1, d0 = 1, d1 = 1, d2 = 1, d3 = 1;
+    Real w[size], dw[size];
+    TabKernel() = default;
+    TabKernel(int D_, Real h) : D(D_)
+    {
+        // KernelWendlandC2 (kernel_wendland_c2.cpp): W_1D, dW_1D; kernel size 2
+        Real kinv_h = 1.0 / h;
+        Real fW2 = kinv_h * kinv_h * 7.0 / (4.0 * Pi), fW3 = kinv_h * kinv_h * kinv_h * 21.0 / (16.0 * Pi);
+        dim_factor = D == 2 ? fW2 * h * h : fW3 * h * h * h; // Kernel::DimensionFactor2D/3D
+        dq = 2.0 / Real(resolution);
+        for (int i = 0; i < size; ++i)
+        {
+            Real q = Real(i - 1) * dq;
+            w[i] = std::pow(1.0 - 0.5 * q, 4) * (1.0 + 2.0 * q);
+            dw[i] = 0.625 * std::pow(q - 2.0, 3) * q;
+        }
+        d0 = (-1.0 * dq) * (-2.0 * dq) * (-3.0 * dq);
+        d1 = dq * (-1.0 * dq) * (-2.0 * dq);
+        d2 = (2.0 * dq) * dq * (-1.0 * dq);
+        d3 = (3.0 * dq) * (2.0 * dq) * dq;
+        inv_h = 1.0 / h;
+        inv_h2 = inv_h * inv_h;
+        inv_h3 = inv_h2 * inv_h;
+        inv_h4 = inv_h3 * inv_h;
+    }
+    Real cubic(const Real *data, Real q) const
+    {
+        int location = (int)std::floor(q / dq);
+        int i = location + 1;
+        Real f1 = q - Real(location) * dq, f0 = f1 + dq, f2 = f1 - dq, f3 = f1 - 2 * dq;
+        return (f1 * f2 * f3) / d0 * data[i - 1] + (f0 * f2 * f3) / d1 * data[i] + (f0 * f1 * f3) / d2 * data[i + 1] +
+               (f0 * f1 * f2) / d3 * data[i + 2];
+    }
+    Real W(Real r) const { return (D == 2 ? inv_h2 : inv_h3) * dim_factor * cubic(w, r * inv_h); }
+    Real dW(Real r) const { return (D == 2 ? inv_h3 : inv_h4) * dim_factor * cubic(dw, r * inv_h); }
+    Real W0() const { return (D == 2 ? inv_h2 : inv_h3) * dim_factor * cubic(w, 0.0); }
+};
+
+// Row-major D x D matrix in a 3 x 3 array.
+struct M3
+{
+    Real m[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    Real &operator()(int r, int c) { return m[r * 3 + c]; }
+    Real operator()(int r, int c) const { return m[r * 3 + c]; }
+    static M3 identity(int D)
+    {
+        M3 I;
+        for (int a = 0; a < D; ++a)
+            I(a, a) = 1.0;
+        return I;
+    }
+};
+inline V3 mul(const M3 &A, const V3 &x, int D)
+{
+    V3 y;
+    for (int r = 0; r < D; ++r)
+    {
+        Real s = 0;
+        for (int c = 0; c < D; ++c)
+            s += A(r, c) * x[c];
+        y[r] = s;
+    }
+    return y;
+}
+inline Real det(const M3 &A, int D)
+{
+    if (D == 2)
+        return A(0, 0) * A(1, 1) - A(0, 1) * A(1, 0);
+    return A(0, 0) * (A(1, 1) * A(2, 2) - A(1, 2) * A(2, 1)) - A(0, 1) * (A(1, 0) * A(2, 2) - A(1, 2) * A(2, 0)) +
+           A(0, 2) * (A(1, 0) * A(2, 1) - A(1, 1) * A(2, 0));
+}
+// Inverse by the adjugate (small fixed-size matrices).
+inline M3 inverse(const M3 &A, int D)
+{
+    M3 R;
+    Real d = det(A, D);
+    if (D == 2)
+    {
+        R(0, 0) = A(1, 1) / d;
+        R(0, 1) = -A(0, 1) / d;
+        R(1, 0) = -A(1, 0) / d;
+        R(1, 1) = A(0, 0) / d;
+        return R;
+    }
+    R(0, 0) = (A(1, 1) * A(2, 2) - A(1, 2) * A(2, 1)) / d;
+    R(0, 1) = (A(0, 2) * A(2, 1) - A(0, 1) * A(2, 2)) / d;
+    R(0, 2) = (A(0, 1) * A(1, 2) - A(0, 2) * A(1, 1)) / d;
+    R(1, 0) = (A(1, 2) * A(2, 0) - A(1, 0) * A(2, 2)) / d;
+    R(1, 1) = (A(0, 0) * A(2, 2) - A(0, 2) * A(2, 0)) / d;
+    R(1, 2) = (A(0, 2) * A(1, 0) - A(0, 0) * A(1, 2)) / d;
+    R(2, 0) = (A(1, 0) * A(2, 1) - A(1, 1) * A(2, 0)) / d;
+    R(2, 1) = (A(0, 1) * A(2, 0) - A(0, 0) * A(2, 1)) / d;
+    R(2, 2) = (A(0, 0) * A(1, 1) - A(0, 1) * A(1, 0)) / d;
+    return R;
+}
+
+// CK fluid state beside the classic Body: Compression, CompressionRate, Displacement,
+// LinearCorrectionMatrix, VolumetricMeasureRef, CompressionSummation.
+struct CKState
+{
+    std::vector<Real> compression, compression_rate, Vol_ref, compression_sum, wall_Vol_ref;
+    std::vector<V3> dpos;
+    std::vector<M3> B;
+    Real present_time = 0, interval = 0; // TimeStepper::TriggerByInterval of the advection step
+    long advection_steps = 0;
+    bool ready = false;
+};
+
 struct Case
 {
     int D = 2;
@@ -379,6 +496,8 @@ struct Case
     std::vector<Neighborhood> inner, contact, obs;
     Box water_box;
     WallShape wall_shape;
+    TabKernel tk;
+    CKState ck;
     V3 sys_lo, sys_up;
     Mesh sort_mesh;
 
@@ -736,6 +855,394 @@ Real upperFront(const Case &cs, int axis, const V3 &lo, const V3 &up)
     return m;
 }
 
+//------------------------------------------------------------------------------
+// CK dam-break numerics (tests/tests_sycl/2d_examples/test_2d_dambreak_sycl/dambreak_sycl.cpp):
+// pair geometry from the current Position (moved once per advection step by
+// UpdateParticlePosition), the tabulated kernel, the neighbour lists of the configuration.
+//------------------------------------------------------------------------------
+inline V3 sub3(const V3 &a, const V3 &b, int D)
+{
+    V3 r;
+    for (int k = 0; k < D; ++k)
+        r[k] = a[k] - b[k];
+    return r;
+}
+// Eigen normalized(): x / |x| for a non-zero x, x itself otherwise
+inline V3 normalized(const V3 &x, int D)
+{
+    Real n2 = sqnorm(x, D);
+    V3 e = x;
+    if (n2 > 0)
+    {
+        Real n = std::sqrt(n2);
+        for (int k = 0; k < D; ++k)
+            e[k] = x[k] / n;
+    }
+    return e;
+}
+
+void ckEnsureState(Case &cs)
+{
+    CKState &ck = cs.ck;
+    size_t n = cs.fluid.n;
+    if (ck.ready && ck.compression.size() == n && ck.wall_Vol_ref.size() == cs.wall.n)
+        return;
+    ck.compression.assign(n, 1.0);   // registerStateVariable("Compression", 1)
+    ck.compression_rate.assign(n, 0.0);
+    ck.compression_sum.assign(n, 1.0);
+    ck.dpos.assign(n, V3());
+    ck.B.assign(n, M3::identity(cs.D)); // "LinearCorrectionMatrix", identity
+    ck.Vol_ref = cs.fluid.Vol;           // registerStateVariableFrom("VolumetricMeasureRef", ...)
+    ck.wall_Vol_ref = cs.wall.Vol;
+    ck.ready = true;
+}
+
+// CompressionSummation<Inner, Contact> + DensityRegularization<FreeSurface>:
+// density_regularization.hpp:40-118, density_regularization.h:164-180
+void ckDensityRegularization(Case &cs)
+{
+    ckEnsureState(cs);
+    const int D = cs.D;
+    Body &f = cs.fluid;
+    CKState &ck = cs.ck;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)f.n; ++i)
+    {
+        Real sum = cs.tk.W0() * ck.Vol_ref[i];
+        const Neighborhood &nb = cs.inner[i];
+        for (size_t k = 0; k < nb.size(); ++k)
+        {
+            UInt j = nb.j[k];
+            Real r = std::sqrt(sqnorm(sub3(f.pos[i], f.pos[j], D), D));
+            sum += cs.tk.W(r) * ck.Vol_ref[j];
+        }
+        const Neighborhood &nw = cs.contact[i];
+        for (size_t k = 0; k < nw.size(); ++k)
+        {
+            UInt j = nw.j[k];
+            Real r = std::sqrt(sqnorm(sub3(f.pos[i], cs.wall.pos[j], D), D));
+            sum += cs.tk.W(r) * ck.wall_Vol_ref[j];
+        }
+        ck.compression_sum[i] = sum;
+        ck.compression[i] = std::max(sum, Real(1));
+        f.rho[i] = ck.compression[i] * cs.rho0;
+    }
+}
+
+// AdvectionStepSetup: fluid_time_step_ck.h:145-149
+void ckAdvectionStepSetup(Case &cs)
+{
+    ckEnsureState(cs);
+    Body &f = cs.fluid;
+    for (size_t i = 0; i < f.n; ++i)
+    {
+        f.Vol[i] = f.mass[i] / f.rho[i];
+        cs.ck.dpos[i] = V3();
+    }
+}
+
+// UpdateParticlePosition: fluid_time_step_ck.h:173-176
+void ckUpdateParticlePosition(Case &cs)
+{
+    Body &f = cs.fluid;
+    for (size_t i = 0; i < f.n; ++i)
+        for (int a = 0; a < cs.D; ++a)
+            f.pos[i][a] += cs.ck.dpos[i][a];
+}
+
+// LinearCorrectionMatrix<Inner<WithUpdate>> + <Contact>: kernel_correction_ck.hpp:25-80,
+// inverseTikhonov (vector_functions.h:199-203) with SqrtEps = 1e-8
+void ckLinearCorrectionMatrix(Case &cs, Real alpha)
+{
+    ckEnsureState(cs);
+    const int D = cs.D;
+    Body &f = cs.fluid;
+    CKState &ck = cs.ck;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)f.n; ++i)
+    {
+        M3 B;
+        auto add = [&](const V3 &xj, Real Vj) {
+            V3 r = sub3(f.pos[i], xj, D);
+            Real dW = cs.tk.dW(std::sqrt(sqnorm(r, D)));
+            V3 e = normalized(r, D);
+            for (int a = 0; a < D; ++a)
+                for (int b = 0; b < D; ++b)
+                    B(a, b) -= r[a] * (dW * e[b] * Vj);
+        };
+        const Neighborhood &nb = cs.inner[i];
+        for (size_t k = 0; k < nb.size(); ++k)
+            add(f.pos[nb.j[k]], f.Vol[nb.j[k]]);
+        const Neighborhood &nw = cs.contact[i];
+        for (size_t k = 0; k < nw.size(); ++k)
+            add(cs.wall.pos[nw.j[k]], cs.wall.Vol[nw.j[k]]);
+        Real determinant = det(B, D);
+        Real det_sqr = std::max(alpha - determinant, Real(0));
+        // inverseTikhonov: (B^T B + eps I)^-1 B^T
+        M3 BtB;
+        for (int a = 0; a < D; ++a)
+            for (int b = 0; b < D; ++b)
+            {
+                Real sum = 0;
+                for (int c = 0; c < D; ++c)
+                    sum += B(c, a) * B(c, b);
+                BtB(a, b) = sum + (a == b ? 1.0e-8 : 0.0);
+            }
+        M3 Inv = inverse(BtB, D), T;
+        for (int a = 0; a < D; ++a)
+            for (int b = 0; b < D; ++b)
+            {
+                Real sum = 0;
+                for (int c = 0; c < D; ++c)
+                    sum += Inv(a, c) * B(b, c);
+                T(a, b) = sum;
+            }
+        Real weight = determinant / (determinant + det_sqr);
+        M3 R;
+        for (int a = 0; a < D; ++a)
+            for (int b = 0; b < D; ++b)
+                R(a, b) = weight * T(a, b) + (1.0 - weight) * (a == b ? 1.0 : 0.0);
+        ck.B[i] = R;
+    }
+}
+
+// AcousticStep1stHalf<Inner<OneLevel, AcousticRiemannSolverCK, LinearCorrectionCK>> +
+// <Contact<Wall, ...>>: acoustic_step_1st_half.hpp:40-190; RiemannSolver AverageP /
+// DissipativeUJump: riemann_solver_ck.hpp:14-50
+void ckAcousticStep1stHalf(Case &cs, Real dt)
+{
+    const int D = cs.D;
+    Body &f = cs.fluid;
+    CKState &ck = cs.ck;
+    const Real Z = cs.rho0c0, inv_Zsum = 1.0 / (Z + Z);
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)f.n; ++i)
+    {
+        ck.compression[i] += 0.5 * dt * ck.compression_rate[i];
+        f.rho[i] = ck.compression[i] * cs.rho0;
+        f.p[i] = cs.getPressure(f.rho[i]);
+        for (int a = 0; a < D; ++a)
+            ck.dpos[i][a] += f.vel[i][a] * dt * 0.5;
+    }
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)f.n; ++i)
+    {
+        V3 force_sum;
+        Real dissipation = 0;
+        const Neighborhood &nb = cs.inner[i];
+        for (size_t k = 0; k < nb.size(); ++k)
+        {
+            UInt j = nb.j[k];
+            V3 r = sub3(f.pos[i], f.pos[j], D);
+            Real dWV = cs.tk.dW(std::sqrt(sqnorm(r, D))) * f.Vol[j];
+            V3 e = normalized(r, D);
+            // AverageP(B_j p_i, B_i p_j) = (Z_j B_j p_i + Z_i B_i p_j) / (Z_i + Z_j)
+            V3 bj = mul(ck.B[j], e, D), bi = mul(ck.B[i], e, D);
+            for (int a = 0; a < D; ++a)
+                force_sum[a] -= inv_Zsum * (f.p[i] * Z * bj[a] + f.p[j] * Z * bi[a]) * 2.0 * dWV;
+            dissipation += (f.p[i] - f.p[j]) * cs.inv_rho0c0_ave * dWV;
+        }
+        for (int a = 0; a < D; ++a)
+            f.force[i][a] += force_sum[a] * f.Vol[i];
+        ck.compression_rate[i] = dissipation * ck.compression[i];
+        // wall contact
+        V3 wforce;
+        Real wdis = 0;
+        const Neighborhood &nw = cs.contact[i];
+        for (size_t k = 0; k < nw.size(); ++k)
+        {
+            UInt j = nw.j[k];
+            V3 r = sub3(f.pos[i], cs.wall.pos[j], D);
+            Real rij = std::sqrt(sqnorm(r, D));
+            Real dWV = cs.tk.dW(rij) * cs.wall.Vol[j];
+            V3 e = normalized(r, D);
+            V3 acc;
+            for (int a = 0; a < D; ++a)
+                acc[a] = -(f.force_prior[i][a] / f.mass[i] - cs.wall.acc_ave[j][a]);
+            Real face = dotd(acc, e, D);
+            Real p_wall = f.p[i] + f.rho[i] * rij * std::max(Real(0), face);
+            V3 be = mul(ck.B[i], e, D);
+            for (int a = 0; a < D; ++a)
+                wforce[a] -= (f.p[i] + p_wall) * be[a] * dWV;
+            wdis += (f.p[i] - p_wall) * cs.inv_rho0c0_ave * dWV;
+        }
+        for (int a = 0; a < D; ++a)
+            f.force[i][a] += wforce[a] * f.Vol[i];
+        ck.compression_rate[i] += wdis * ck.compression[i];
+    }
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)f.n; ++i)
+        for (int a = 0; a < D; ++a)
+            f.vel[i][a] += (f.force_prior[i][a] + f.force[i][a]) / f.mass[i] * dt;
+}
+
+// AcousticStep2ndHalf<Inner<...>> + <Contact<Wall, ...>>: acoustic_step_2nd_half.hpp:20-120;
+// AverageV / DissipativePJump: riemann_solver_ck.hpp:20-45
+void ckAcousticStep2ndHalf(Case &cs, Real dt)
+{
+    const int D = cs.D;
+    Body &f = cs.fluid;
+    CKState &ck = cs.ck;
+    const Real Z = cs.rho0c0, inv_Zsum = 1.0 / (Z + Z);
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)f.n; ++i)
+        for (int a = 0; a < D; ++a)
+            ck.dpos[i][a] += f.vel[i][a] * dt * 0.5;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)f.n; ++i)
+    {
+        Real divergence = 0;
+        V3 p_dis;
+        const Neighborhood &nb = cs.inner[i];
+        for (size_t k = 0; k < nb.size(); ++k)
+        {
+            UInt j = nb.j[k];
+            V3 r = sub3(f.pos[i], f.pos[j], D);
+            Real dWV = cs.tk.dW(std::sqrt(sqnorm(r, D))) * f.Vol[j];
+            V3 e = normalized(r, D);
+            V3 be = mul(ck.B[i], e, D), dv;
+            for (int a = 0; a < D; ++a)
+            {
+                Real v_ave = (f.vel[i][a] * Z + f.vel[j][a] * Z) * inv_Zsum;
+                dv[a] = f.vel[i][a] - v_ave;
+            }
+            divergence += 2.0 * dotd(dv, be, D) * dWV;
+            Real u_jump = dotd(sub3(f.vel[i], f.vel[j], D), e, D);
+            Real pj = cs.PJump(u_jump) * dWV;
+            for (int a = 0; a < D; ++a)
+                p_dis[a] += pj * e[a];
+        }
+        ck.compression_rate[i] += divergence * ck.compression[i];
+        for (int a = 0; a < D; ++a)
+            f.force[i][a] = p_dis[a] * f.Vol[i];
+        Real wdiv = 0;
+        V3 wdis;
+        const Neighborhood &nw = cs.contact[i];
+        for (size_t k = 0; k < nw.size(); ++k)
+        {
+            UInt j = nw.j[k];
+            V3 r = sub3(f.pos[i], cs.wall.pos[j], D);
+            Real dWV = cs.tk.dW(std::sqrt(sqnorm(r, D))) * cs.wall.Vol[j];
+            V3 e = normalized(r, D);
+            V3 vel_diff, be = mul(ck.B[i], e, D);
+            for (int a = 0; a < D; ++a)
+                vel_diff[a] = 2.0 * (f.vel[i][a] - cs.wall.vel_ave[j][a]);
+            wdiv += dotd(vel_diff, be, D) * dWV;
+            Real en = dotd(e, cs.wall.normal[j], D);
+            Real sgn = en > 0 ? 1.0 : (en < 0 ? -1.0 : 0.0);
+            V3 n_star;
+            for (int a = 0; a < D; ++a)
+                n_star[a] = sgn * cs.wall.normal[j][a];
+            Real pj = cs.PJump(dotd(vel_diff, n_star, D)) * dWV;
+            for (int a = 0; a < D; ++a)
+                wdis[a] += pj * n_star[a];
+        }
+        ck.compression_rate[i] += wdiv * ck.compression[i];
+        for (int a = 0; a < D; ++a)
+            f.force[i][a] += wdis[a] * f.Vol[i];
+    }
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)f.n; ++i)
+    {
+        ck.compression[i] += 0.5 * dt * ck.compression_rate[i];
+        f.rho[i] = ck.compression[i] * cs.rho0;
+    }
+}
+
+// AcousticTimeStepCK: fluid_time_step_ck.hpp:25-57 (sound speed c0 for this fluid)
+Real ckAcousticTimeStep(const Case &cs)
+{
+    const Body &f = cs.fluid;
+    Real m = 0;
+    for (size_t i = 0; i < f.n; ++i)
+    {
+        V3 F;
+        for (int a = 0; a < cs.D; ++a)
+            F[a] = f.force[i][a] + f.force_prior[i][a];
+        Real acc_scale = std::sqrt(4.0 * cs.h_min * std::sqrt(sqnorm(F, cs.D)) / f.mass[i]);
+        m = std::max(m, std::max(cs.c0 + std::sqrt(sqnorm(f.vel[i], cs.D)), acc_scale));
+    }
+    return cs.acoustic_cfl * cs.h_min / (m + TinyReal);
+}
+
+// AdvectionTimeStepCK: fluid_time_step_ck.cpp:16-20, fluid_time_step_ck.h:106-109
+Real ckAdvectionTimeStep(const Case &cs)
+{
+    const Body &f = cs.fluid;
+    Real m = 0;
+    for (size_t i = 0; i < f.n; ++i)
+        m = std::max(m, sqnorm(f.vel[i], cs.D));
+    return cs.advection_cfl * cs.h_min / (std::max(std::sqrt(m), cs.U_ref) + TinyReal);
+}
+
+// The observer pressure through the tabulated kernel with the current fluid volumes
+// (Interpolation<Contact<Real>>: interpolation_dynamics.hpp:46-60)
+void ckObservePressure(Case &cs)
+{
+    Body &o = cs.observer;
+    for (size_t i = 0; i < o.n; ++i)
+    {
+        Real q = 0, ttl = 0;
+        const Neighborhood &nb = cs.obs[i];
+        for (size_t n = 0; n < nb.size(); ++n)
+        {
+            UInt j = nb.j[n];
+            Real r = std::sqrt(sqnorm(sub3(o.pos[i], cs.fluid.pos[j], cs.D), cs.D));
+            Real w = cs.tk.W(r) * cs.fluid.Vol[j];
+            q += w * cs.fluid.p[j];
+            ttl += w;
+        }
+        o.observed[i] = q / (ttl + TinyReal);
+    }
+}
+
+// Set-up part of dambreak_sycl.cpp:138-169: the advection interval from the initial state,
+// then density regularization, advection-step set-up and correction matrices.
+void ckInitialize(Case &cs)
+{
+    ckEnsureState(cs);
+    cs.ck.present_time = 0;
+    cs.ck.interval = ckAdvectionTimeStep(cs);
+    cs.ck.advection_steps = 0;
+    ckDensityRegularization(cs);
+    ckAdvectionStepSetup(cs);
+    ckLinearCorrectionMatrix(cs, 0.5);
+}
+
+// One pass of the dambreak_sycl.cpp:181-198 loop body up to the advection trigger:
+// acoustic dt, both halves, and on trigger the new interval and the position update.
+// Returns 1 when an advection step is due (the caller then observes and calls
+// ckConfiguration).
+int ckAcousticStep(Case &cs, Real *physical_time)
+{
+    Real dt = ckAcousticTimeStep(cs);
+    *physical_time += dt;
+    cs.ck.present_time += dt;
+    ckAcousticStep1stHalf(cs, dt);
+    ckAcousticStep2ndHalf(cs, dt);
+    if (cs.ck.present_time > cs.ck.interval)
+    {
+        cs.ck.present_time = 0;
+        cs.ck.interval = ckAdvectionTimeStep(cs);
+        cs.ck.advection_steps++;
+        ckUpdateParticlePosition(cs);
+        return 1;
+    }
+    return 0;
+}
+
+// dambreak_sycl.cpp:230-245: cell list, relations, density regularization, advection-step
+// set-up, correction matrices (the Morton re-sort of the driver only permutes particles and
+// is not applied).
+void ckConfiguration(Case &cs)
+{
+    cs.fluid_cells.update(cs.fluid);
+    updateConfiguration(cs);
+    ckDensityRegularization(cs);
+    ckAdvectionStepSetup(cs);
+    ckLinearCorrectionMatrix(cs, 0.5);
+}
+
 // Lattice generation: particle_generator_lattice_{2d,3d}.cpp:12-23
 template <class Contain>
 std::vector<V3> lattice(int D, const V3 &lo, const V3 &up, Real dp, Contain contain)
@@ -803,6 +1310,7 @@ extern "C"
         cs->h = d->h_ratio * d->dp;
         cs->h_min = cs->h;
         cs->kernel = Kernel(D, cs->h);
+        cs->tk = TabKernel(D, cs->h);
         cs->rho0 = d->rho0;
         cs->c0 = d->c0;
         cs->U_ref = d->U_ref;
@@ -879,6 +1387,23 @@ extern "C"
     static Body *body_of(Case *cs, int b) { return b == 0 ? &cs->fluid : (b == 1 ? &cs->wall : &cs->observer); }
 
     size_t orc_num_particles(void *h, int b) { return body_of(static_cast<Case *>(h), b)->n; }
+
+    // Resizes a body to n particles with zeroed variables and ids 0..n-1 (the caller sets
+    // every variable it needs with orc_set, then rebuilds cell lists and configurations):
+    // lets a test hold an arbitrary particle set, e.g. one rank's slab plus ghosts.
+    void orc_body_resize(void *h, int b, size_t n)
+    {
+        Case *cs = static_cast<Case *>(h);
+        body_of(cs, b)->resize(n);
+        cs->ck.ready = false;
+        if (b == 0)
+        {
+            cs->inner.clear();
+            cs->contact.clear();
+        }
+        if (b == 2)
+            cs->obs.clear();
+    }
 
     // Scalar case constants: 0 sigma0, 1 W0, 2 h, 3 rc, 4 contact depth, 5 inv_rho0c0_ave,
     // 6 rho0c0_geo_ave, 7 inv_c0_ave, 8 p0, 9 factor_W, 10 factor_dW
@@ -1065,6 +1590,65 @@ extern "C"
         return upperFront(*cs, axis, l, u);
     }
     double orc_lattice_number_density(int dim, double h, double dp) { return latticeNumberDensity(Kernel(dim, h), dp); }
+
+    // CK numerics (the tests_sycl dam-break drivers)
+    double orc_ck_kernel(void *h, int which, double r)
+    {
+        Case *cs = static_cast<Case *>(h);
+        return which == 0 ? cs->tk.W(r) : (which == 1 ? cs->tk.dW(r) : cs->tk.W0());
+    }
+    void orc_ck_initialize(void *h) { ckInitialize(*static_cast<Case *>(h)); }
+    int orc_ck_acoustic_step(void *h, double *physical_time)
+    {
+        return ckAcousticStep(*static_cast<Case *>(h), physical_time);
+    }
+    void orc_ck_configuration(void *h) { ckConfiguration(*static_cast<Case *>(h)); }
+    void orc_ck_density_regularization(void *h) { ckDensityRegularization(*static_cast<Case *>(h)); }
+    void orc_ck_advection_step_setup(void *h) { ckAdvectionStepSetup(*static_cast<Case *>(h)); }
+    void orc_ck_linear_correction_matrix(void *h, double alpha)
+    {
+        ckLinearCorrectionMatrix(*static_cast<Case *>(h), alpha);
+    }
+    void orc_ck_acoustic_1st_half(void *h, double dt) { ckAcousticStep1stHalf(*static_cast<Case *>(h), dt); }
+    void orc_ck_acoustic_2nd_half(void *h, double dt) { ckAcousticStep2ndHalf(*static_cast<Case *>(h), dt); }
+    double orc_ck_acoustic_time_step(void *h) { return ckAcousticTimeStep(*static_cast<Case *>(h)); }
+    double orc_ck_advection_time_step(void *h) { return ckAdvectionTimeStep(*static_cast<Case *>(h)); }
+    void orc_ck_update_particle_position(void *h) { ckUpdateParticlePosition(*static_cast<Case *>(h)); }
+    long orc_ck_advection_steps(void *h) { return static_cast<Case *>(h)->ck.advection_steps; }
+    void orc_ck_observe_pressure(void *h, double *out)
+    {
+        Case *cs = static_cast<Case *>(h);
+        updateObserverConfiguration(*cs);
+        ckObservePressure(*cs);
+        std::copy(cs->observer.observed.begin(), cs->observer.observed.end(), out);
+    }
+    // CK variables of the fluid: 0 Compression, 1 CompressionRate, 2 VolumetricMeasureRef,
+    // 3 CompressionSummation (n values); 4 Displacement (n x dim); 5 LinearCorrectionMatrix
+    // (n x dim x dim, row-major).
+    void orc_ck_get(void *h, int which, double *out)
+    {
+        Case *cs = static_cast<Case *>(h);
+        ckEnsureState(*cs);
+        CKState &ck = cs->ck;
+        const int D = cs->D;
+        size_t n = cs->fluid.n;
+        const std::vector<Real> *v = which == 0 ? &ck.compression
+                                     : which == 1 ? &ck.compression_rate
+                                     : which == 2 ? &ck.Vol_ref
+                                     : which == 3 ? &ck.compression_sum
+                                                  : nullptr;
+        if (v)
+            std::copy(v->begin(), v->end(), out);
+        else if (which == 4)
+            for (size_t i = 0; i < n; ++i)
+                for (int a = 0; a < D; ++a)
+                    out[i * D + a] = ck.dpos[i][a];
+        else
+            for (size_t i = 0; i < n; ++i)
+                for (int a = 0; a < D; ++a)
+                    for (int b = 0; b < D; ++b)
+                        out[(i * D + a) * D + b] = ck.B[i](a, b);
+    }
 
     // One advection step of the dam-break loop (Dambreak.cpp:166-220 for loop_style 0;
     // test_3d_dambreak/dambreak.cpp:183-224 for loop_style 1, whose acoustic dt is taken

@@ -228,6 +228,101 @@ extern "C" int sphx_body_register(sphx_body b, const char *name, sphx_dtype dtyp
     return b->require(name, dtype, ncomp, &f);
 }
 
+namespace
+{
+// AoS (count x nc) <-> rows [first, first + count) of an SoA array with row stride
+// `stride` (component c of row r at soa[c * stride + r]); 4- or 8-byte elements.
+template <typename T>
+__global__ void k_aos_to_soa(size_t count, int nc, const T *__restrict__ aos, T *__restrict__ soa, size_t stride,
+                             size_t first)
+{
+    size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= count * size_t(nc))
+        return;
+    size_t c = k / count, i = k - c * count;
+    soa[c * stride + first + i] = aos[i * size_t(nc) + c];
+}
+template <typename T>
+__global__ void k_soa_to_aos(size_t count, int nc, const T *__restrict__ soa, size_t stride, size_t first,
+                             T *__restrict__ aos)
+{
+    size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= count * size_t(nc))
+        return;
+    size_t i = k / size_t(nc), c = k - i * size_t(nc);
+    aos[k] = soa[c * stride + first + i];
+}
+
+int transpose(sphx_ctx ctx, size_t es, size_t count, int nc, size_t stride, size_t first, const void *src, void *dst,
+              bool to_soa)
+{
+    unsigned g = grid_for(count * size_t(nc), 256);
+    cudaStream_t s = ctx->stream;
+    if (es == 8)
+    {
+        if (to_soa)
+            k_aos_to_soa<<<g, 256, 0, s>>>(count, nc, static_cast<const double *>(src), static_cast<double *>(dst),
+                                           stride, first);
+        else
+            k_soa_to_aos<<<g, 256, 0, s>>>(count, nc, static_cast<const double *>(src), stride, first,
+                                           static_cast<double *>(dst));
+    }
+    else
+    {
+        if (to_soa)
+            k_aos_to_soa<<<g, 256, 0, s>>>(count, nc, static_cast<const uint32_t *>(src),
+                                           static_cast<uint32_t *>(dst), stride, first);
+        else
+            k_soa_to_aos<<<g, 256, 0, s>>>(count, nc, static_cast<const uint32_t *>(src), stride, first,
+                                           static_cast<uint32_t *>(dst));
+    }
+    SPHX_LAUNCHED(ctx);
+    return SPHX_OK;
+}
+
+// Host AoS rows -> device SoA rows [first, first + count): one copy of the host buffer (at
+// full link speed when the caller's buffer is pinned), then the transpose on the device.
+// Synchronous: the host buffer may be reused when the call returns.
+int upload_rows(sphx_body b, Field *f, const void *host, size_t first, size_t count)
+{
+    if (count == 0)
+        return SPHX_OK;
+    sphx_ctx ctx = b->ctx;
+    size_t es = dtype_size(f->dtype), bytes = count * size_t(f->ncomp) * es;
+    if (f->ncomp == 1)
+        SPHX_CUDA(cudaMemcpyAsync(static_cast<unsigned char *>(f->dev) + first * es, host, bytes,
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    else
+    {
+        SPHX_TRY(ctx->ensure_scratch(bytes));
+        SPHX_CUDA(cudaMemcpyAsync(ctx->d_scratch, host, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        SPHX_TRY(transpose(ctx, es, count, f->ncomp, b->n, first, ctx->d_scratch, f->dev, true));
+    }
+    SPHX_CUDA(cudaStreamSynchronize(ctx->stream));
+    return SPHX_OK;
+}
+
+// Device SoA rows -> host AoS: transpose on the device, then one copy (synchronises).
+int download_rows(sphx_body b, const Field *f, void *host, size_t first, size_t count)
+{
+    if (count == 0)
+        return SPHX_OK;
+    sphx_ctx ctx = b->ctx;
+    size_t es = dtype_size(f->dtype), bytes = count * size_t(f->ncomp) * es;
+    if (f->ncomp == 1)
+        SPHX_CUDA(cudaMemcpyAsync(host, static_cast<const unsigned char *>(f->dev) + first * es, bytes,
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    else
+    {
+        SPHX_TRY(ctx->ensure_scratch(bytes));
+        SPHX_TRY(transpose(ctx, es, count, f->ncomp, b->n, first, f->dev, ctx->d_scratch, false));
+        SPHX_CUDA(cudaMemcpyAsync(host, ctx->d_scratch, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    SPHX_CUDA(cudaStreamSynchronize(ctx->stream));
+    return SPHX_OK;
+}
+} // namespace
+
 extern "C" int sphx_body_upload(sphx_body b, const char *name, sphx_dtype dtype, int ncomp, const void *host,
                                 size_t n)
 {
@@ -237,18 +332,7 @@ extern "C" int sphx_body_upload(sphx_body b, const char *name, sphx_dtype dtype,
         return fail(SPHX_ERR_INVALID_ARG, "upload of %s: %zu values for a body of %zu particles", name, n, b->n);
     Field *f;
     SPHX_TRY(b->require(name, dtype, ncomp, &f));
-    size_t es = dtype_size(dtype);
-    if (n == 0)
-        return SPHX_OK;
-    // AoS -> SoA transpose on the host, then one copy per component.
-    std::vector<unsigned char> soa(n * ncomp * es);
-    const unsigned char *src = static_cast<const unsigned char *>(host);
-    for (size_t i = 0; i < n; ++i)
-        for (int c = 0; c < ncomp; ++c)
-            std::memcpy(&soa[(c * n + i) * es], &src[(i * ncomp + c) * es], es);
-    SPHX_CUDA(cudaMemcpyAsync(f->dev, soa.data(), soa.size(), cudaMemcpyHostToDevice, b->ctx->stream));
-    SPHX_CUDA(cudaStreamSynchronize(b->ctx->stream));
-    return SPHX_OK;
+    return upload_rows(b, f, host, 0, n);
 }
 
 extern "C" int sphx_body_download(sphx_body b, const char *name, void *host, size_t n)
@@ -260,17 +344,33 @@ extern "C" int sphx_body_download(sphx_body b, const char *name, void *host, siz
         return fail(SPHX_ERR_NOT_FOUND, "variable %s is not registered", name);
     if (n != b->n)
         return fail(SPHX_ERR_INVALID_ARG, "download of %s: buffer for %zu of %zu particles", name, n, b->n);
-    size_t es = dtype_size(f->dtype);
-    if (n == 0)
-        return SPHX_OK;
-    std::vector<unsigned char> soa(n * f->ncomp * es);
-    SPHX_CUDA(cudaMemcpyAsync(soa.data(), f->dev, soa.size(), cudaMemcpyDeviceToHost, b->ctx->stream));
-    SPHX_CUDA(cudaStreamSynchronize(b->ctx->stream));
-    unsigned char *dst = static_cast<unsigned char *>(host);
-    for (size_t i = 0; i < n; ++i)
-        for (int c = 0; c < f->ncomp; ++c)
-            std::memcpy(&dst[(i * f->ncomp + c) * es], &soa[(c * n + i) * es], es);
-    return SPHX_OK;
+    return download_rows(b, f, host, 0, n);
+}
+
+extern "C" int sphx_body_upload_rows(sphx_body b, const char *name, const void *host, size_t first, size_t count)
+{
+    if (!b || !name || (count && !host))
+        return fail(SPHX_ERR_INVALID_ARG, "invalid upload arguments");
+    Field *f = b->find(name);
+    if (!f)
+        return fail(SPHX_ERR_NOT_FOUND, "variable %s is not registered", name);
+    if (first > b->n || count > b->n - first)
+        return fail(SPHX_ERR_INVALID_ARG, "rows [%zu, %zu) of %s outside a body of %zu particles", first,
+                    first + count, name, b->n);
+    return upload_rows(b, f, host, first, count);
+}
+
+extern "C" int sphx_body_download_rows(sphx_body b, const char *name, void *host, size_t first, size_t count)
+{
+    if (!b || !name || (count && !host))
+        return fail(SPHX_ERR_INVALID_ARG, "invalid download arguments");
+    Field *f = b->find(name);
+    if (!f)
+        return fail(SPHX_ERR_NOT_FOUND, "variable %s is not registered", name);
+    if (first > b->n || count > b->n - first)
+        return fail(SPHX_ERR_INVALID_ARG, "rows [%zu, %zu) of %s outside a body of %zu particles", first,
+                    first + count, name, b->n);
+    return download_rows(b, f, host, first, count);
 }
 
 extern "C" int sphx_body_device_ptr(sphx_body b, const char *name, void **dev, sphx_dtype *dtype, int *ncomp)

@@ -52,6 +52,8 @@ SIGNATURES = {
     "sphx_body_register": (_i, [_vp, C.c_char_p, _i, _i]),
     "sphx_body_upload": (_i, [_vp, C.c_char_p, _i, _i, _vp, _sz]),
     "sphx_body_download": (_i, [_vp, C.c_char_p, _vp, _sz]),
+    "sphx_body_upload_rows": (_i, [_vp, C.c_char_p, _vp, _sz, _sz]),
+    "sphx_body_download_rows": (_i, [_vp, C.c_char_p, _vp, _sz, _sz]),
     "sphx_body_device_ptr": (_i, [_vp, C.c_char_p, _pvp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "sphx_mesh_from_bounds": (_i, [_i, _pd, _pd, _d, _i, C.POINTER(MeshDesc)]),
     "sphx_cell_list_create": (_i, [_vp, C.POINTER(MeshDesc), _sz, _pvp]),

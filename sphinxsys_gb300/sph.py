@@ -287,12 +287,37 @@ class SPHBody:
         ncomp = 1 if a.ndim == 1 else a.shape[1]
         N.call("sphx_body_upload", self.handle, name.encode(), dtype, ncomp, a.ctypes.data_as(C.c_void_p), self.n)
 
-    def download(self, name: str) -> np.ndarray:
+    def download(self, name: str, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """Copies a variable to the host (AoS, n x ncomp; n for scalars).  `out`, when given,
+        is a C-contiguous array of that size and type to fill (e.g. pinned host memory)."""
         ptr, dt, nc = C.c_void_p(), C.c_int(), C.c_int()
         N.call("sphx_body_device_ptr", self.handle, name.encode(), C.byref(ptr), C.byref(dt), C.byref(nc))
-        out = np.zeros((self.n, nc.value), dtype=np.float64 if dt.value == N.F64 else np.uint32)
-        N.call("sphx_body_download", self.handle, name.encode(), out.ctypes.data_as(C.c_void_p), self.n)
-        return out[:, 0].copy() if nc.value == 1 else out
+        dtype = np.float64 if dt.value == N.F64 else np.uint32
+        if out is not None:
+            if out.dtype != dtype or out.size != self.n * nc.value or not out.flags["C_CONTIGUOUS"]:
+                raise ValueError(f"download of {name}: out must be C-contiguous {dtype.__name__} of "
+                                 f"{self.n * nc.value} values")
+            N.call("sphx_body_download", self.handle, name.encode(), out.ctypes.data_as(C.c_void_p), self.n)
+            return out
+        res = np.zeros((self.n, nc.value), dtype=dtype)
+        N.call("sphx_body_download", self.handle, name.encode(), res.ctypes.data_as(C.c_void_p), self.n)
+        return res[:, 0].copy() if nc.value == 1 else res
+
+    def upload_rows(self, name: str, values: np.ndarray, first: int) -> None:
+        """Writes rows [first, first + len(values)) of a registered variable."""
+        a = np.ascontiguousarray(values)
+        count = a.shape[0] if a.ndim else 0
+        N.call("sphx_body_upload_rows", self.handle, name.encode(), a.ctypes.data_as(C.c_void_p), int(first), count)
+
+    def download_rows(self, name: str, first: int, count: int) -> np.ndarray:
+        """Rows [first, first + count) of a registered variable (count x ncomp; count for
+        scalars)."""
+        ptr, dt, nc = C.c_void_p(), C.c_int(), C.c_int()
+        N.call("sphx_body_device_ptr", self.handle, name.encode(), C.byref(ptr), C.byref(dt), C.byref(nc))
+        res = np.zeros((count, nc.value), dtype=np.float64 if dt.value == N.F64 else np.uint32)
+        N.call("sphx_body_download_rows", self.handle, name.encode(), res.ctypes.data_as(C.c_void_p), int(first),
+               int(count))
+        return res[:, 0].copy() if nc.value == 1 else res
 
     def device_ptr(self, name: str) -> int:
         ptr = C.c_void_p()
