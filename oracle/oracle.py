@@ -90,6 +90,26 @@ def lib() -> C.CDLL:
         L.orc_lattice_number_density.argtypes = [i, d, d]
         L.orc_set_num_threads.argtypes = [i]
         L.orc_get_max_threads.restype = i
+        L.orc_ck_kernel.restype = d
+        L.orc_ck_kernel.argtypes = [vp, i, d]
+        L.orc_ck_initialize.argtypes = [vp]
+        L.orc_ck_acoustic_step.restype = i
+        L.orc_ck_acoustic_step.argtypes = [vp, dp_]
+        L.orc_ck_configuration.argtypes = [vp]
+        L.orc_ck_density_regularization.argtypes = [vp]
+        L.orc_ck_advection_step_setup.argtypes = [vp]
+        L.orc_ck_linear_correction_matrix.argtypes = [vp, d]
+        L.orc_ck_acoustic_1st_half.argtypes = [vp, d]
+        L.orc_ck_acoustic_2nd_half.argtypes = [vp, d]
+        L.orc_ck_acoustic_time_step.restype = d
+        L.orc_ck_acoustic_time_step.argtypes = [vp]
+        L.orc_ck_advection_time_step.restype = d
+        L.orc_ck_advection_time_step.argtypes = [vp]
+        L.orc_ck_update_particle_position.argtypes = [vp]
+        L.orc_ck_advection_steps.restype = C.c_long
+        L.orc_ck_advection_steps.argtypes = [vp]
+        L.orc_ck_observe_pressure.argtypes = [vp, dp_]
+        L.orc_ck_get.argtypes = [vp, i, dp_]
         L.orc_advection_step.restype = i
         L.orc_advection_step.argtypes = [vp, i, C.c_long, dp_, dp_, dp_, i, dp_, dp_]
         _lib = L
@@ -249,3 +269,39 @@ class OracleCase:
                                        C.byref(Dt), int(observe), _p(obs), _p(en))
         self.iteration += 1
         return sub, Dt.value, obs[: self.n(OBSERVER)], float(en[0])
+
+    # ------------------------------------------------------------------ CK numerics
+    CK_FIELDS = ("Compression", "CompressionRate", "VolumetricMeasureRef", "CompressionSummation",
+                 "Displacement", "LinearCorrectionMatrix")
+
+    def ck_kernel(self, which: str, r: float = 0.0) -> float:
+        """Tabulated Wendland C2 of this case: which in ("W", "dW", "W0")."""
+        return float(lib().orc_ck_kernel(self.h, ("W", "dW", "W0").index(which), float(r)))
+
+    def ck_initialize(self) -> None:
+        lib().orc_ck_initialize(self.h)
+
+    def ck_acoustic_step(self) -> bool:
+        """One loop pass of dambreak_sycl.cpp; True when an advection step fell due (the
+        positions were moved; call ck_configuration after observing)."""
+        return bool(lib().orc_ck_acoustic_step(self.h, C.byref(self.physical_time)))
+
+    def ck_configuration(self) -> None:
+        lib().orc_ck_configuration(self.h)
+
+    def ck_advection_steps(self) -> int:
+        return int(lib().orc_ck_advection_steps(self.h))
+
+    def ck_observe_pressure(self) -> np.ndarray:
+        out = np.zeros(max(self.n(OBSERVER), 1))
+        lib().orc_ck_observe_pressure(self.h, _p(out))
+        return out[: self.n(OBSERVER)]
+
+    def ck_get(self, name: str) -> np.ndarray:
+        which = self.CK_FIELDS.index(name)
+        n, d = self.n(FLUID), self.dim
+        size = n * (1 if which < 4 else (d if which == 4 else d * d))
+        out = np.zeros(max(size, 1))
+        lib().orc_ck_get(self.h, which, _p(out))
+        out = out[:size]
+        return out if which < 4 else (out.reshape(n, d) if which == 4 else out.reshape(n, d, d))

@@ -66,3 +66,60 @@ def test_oracle_2d_dambreak_passes_reference_dtw_regression(golden):
     for q, cur in (("FluidObserver_Pressure", pressure), ("WaterBody_TotalMechanicalEnergy", energy)):
         ok, d = regression.passes(series_keys(golden, "dambreak2d/" + q), cur, golden[f"dambreak2d/{q}/dtw"])
         assert ok, (q, d)
+
+
+def test_ck_tabulated_kernel_matches_analytic_wendland():
+    """KernelTabulatedCK's cubic interpolation on 24 entries (dq = 0.1) against the
+    analytic Wendland C2 of the same smoothing length: exact at table nodes, within 1e-3
+    relative of the peak between them, zero slope at r = 0."""
+    oc = O.OracleCase(cases.dambreak_2d())
+    h = oc.constant("h")
+    fW, fdW = oc.constant("factor_W"), oc.constant("factor_dW")
+    assert abs(oc.ck_kernel("W0") - oc.constant("W0")) < 1e-12 * oc.constant("W0")
+    for q in np.linspace(0.0, 1.99, 200):
+        r = q * h
+        w = fW * (1 - 0.5 * q) ** 4 * (1 + 2 * q)
+        dw = fdW * 0.625 * (q - 2) ** 3 * q
+        assert abs(oc.ck_kernel("W", r) - w) < 1e-3 * fW
+        assert abs(oc.ck_kernel("dW", r) - dw) < 1e-3 * abs(fdW)
+    for k in range(0, 20):
+        q = 0.1 * k
+        w = fW * (1 - 0.5 * q) ** 4 * (1 + 2 * q)
+        assert abs(oc.ck_kernel("W", q * h) - w) < 1e-9 * fW
+    assert abs(oc.ck_kernel("dW", 0.0)) < 1e-9 * abs(fdW)
+
+
+def test_ck_correction_matrix_is_identity_on_a_full_lattice():
+    """LinearCorrectionMatrix (alpha 0.5) of an interior lattice particle is close to the
+    identity (B = (-sum r_ij nablaW_ij^T V_j)^-1 and the sum is about I there)."""
+    oc = O.OracleCase(cases.dambreak_2d())
+    oc.ck_initialize()
+    B = oc.ck_get("LinearCorrectionMatrix")
+    x = oc.get("Position")
+    interior = (x[:, 0] > 0.3) & (x[:, 0] < 1.7) & (x[:, 1] > 0.3) & (x[:, 1] < 0.7)
+    assert interior.sum() > 100
+    assert np.max(np.abs(B[interior] - np.eye(2))) < 0.05
+    c = oc.ck_get("Compression")
+    assert np.all(c >= 1.0)
+
+
+@pytest.mark.slow
+def test_ck_oracle_2d_dambreak_passes_reference_dtw_regression(golden):
+    """The CK numerics (tests_sycl/2d_examples/test_2d_dambreak_sycl/dambreak_sycl.cpp loop:
+    TriggerByInterval advection steps, observation every 200 advection steps) to t = 20
+    against the series stored with that test (regression_test_tool of the SYCL test)."""
+    oc = O.OracleCase(cases.dambreak_2d())
+    oc.ck_initialize()
+    pressure = [oc.ck_observe_pressure()[0]]
+    energy = [oc.total_mechanical_energy()]
+    while oc.physical_time.value < 20.0:
+        if oc.ck_acoustic_step():
+            if (1 + oc.ck_advection_steps()) % 200 == 0:
+                energy.append(oc.total_mechanical_energy())
+                pressure.append(oc.ck_observe_pressure()[0])
+            oc.ck_configuration()
+    assert 20 <= len(pressure) <= 26
+    for q, cur in (("FluidObserver_Pressure", pressure), ("WaterBody_TotalMechanicalEnergy", energy)):
+        ok, d = regression.passes(series_keys(golden, "dambreak2d_ck/" + q), cur,
+                                  golden[f"dambreak2d_ck/{q}/dtw"])
+        assert ok, (q, d)
