@@ -198,6 +198,39 @@ int sphx_total_mechanical_energy(sphx_body fluid, const double *gravity, double 
 int sphx_upper_front_in_axis_direction(sphx_body fluid, int axis, const double *region_lower,
                                        const double *region_upper, double *front);
 
+/* ------------------------------------------------------------------ CK numerics
+ * The particle methods of the tests_sycl dam-break drivers
+ * (tests/tests_sycl/2d_examples/test_2d_dambreak_sycl/dambreak_sycl.cpp:97-123), FP64,
+ * on the relations above: pair geometry from the current Position with the tabulated
+ * Wendland C2 (KernelTabulatedCK, kernel_tabulated_ck.h:37-62); the state variables
+ * Compression, CompressionRate, Displacement, LinearCorrectionMatrix (dim x dim,
+ * row-major components), VolumetricMeasureRef and CompressionSummation are registered on
+ * first use with their reference initial values (1, 0, 0, identity, a copy of
+ * VolumetricMeasure, 1). */
+/* CompressionSummation<Inner, Contact> + DensityRegularization<FreeSurface>
+ * (density_regularization.hpp:40-118). */
+int sphx_ck_density_regularization(sphx_relation inner, sphx_relation wall_contact, const sphx_fluid_params *p);
+/* AdvectionStepSetup (fluid_time_step_ck.h:145-149): Vol = m / rho, Displacement = 0. */
+int sphx_ck_advection_step_setup(sphx_body fluid);
+/* UpdateParticlePosition (fluid_time_step_ck.h:173-176): Position += Displacement. */
+int sphx_ck_update_particle_position(sphx_body fluid);
+/* LinearCorrectionMatrix<Inner<WithUpdate>> + <Contact> (kernel_correction_ck.hpp:25-80). */
+int sphx_ck_linear_correction_matrix(sphx_relation inner, sphx_relation wall_contact, double alpha);
+/* AcousticStep1stHalf / 2ndHalf <Inner<OneLevel, AcousticRiemannSolverCK, LinearCorrectionCK>>
+ * + <Contact<Wall, ...>> (acoustic_step_1st_half.hpp, acoustic_step_2nd_half.hpp). */
+int sphx_ck_acoustic_step_1st_half(sphx_relation inner, sphx_relation wall_contact, const sphx_fluid_params *p,
+                                   double dt);
+int sphx_ck_acoustic_step_2nd_half(sphx_relation inner, sphx_relation wall_contact, const sphx_fluid_params *p,
+                                   double dt);
+/* AcousticTimeStepCK / AdvectionTimeStepCK (fluid_time_step_ck.hpp:25-57,
+ * fluid_time_step_ck.cpp:16-20); synchronise. */
+int sphx_ck_acoustic_time_step(sphx_body fluid, const sphx_fluid_params *p, double *dt);
+int sphx_ck_advection_time_step(sphx_body fluid, const sphx_fluid_params *p, double *dt);
+/* Interpolation<Contact<Real>> of a fluid variable at the observer points with the
+ * tabulated kernel and the current volumes (interpolation_dynamics.hpp:46-60); out has
+ * one value per observer (synchronises). */
+int sphx_ck_observe_quantity(sphx_relation observer_contact, const char *name, double *out);
+
 /* ------------------------------------------------------------------ mixed precision
  * A fused solver for one fluid body against one static wall body (the dam-break
  * configuration of Dambreak.cpp) in mixed precision; it has no single reference

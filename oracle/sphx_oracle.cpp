@@ -1615,9 +1615,13 @@ extern "C"
     double orc_ck_advection_time_step(void *h) { return ckAdvectionTimeStep(*static_cast<Case *>(h)); }
     void orc_ck_update_particle_position(void *h) { ckUpdateParticlePosition(*static_cast<Case *>(h)); }
     long orc_ck_advection_steps(void *h) { return static_cast<Case *>(h)->ck.advection_steps; }
+    // The observer relation is searched on a cell list of the current positions (the
+    // driver's relation update at observation time runs on the cell list of the previous
+    // configuration; the fluid cell list is rebuilt right after it anyway).
     void orc_ck_observe_pressure(void *h, double *out)
     {
         Case *cs = static_cast<Case *>(h);
+        cs->fluid_cells.update(cs->fluid);
         updateObserverConfiguration(*cs);
         ckObservePressure(*cs);
         std::copy(cs->observer.observed.begin(), cs->observer.observed.end(), out);

@@ -13,7 +13,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libsphx_cuda.so")
-SOURCES = ["sphx_core.cu", "cell_list.cu", "relation.cu", "fluid.cu", "mixed.cu", "batch.cu"]
+SOURCES = ["sphx_core.cu", "cell_list.cu", "relation.cu", "fluid.cu", "mixed.cu", "batch.cu", "ck.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I", os.path.join(ROOT, "include")]

@@ -259,3 +259,70 @@ class MixedPrecisionDamBreak:
         if getattr(self, "handle", None) is not None and self._N._lib is not None:
             self._N._lib.sphx_mp_destroy(self.handle)
             self.handle = None
+
+
+class DamBreakCK:
+    """The dam break with the CK particle methods of
+    tests/tests_sycl/2d_examples/test_2d_dambreak_sycl/dambreak_sycl.cpp (FP64 on the CUDA
+    policy): set-up as ``DamBreak`` (bodies, relations, normals, gravity), then the CK
+    loop: every pass one acoustic step (AcousticTimeStepCK, both halves) and, when the
+    advection trigger fires, UpdateParticlePosition and the configuration update with
+    density regularization, advection-step set-up and correction matrices.  The driver's
+    Morton re-sort only permutes particles and is not applied."""
+
+    def __init__(self, case: DamBreakCase, device: int = 0):
+        self.fp64 = DamBreak(case, device=device)
+        self.case = case
+        sim = self.fp64
+        f, inner, contact = sim.water_block, sim.water_block_inner, sim.water_wall_contact
+        self.water_block = f
+        self.correction = S.LinearCorrectionMatrixCK(inner, contact, 0.5)
+        self.first_half = S.AcousticStep1stHalfCK(inner, contact)
+        self.second_half = S.AcousticStep2ndHalfCK(inner, contact)
+        self.regularization = S.DensityRegularizationCK(inner, contact)
+        self.setup = S.AdvectionStepSetupCK(f)
+        self.update_position = S.UpdateParticlePositionCK(f)
+        self.acoustic_dt = S.AcousticTimeStepCK(f)
+        self.advection_dt = S.AdvectionTimeStepCK(f, case.U_ref)
+        self.observe = S.ObservingQuantityCK(sim.fluid_observer_contact, "Pressure")
+        # dambreak_sycl.cpp:156-169: trigger from the initial state, then the set-up passes
+        self.advection_trigger = S.TriggerByInterval(self.advection_dt.exec())
+        self.regularization.exec()
+        self.setup.exec()
+        self.correction.exec()
+        self.physical_time = 0.0
+        self.advection_steps = 1  # RestartStep() + 1
+        self.acoustic_steps = 0
+
+    def acoustic_step(self) -> bool:
+        """One loop pass up to the trigger; True when an advection step fell due (positions
+        moved; observe, then call ``configuration``)."""
+        dt = self.acoustic_dt.exec()
+        self.physical_time += dt
+        self.advection_trigger.increment(dt)
+        self.first_half.exec(dt)
+        self.second_half.exec(dt)
+        self.acoustic_steps += 1
+        if self.advection_trigger(self.advection_dt):
+            self.advection_steps += 1
+            self.update_position.exec()
+            return True
+        return False
+
+    def configuration(self) -> None:
+        sim = self.fp64
+        self.water_block.updateCellLinkedList()
+        sim.water_block_inner.updateConfiguration()
+        sim.water_wall_contact.updateConfiguration()
+        self.regularization.exec()
+        self.setup.exec()
+        self.correction.exec()
+
+    def observe_pressure(self) -> np.ndarray:
+        sim = self.fp64
+        sim.water_block.updateCellLinkedList()
+        sim.fluid_observer_contact.updateConfiguration()
+        return self.observe.exec()
+
+    def mechanical_energy(self) -> float:
+        return self.fp64.mechanical_energy.exec()

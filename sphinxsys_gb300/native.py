@@ -79,6 +79,15 @@ SIGNATURES = {
     "sphx_observe_quantity": (_i, [_vp, C.c_char_p, _pd]),
     "sphx_total_mechanical_energy": (_i, [_vp, _pd, _pd]),
     "sphx_upper_front_in_axis_direction": (_i, [_vp, _i, _pd, _pd, _pd]),
+    "sphx_ck_density_regularization": (_i, [_vp, _vp, C.POINTER(FluidParams)]),
+    "sphx_ck_advection_step_setup": (_i, [_vp]),
+    "sphx_ck_update_particle_position": (_i, [_vp]),
+    "sphx_ck_linear_correction_matrix": (_i, [_vp, _vp, _d]),
+    "sphx_ck_acoustic_step_1st_half": (_i, [_vp, _vp, C.POINTER(FluidParams), _d]),
+    "sphx_ck_acoustic_step_2nd_half": (_i, [_vp, _vp, C.POINTER(FluidParams), _d]),
+    "sphx_ck_acoustic_time_step": (_i, [_vp, C.POINTER(FluidParams), _pd]),
+    "sphx_ck_advection_time_step": (_i, [_vp, C.POINTER(FluidParams), _pd]),
+    "sphx_ck_observe_quantity": (_i, [_vp, C.c_char_p, _pd]),
     "sphx_mp_create": (_i, [_vp, _vp, C.POINTER(FluidParams), _pd, _pvp]),
     "sphx_mp_destroy": (_i, [_vp]),
     "sphx_mp_advection_step": (_i, [_vp, _i, C.POINTER(C.c_int), _pd, _pd]),

@@ -629,3 +629,120 @@ class UpperFrontInAxisDirection:
         N.call("sphx_upper_front_in_axis_direction", self.body.handle, self.axis, _dptr(self.lo), _dptr(self.up),
                C.byref(out))
         return out.value
+
+
+# ------------------------------------------------------------------ CK particle methods
+# The dynamics the tests_sycl drivers add to their ParticleMethodContainer<par_ck>
+# (dambreak_sycl.cpp:97-123), on the CUDA policy.  Their state variables are registered
+# by the library on first use with the reference's initial values.
+class LinearCorrectionMatrixCK:
+    """addInteractionDynamics<LinearCorrectionMatrix, WithUpdate>(inner, alpha)
+    .addPostContactInteraction(contact)."""
+
+    def __init__(self, inner: InnerRelation, contact: Optional[ContactRelation], alpha: float = 0.5):
+        self.inner, self.contact, self.alpha = inner, contact, float(alpha)
+
+    def exec(self, dt: float = 0.0) -> None:
+        N.call("sphx_ck_linear_correction_matrix", self.inner.handle,
+               self.contact.handle if self.contact else None, self.alpha)
+
+
+class _CKFluidDynamics:
+    _fn = ""
+
+    def __init__(self, inner: InnerRelation, contact: Optional[ContactRelation]):
+        self.inner, self.contact = inner, contact
+        self.params = fluid_params(inner.body)
+
+    def exec(self, dt: float = 0.0) -> None:
+        args = [self.inner.handle, self.contact.handle if self.contact else None, C.byref(self.params)]
+        if self._fn != "sphx_ck_density_regularization":
+            args.append(float(dt))
+        N.call(self._fn, *args)
+
+
+class AcousticStep1stHalfCK(_CKFluidDynamics):
+    """AcousticStep1stHalf<OneLevel, AcousticRiemannSolverCK, LinearCorrectionCK> with its
+    Contact<Wall, ...> part."""
+    _fn = "sphx_ck_acoustic_step_1st_half"
+
+
+class AcousticStep2ndHalfCK(_CKFluidDynamics):
+    """AcousticStep2ndHalf<OneLevel, AcousticRiemannSolverCK, LinearCorrectionCK> with its
+    Contact<Wall, ...> part."""
+    _fn = "sphx_ck_acoustic_step_2nd_half"
+
+
+class DensityRegularizationCK(_CKFluidDynamics):
+    """CompressionSummation (inner + contact) with the post-state
+    DensityRegularization<WeaklyCompressibleFluid, FreeSurface>."""
+    _fn = "sphx_ck_density_regularization"
+
+
+class AdvectionStepSetupCK:
+    def __init__(self, body: SPHBody):
+        self.body = body
+
+    def exec(self, dt: float = 0.0) -> None:
+        N.call("sphx_ck_advection_step_setup", self.body.handle)
+
+
+class UpdateParticlePositionCK:
+    def __init__(self, body: SPHBody):
+        self.body = body
+
+    def exec(self, dt: float = 0.0) -> None:
+        N.call("sphx_ck_update_particle_position", self.body.handle)
+
+
+class AcousticTimeStepCK:
+    def __init__(self, body: SPHBody, acoustic_cfl: float = 0.6):
+        self.body = body
+        self.params = fluid_params(body, acoustic_cfl=acoustic_cfl)
+
+    def exec(self, dt: float = 0.0) -> float:
+        out = C.c_double()
+        N.call("sphx_ck_acoustic_time_step", self.body.handle, C.byref(self.params), C.byref(out))
+        return out.value
+
+
+class AdvectionTimeStepCK:
+    def __init__(self, body: SPHBody, U_ref: float, advection_cfl: float = 0.25):
+        self.body = body
+        self.params = fluid_params(body, U_ref=U_ref, advection_cfl=advection_cfl)
+
+    def exec(self, dt: float = 0.0) -> float:
+        out = C.c_double()
+        N.call("sphx_ck_advection_time_step", self.body.handle, C.byref(self.params), C.byref(out))
+        return out.value
+
+
+class ObservingQuantityCK:
+    """Interpolation<Contact<Real>> of a fluid variable at the observers (tabulated kernel,
+    current volumes)."""
+
+    def __init__(self, contact: ContactRelation, name: str):
+        self.contact, self.name = contact, name
+
+    def exec(self) -> np.ndarray:
+        out = np.zeros(max(1, self.contact.body.n))
+        N.call("sphx_ck_observe_quantity", self.contact.handle, self.name.encode(), _dptr(out))
+        return out[: self.contact.body.n]
+
+
+class TriggerByInterval:
+    """TimeStepper::TriggerByInterval (sph_solver.cpp:53-80): fires once the physical time
+    accumulated since it last fired exceeds the interval, then re-evaluates the interval."""
+
+    def __init__(self, interval: float):
+        self.present_time, self.interval = 0.0, float(interval)
+
+    def increment(self, dt: float) -> None:
+        self.present_time += dt
+
+    def __call__(self, evaluator) -> bool:
+        if self.present_time > self.interval:
+            self.present_time = 0.0
+            self.interval = evaluator.exec()
+            return True
+        return False
