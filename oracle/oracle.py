@@ -33,6 +33,12 @@ class OrcCaseDesc(C.Structure):
     ]
 
 
+class OrcTGVDesc(C.Structure):
+    _fields_ = [("dim", C.c_int), ("velocity_kind", C.c_int), ("L", C.c_double), ("dp", C.c_double),
+                ("h_ratio", C.c_double), ("rho0", C.c_double), ("U", C.c_double), ("c0", C.c_double),
+                ("Re", C.c_double)]
+
+
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (a second or two)."""
     src = os.path.join(HERE, "sphx_oracle.cpp")
@@ -110,6 +116,16 @@ def lib() -> C.CDLL:
         L.orc_ck_advection_steps.argtypes = [vp]
         L.orc_ck_observe_pressure.argtypes = [vp, dp_]
         L.orc_ck_get.argtypes = [vp, i, dp_]
+        L.orc_tgv_create.restype = vp
+        L.orc_tgv_create.argtypes = [C.POINTER(OrcTGVDesc)]
+        L.orc_tgv_advection_step.restype = i
+        L.orc_tgv_advection_step.argtypes = [vp, dp_, dp_]
+        L.orc_total_kinetic_energy.restype = d
+        L.orc_total_kinetic_energy.argtypes = [vp]
+        L.orc_maximum_speed.restype = d
+        L.orc_maximum_speed.argtypes = [vp]
+        L.orc_cell_entries.restype = sz
+        L.orc_cell_entries.argtypes = [vp, i]
         L.orc_advection_step.restype = i
         L.orc_advection_step.argtypes = [vp, i, C.c_long, dp_, dp_, dp_, i, dp_, dp_]
         _lib = L
@@ -305,3 +321,32 @@ class OracleCase:
         lib().orc_ck_get(self.h, which, _p(out))
         out = out[:size]
         return out if which < 4 else (out.reshape(n, d) if which == 4 else out.reshape(n, d, d))
+
+
+class OracleTGV(OracleCase):
+    """A Taylor-Green vortex held by the oracle (periodic box, no wall or observer)."""
+
+    def __init__(self, tgv):
+        self.case = tgv
+        self.dim = tgv.dim
+        self._desc = OrcTGVDesc(tgv.dim, tgv.velocity_kind, tgv.L, tgv.dp, tgv.h_ratio, tgv.rho0, tgv.U, tgv.c0,
+                                tgv.Re)
+        self.h = lib().orc_tgv_create(C.byref(self._desc))
+        self.iteration = 0
+        self.physical_time = C.c_double(0.0)
+        self.acoustic_dt = C.c_double(0.0)
+
+    def advection_step(self, observe: bool = False):
+        Dt = C.c_double()
+        sub = lib().orc_tgv_advection_step(self.h, C.byref(self.physical_time), C.byref(Dt))
+        self.iteration += 1
+        return sub, Dt.value
+
+    def kinetic_energy(self) -> float:
+        return float(lib().orc_total_kinetic_energy(self.h))
+
+    def maximum_speed(self) -> float:
+        return float(lib().orc_maximum_speed(self.h))
+
+    def cell_entries(self) -> int:
+        return int(lib().orc_cell_entries(self.h, FLUID))

@@ -333,31 +333,77 @@ struct Neighborhood
     size_t size() const { return j.size(); }
 };
 
-// Cell lists: cell_linked_list.cpp:22-101; canonical ascending-index order.
+// Periodic images of PeriodicConditionUsingCellLinkedList (domain_bounding.cpp:16-60): along
+// each periodic axis in turn, every entry (particle or an image of an earlier axis) with
+// lower < x_a < lower + rc gets an image at x_a + L in the cell list, every entry with
+// upper - rc < x_a < upper one at x_a - L.  Canonical order: per axis all lower-side images
+// in entry order, then all upper-side ones (the reference inserts them concurrently).
+struct Periodicity
+{
+    bool on[3] = {false, false, false};
+    Real lower[3] = {0, 0, 0}, upper[3] = {0, 0, 0};
+    Real rc = 0;
+    bool any() const { return on[0] || on[1] || on[2]; }
+};
+
+// Cell lists: cell_linked_list.cpp:22-101; canonical ascending-index order.  Entries are
+// the particles (entry e = particle e) followed by periodic images; particle_index[k] is
+// the particle of the k-th entry in cell order, entry_sorted[k] that entry.
 struct CellList
 {
     Mesh mesh;
-    std::vector<UInt> cell_offset, particle_index;
-    void update(const Body &b)
+    std::vector<UInt> cell_offset, particle_index, entry_sorted, entry_index;
+    std::vector<V3> entry_pos;
+    void update(const Body &b, const Periodicity *per = nullptr)
     {
+        entry_pos.assign(b.pos.begin(), b.pos.end());
+        entry_index.resize(b.n);
+        std::iota(entry_index.begin(), entry_index.end(), 0u);
+        if (per && per->any())
+            for (int a = 0; a < mesh.D; ++a)
+            {
+                if (!per->on[a])
+                    continue;
+                size_t n_cur = entry_pos.size();
+                Real L = per->upper[a] - per->lower[a];
+                for (int side = 0; side < 2; ++side)
+                    for (size_t e = 0; e < n_cur; ++e)
+                    {
+                        Real x = entry_pos[e][a];
+                        bool take = side == 0 ? (x > per->lower[a] && x < per->lower[a] + per->rc)
+                                              : (x < per->upper[a] && x > per->upper[a] - per->rc);
+                        if (!take)
+                            continue;
+                        V3 p = entry_pos[e];
+                        p[a] = side == 0 ? x + L : x - L;
+                        entry_pos.push_back(p);
+                        entry_index.push_back(entry_index[e]);
+                    }
+            }
+        size_t ne = entry_pos.size();
         size_t nc = mesh.numCells();
-        std::vector<UInt> cell(b.n);
+        std::vector<UInt> cell(ne);
         cell_offset.assign(nc + 1, 0);
 #pragma omp parallel for schedule(static)
-        for (long i = 0; i < (long)b.n; ++i)
+        for (long e = 0; e < (long)ne; ++e)
         {
             int c[3];
-            mesh.cellIndex(b.pos[i], c);
-            cell[i] = mesh.linear(c);
+            mesh.cellIndex(entry_pos[e], c);
+            cell[e] = mesh.linear(c);
         }
-        for (size_t i = 0; i < b.n; ++i)
-            cell_offset[cell[i] + 1]++;
+        for (size_t e = 0; e < ne; ++e)
+            cell_offset[cell[e] + 1]++;
         for (size_t c = 0; c < nc; ++c)
             cell_offset[c + 1] += cell_offset[c];
         std::vector<UInt> fill(cell_offset.begin(), cell_offset.end() - 1);
-        particle_index.assign(std::max(b.n, nc), 0);
-        for (size_t i = 0; i < b.n; ++i)
-            particle_index[fill[cell[i]]++] = UInt(i);
+        entry_sorted.assign(std::max(ne, nc), 0);
+        particle_index.assign(std::max(ne, nc), 0);
+        for (size_t e = 0; e < ne; ++e)
+        {
+            UInt k = fill[cell[e]]++;
+            entry_sorted[k] = UInt(e);
+            particle_index[k] = entry_index[e];
+        }
     }
 };
 
@@ -498,6 +544,11 @@ struct Case
     WallShape wall_shape;
     TabKernel tk;
     CKState ck;
+    // Taylor-Green set-up (taylor_green.cpp): periodic box, viscosity, plain DensitySummation
+    Periodicity periodic;
+    Real mu = 0;
+    bool free_surface = true;
+    std::vector<V3> viscous_force, prev_viscous;
     V3 sys_lo, sys_up;
     Mesh sort_mesh;
 
@@ -541,9 +592,10 @@ void searchNeighbors(const Case &cs, const Body &src, const Body &tgt, const Cel
                     for (UInt k = cl.cell_offset[lc]; k < cl.cell_offset[lc + 1]; ++k)
                     {
                         UInt j = cl.particle_index[k];
+                        const V3 &xj = cl.entry_pos[cl.entry_sorted[k]]; // the particle or its image
                         V3 d;
                         for (int a = 0; a < D; ++a)
-                            d[a] = src.pos[i][a] - tgt.pos[j][a];
+                            d[a] = src.pos[i][a] - xj[a];
                         Real r2 = sqnorm(d, D);
                         if (r2 < cs.kernel.rc_sqr && (!INNER || UInt(i) != j))
                         {
@@ -596,9 +648,10 @@ void densitySummation(Case &cs)
         rho_sum += sigma_c * cs.rho0 * cs.rho0 * cs.inv_sigma0 / f.mass[i];
         f.rho_sum[i] = rho_sum;
     }
+    // DensitySummation<Inner<FreeSurface>>: max(rho_sum, rho0); <Inner<>>: rho_sum
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < (long)f.n; ++i)
-        f.rho[i] = std::max(f.rho_sum[i], cs.rho0);
+        f.rho[i] = cs.free_surface ? std::max(f.rho_sum[i], cs.rho0) : f.rho_sum[i];
 }
 
 //------------------------------------------------------------------------------
@@ -1236,11 +1289,143 @@ int ckAcousticStep(Case &cs, Real *physical_time)
 // is not applied).
 void ckConfiguration(Case &cs)
 {
-    cs.fluid_cells.update(cs.fluid);
+    cs.fluid_cells.update(cs.fluid, &cs.periodic);
     updateConfiguration(cs);
     ckDensityRegularization(cs);
     ckAdvectionStepSetup(cs);
     ckLinearCorrectionMatrix(cs, 0.5);
+}
+
+//------------------------------------------------------------------------------
+// Taylor-Green vortex (tests/2d_examples/test_2d_taylor_green/taylor_green.cpp)
+//------------------------------------------------------------------------------
+// ViscousForce<Inner<>, FixedViscosity, NoKernelCorrection> (viscous_dynamics.hpp:25-53)
+// with the ForcePrior update (force_prior.hpp:22-26)
+void viscousForceInner(Case &cs)
+{
+    const int D = cs.D;
+    Body &f = cs.fluid;
+    cs.viscous_force.resize(f.n);
+    cs.prev_viscous.resize(f.n);
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)f.n; ++i)
+    {
+        V3 force;
+        const Neighborhood &nb = cs.inner[i];
+        for (size_t n = 0; n < nb.size(); ++n)
+        {
+            UInt j = nb.j[n];
+            const V3 &e = nb.e[n];
+            Real denom = nb.r[n] + 0.01 * cs.h;
+            Real ee = 0;
+            for (int a = 0; a < D; ++a)
+                ee += e[a] * (2.0 * e[a]); // e . ((B_i + B_j) e) with B = 1
+            for (int a = 0; a < D; ++a)
+            {
+                Real vd = (f.vel[i][a] - f.vel[j][a]) / denom;
+                force[a] += ee * cs.mu * vd * nb.dW[n] * f.Vol[j];
+            }
+        }
+        for (int a = 0; a < D; ++a)
+            cs.viscous_force[i][a] = force[a] * f.Vol[i];
+    }
+    for (size_t i = 0; i < f.n; ++i)
+        for (int a = 0; a < D; ++a)
+        {
+            f.force_prior[i][a] += cs.viscous_force[i][a] - cs.prev_viscous[i][a];
+            cs.prev_viscous[i][a] = cs.viscous_force[i][a];
+        }
+}
+
+// TransportVelocityCorrection<Inner<SPHAdaptation, TruncatedLinear>> with coefficient 0.2
+// and the default limiter slope 100 (transport_velocity_correction.hpp:32-66,
+// common_functors.h:82-94)
+void transportVelocityCorrectionInner(Case &cs, Real coefficient)
+{
+    const int D = cs.D;
+    Body &f = cs.fluid;
+    std::vector<V3> inc(f.n);
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)f.n; ++i)
+    {
+        V3 s;
+        const Neighborhood &nb = cs.inner[i];
+        for (size_t n = 0; n < nb.size(); ++n)
+            for (int a = 0; a < D; ++a)
+                s[a] -= (1.0 + 1.0) * nb.dW[n] * f.Vol[nb.j[n]] * nb.e[n][a];
+        inc[i] = s;
+    }
+    Real h2 = cs.h * cs.h, scaling = coefficient * h2;
+    for (size_t i = 0; i < f.n; ++i)
+    {
+        Real sq = sqnorm(inc[i], D);
+        Real lim = std::min(100.0 * (h2 * sq), Real(1));
+        for (int a = 0; a < D; ++a)
+            f.pos[i][a] += scaling * lim * inc[i][a] * 1.0 * 1.0;
+    }
+}
+
+// PeriodicBounding::checkLowerBound / checkUpperBound (domain_bounding.h:103-113)
+void periodicBounding(Case &cs)
+{
+    Body &f = cs.fluid;
+    for (int a = 0; a < cs.D; ++a)
+    {
+        if (!cs.periodic.on[a])
+            continue;
+        Real L = cs.periodic.upper[a] - cs.periodic.lower[a];
+        for (size_t i = 0; i < f.n; ++i)
+        {
+            if (f.pos[i][a] < cs.periodic.lower[a])
+                f.pos[i][a] += L;
+            if (f.pos[i][a] > cs.periodic.upper[a])
+                f.pos[i][a] -= L;
+        }
+    }
+}
+
+// One pass of the taylor_green.cpp:133-164 advection loop; returns the acoustic sub-steps.
+int tgvAdvectionStep(Case &cs, Real *physical_time, Real *advection_dt)
+{
+    Real Dt = advectionTimeStep(cs);
+    densitySummation(cs);
+    viscousForceInner(cs);
+    transportVelocityCorrectionInner(cs, 0.2);
+    Real relaxation = 0;
+    int sub = 0;
+    while (relaxation < Dt)
+    {
+        Real dt = std::min(acousticTimeStep(cs), Dt);
+        relaxation += dt;
+        integration1stHalf(cs, dt);
+        integration2ndHalf(cs, dt);
+        *physical_time += dt;
+        ++sub;
+    }
+    periodicBounding(cs);
+    cs.fluid_cells.update(cs.fluid, &cs.periodic);
+    updateConfiguration(cs);
+    if (advection_dt)
+        *advection_dt = Dt;
+    return sub;
+}
+
+Real totalKineticEnergy(const Case &cs)
+{
+    const Body &f = cs.fluid;
+    Real e = 0;
+    for (size_t i = 0; i < f.n; ++i)
+        e += 0.5 * f.mass[i] * sqnorm(f.vel[i], cs.D);
+    return e;
+}
+
+Real maximumSpeed(const Case &cs)
+{
+    const Body &f = cs.fluid;
+    Real m = 0;
+    for (size_t i = 0; i < f.n; ++i)
+        m = std::max(m, std::sqrt(sqnorm(f.vel[i], cs.D)));
+    return m;
 }
 
 // Lattice generation: particle_generator_lattice_{2d,3d}.cpp:12-23
@@ -1376,7 +1561,7 @@ extern "C"
         cs->sort_mesh = m;
         // SearchDepthContact: base_body_relation.cpp:10-16
         cs->contact_depth = 1 + int(std::floor(cs->kernel.rc * (1.0 / m.gs)));
-        cs->fluid_cells.update(cs->fluid);
+        cs->fluid_cells.update(cs->fluid, &cs->periodic);
         cs->wall_cells.update(cs->wall);
         updateConfiguration(*cs);
         updateObserverConfiguration(*cs);
@@ -1523,7 +1708,7 @@ extern "C"
     {
         Case *cs = static_cast<Case *>(h);
         if (b == 0)
-            cs->fluid_cells.update(cs->fluid);
+            cs->fluid_cells.update(cs->fluid, &cs->periodic);
         else
             cs->wall_cells.update(cs->wall);
     }
@@ -1591,6 +1776,98 @@ extern "C"
     }
     double orc_lattice_number_density(int dim, double h, double dp) { return latticeNumberDensity(Kernel(dim, h), dp); }
 
+    // Taylor-Green vortex: a periodic box [0, L]^dim of lattice particles at rest density,
+    // velocity kind 0 the 2D taylor_green.cpp field (-cos 2pi x sin 2pi y, sin 2pi x cos 2pi y)
+    // on L = 1, kind 1 the 3D field (sin x cos y cos z, -cos x sin y cos z, 0) on L = 2 pi;
+    // mu = rho0 U L / Re, the Riemann dissipation of the 2nd half off (NoRiemannSolver),
+    // DensitySummation<Inner<>>, AdvectionViscousTimeStep reference speed max(U, mu/rho0/h).
+    struct OrcTGVDesc
+    {
+        int dim, velocity_kind;
+        double L, dp, h_ratio, rho0, U, c0, Re;
+    };
+    void *orc_tgv_create(const OrcTGVDesc *d)
+    {
+        Case *cs = new Case();
+        const int D = d->dim;
+        cs->D = D;
+        cs->dp = d->dp;
+        cs->h = d->h_ratio * d->dp;
+        cs->h_min = cs->h;
+        cs->kernel = Kernel(D, cs->h);
+        cs->tk = TabKernel(D, cs->h);
+        cs->rho0 = d->rho0;
+        cs->c0 = d->c0;
+        cs->p0 = d->rho0 * d->c0 * d->c0;
+        cs->mu = d->rho0 * d->U * d->L / d->Re;
+        cs->U_ref = std::max(d->U, cs->mu / d->rho0 / cs->h);
+        cs->limiter_slope = 0.0; // NoRiemannSolver in the 2nd half: DissipativePJump = 0
+        cs->free_surface = false;
+        for (int a = 0; a < 3; ++a)
+        {
+            cs->sys_lo[a] = 0.0;
+            cs->sys_up[a] = a < D ? d->L : 0.0;
+            cs->periodic.on[a] = a < D;
+            cs->periodic.lower[a] = 0.0;
+            cs->periodic.upper[a] = a < D ? d->L : 0.0;
+        }
+        cs->periodic.rc = cs->kernel.rc;
+        cs->sigma0 = latticeNumberDensity(cs->kernel, cs->dp);
+        cs->inv_sigma0 = 1.0 / cs->sigma0;
+        cs->W0 = cs->kernel.W0();
+        Real Z = cs->rho0 * cs->c0;
+        Real inv_sum = 1.0 / (Z + Z);
+        cs->rho0c0 = Z;
+        cs->inv_rho0c0_ave = (Z + Z) / (std::pow(Z, 2.0) + std::pow(Z, 2.0));
+        cs->rho0c0_geo_ave = 2.0 * Z * Z * inv_sum;
+        cs->inv_c0_ave = 0.5 * (cs->rho0 + cs->rho0) * cs->inv_rho0c0_ave;
+        Real vol = D == 2 ? cs->dp * cs->dp : cs->dp * cs->dp * cs->dp;
+        auto fpos = lattice(D, cs->sys_lo, cs->sys_up, cs->dp, [&](const V3 &) { return true; });
+        cs->fluid.resize(fpos.size());
+        cs->wall.resize(0);
+        cs->observer.resize(0);
+        for (size_t i = 0; i < fpos.size(); ++i)
+        {
+            const V3 &x = fpos[i];
+            cs->fluid.pos[i] = x;
+            cs->fluid.Vol[i] = vol;
+            cs->fluid.rho[i] = cs->rho0;
+            cs->fluid.mass[i] = cs->rho0 * vol;
+            V3 &v = cs->fluid.vel[i];
+            if (d->velocity_kind == 0)
+            {
+                v[0] = -std::cos(2.0 * Pi * x[0]) * std::sin(2.0 * Pi * x[1]);
+                v[1] = std::sin(2.0 * Pi * x[0]) * std::cos(2.0 * Pi * x[1]);
+            }
+            else
+            {
+                v[0] = std::sin(x[0]) * std::cos(x[1]) * std::cos(x[2]);
+                v[1] = -std::cos(x[0]) * std::sin(x[1]) * std::cos(x[2]);
+                v[2] = 0.0;
+            }
+        }
+        Mesh m = Mesh::fromBounds(D, cs->sys_lo, cs->sys_up, cs->kernel.rc, 2);
+        cs->fluid_cells.mesh = m;
+        cs->wall_cells.mesh = m;
+        cs->sort_mesh = m;
+        cs->contact_depth = 1 + int(std::floor(cs->kernel.rc * (1.0 / m.gs)));
+        cs->fluid_cells.update(cs->fluid, &cs->periodic);
+        cs->wall_cells.update(cs->wall);
+        updateConfiguration(*cs);
+        return cs;
+    }
+    int orc_tgv_advection_step(void *h, double *physical_time, double *advection_dt)
+    {
+        return tgvAdvectionStep(*static_cast<Case *>(h), physical_time, advection_dt);
+    }
+    double orc_total_kinetic_energy(void *h) { return totalKineticEnergy(*static_cast<Case *>(h)); }
+    double orc_maximum_speed(void *h) { return maximumSpeed(*static_cast<Case *>(h)); }
+    size_t orc_cell_entries(void *h, int b)
+    {
+        Case *cs = static_cast<Case *>(h);
+        return (b == 0 ? cs->fluid_cells : cs->wall_cells).entry_pos.size();
+    }
+
     // CK numerics (the tests_sycl dam-break drivers)
     double orc_ck_kernel(void *h, int which, double r)
     {
@@ -1621,7 +1898,7 @@ extern "C"
     void orc_ck_observe_pressure(void *h, double *out)
     {
         Case *cs = static_cast<Case *>(h);
-        cs->fluid_cells.update(cs->fluid);
+        cs->fluid_cells.update(cs->fluid, &cs->periodic);
         updateObserverConfiguration(*cs);
         ckObservePressure(*cs);
         std::copy(cs->observer.observed.begin(), cs->observer.observed.end(), out);
@@ -1698,7 +1975,7 @@ extern "C"
         long it = iteration + 1;
         if (it % 100 == 0 && it != 1)
             particleSorting(*cs);
-        cs->fluid_cells.update(cs->fluid);
+        cs->fluid_cells.update(cs->fluid, &cs->periodic);
         updateConfiguration(*cs);
         updateObserverConfiguration(*cs);
         return substeps;

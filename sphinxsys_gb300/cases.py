@@ -221,3 +221,39 @@ def _column_case(name: str, dim: int, L: float, H: float, W: float, dp: float) -
         water_center=water_hs, water_halfsize=water_hs, outer_center=inner_hs, outer_halfsize=outer_hs,
         inner_center=inner_hs, inner_halfsize=inner_hs, rho0=1.0, c0=c0, U_ref=U_ref, gravity=(0.0, 0.0, -g),
         observers=[(DL, 0.5 * DW, 0.2 * H)], loop_style=0, vertical_axis=2)
+
+
+@dataclass
+class TaylorGreenCase:
+    """A periodic Taylor-Green vortex: lattice particles in [0, L]^dim at rest density.
+
+    velocity_kind 0 is tests/2d_examples/test_2d_taylor_green/taylor_green.cpp:13-45
+    (L = 1, u = -cos 2pi x sin 2pi y, v = sin 2pi x cos 2pi y, U = 1, c0 = 10, Re = 100);
+    kind 1 the 3D vortex u = sin x cos y cos z, v = -cos x sin y cos z, w = 0 on
+    [0, 2 pi]^3 (rho0 = 1, c0 = 10, Re = 100)."""
+    name: str
+    dim: int
+    L: float
+    dp: float
+    velocity_kind: int = 0
+    h_ratio: float = 1.3
+    rho0: float = 1.0
+    U: float = 1.0
+    c0: float = 10.0
+    Re: float = 100.0
+
+    @property
+    def h(self) -> float:
+        return self.h_ratio * self.dp
+
+    @property
+    def mu(self) -> float:
+        return self.rho0 * self.U * self.L / self.Re
+
+
+def taylor_green_2d(resolution: int = 100) -> TaylorGreenCase:
+    return TaylorGreenCase(f"taylor_green2d_{resolution}", 2, 1.0, 1.0 / resolution, 0)
+
+
+def taylor_green_3d(resolution: int = 256) -> TaylorGreenCase:
+    return TaylorGreenCase(f"taylor_green3d_{resolution}", 3, 2.0 * math.pi, 2.0 * math.pi / resolution, 1)

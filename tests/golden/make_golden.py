@@ -26,6 +26,7 @@ CASES = {
     "dambreak3d_ck": "tests/tests_sycl/3d_examples/test_3d_dambreak_sycl/regression_test_tool",
     "stlw2d": "tests/2d_examples/test_2d_stlw/regression_test_tool",
     "still_water2d_ck": "tests/tests_sycl/2d_examples/test_2d_still_water_sycl/regression_test_tool",
+    "taylor_green2d": "tests/2d_examples/test_2d_taylor_green/regression_test_tool",
 }
 # the CK 3D pressure series (6 probes x ~2300 samples per run) is not used by the tests
 SKIP = {("dambreak3d_ck", "FluidObserver_Pressure")}

@@ -123,3 +123,40 @@ def test_ck_oracle_2d_dambreak_passes_reference_dtw_regression(golden):
         ok, d = regression.passes(series_keys(golden, "dambreak2d_ck/" + q), cur,
                                   golden[f"dambreak2d_ck/{q}/dtw"])
         assert ok, (q, d)
+
+
+def test_periodic_images_of_a_taylor_green_box():
+    """PeriodicConditionUsingCellLinkedList images: every particle within the cut-off of a
+    periodic face appears once more per face (corners once more per pair of faces), and the
+    inner relation of a periodic lattice is uniform: every particle has the full lattice
+    neighbourhood."""
+    tg = cases.taylor_green_2d(40)
+    o = O.OracleTGV(tg)
+    x = o.get("Position")
+    rc = o.constant("rc")
+    near = [(x[:, a] < rc) | (x[:, a] > 1.0 - rc) for a in range(2)]
+    expect = len(x) + near[0].sum() + near[1].sum() + (near[0] & near[1]).sum()
+    assert o.cell_entries() == expect
+    nb = o.neighbors(O.INNER)
+    assert np.all(nb["counts"] == 20)
+    assert np.all(nb["r"] < rc)
+
+
+@pytest.mark.slow
+def test_oracle_taylor_green_passes_reference_dtw_regression(golden):
+    """taylor_green.cpp to t = 5 (kinetic energy at t = 0 and every 0.1, maximum speed every
+    0.1) against the stored runs with RegressionTestDynamicTimeWarping's rule."""
+    o = O.OracleTGV(cases.taylor_green_2d())
+    ke, ms = [o.kinetic_energy()], []
+    while o.physical_time.value < 5.0:
+        integ = 0.0
+        while integ < 0.1:
+            t0 = o.physical_time.value
+            o.advection_step()
+            integ += o.physical_time.value - t0
+        ke.append(o.kinetic_energy())
+        ms.append(o.maximum_speed())
+    for q, cur in (("WaterBody_TotalKineticEnergy", ke), ("WaterBody_MaximumSpeed", ms)):
+        ok, d = regression.passes(series_keys(golden, "taylor_green2d/" + q), cur,
+                                  golden[f"taylor_green2d/{q}/dtw"])
+        assert ok, (q, d)
