@@ -115,6 +115,18 @@ int sphx_cell_list_num_cells(sphx_cell_list cl, size_t *ncells);
 /* Copies CellOffset (ncells+1) and ParticleIndex (n) to the host. */
 int sphx_cell_list_download(sphx_cell_list cl, uint32_t *cell_offset, uint32_t *particle_index, size_t n);
 
+/* PeriodicConditionUsingCellLinkedList (domain_bounding.cpp:16-60): once an axis is set, every
+ * update also inserts periodic images: along each periodic axis in turn, each entry (a
+ * particle or an image of an earlier axis) with lower < x < lower + cutoff gets an image at
+ * x + (upper - lower), each with upper - cutoff < x < upper one at x - (upper - lower).
+ * Relations built on the list see the images at their translated positions and record the
+ * real particle's index.  Requires 2 cutoff < upper - lower. */
+int sphx_cell_list_set_periodic(sphx_cell_list cl, int axis, double lower, double upper, double cutoff);
+/* Entries (particles + periodic images) of the last update. */
+int sphx_cell_list_num_entries(sphx_cell_list cl, size_t *n_entries);
+/* PeriodicBounding (domain_bounding.h:103-113): x < lower -> x + L, x > upper -> x - L. */
+int sphx_periodic_bounding(sphx_body body, int axis, double lower, double upper);
+
 /* exclusive_scan(ParallelDevicePolicy, ...) (src/src_sycl/shared/common/
  * algorithm_primitive_sycl.h:96-122): device u32 exclusive prefix sum of n entries,
  * returns the total through *total (synchronises). */
@@ -197,6 +209,24 @@ int sphx_total_mechanical_energy(sphx_body fluid, const double *gravity, double 
 /* UpperFrontInAxisDirection over an axis-aligned box region (general_reduce.h:82-99). */
 int sphx_upper_front_in_axis_direction(sphx_body fluid, int axis, const double *region_lower,
                                        const double *region_upper, double *front);
+
+/* Keeps r_ij in the relation's storage from its next update on (the viscous force needs the
+ * configuration-time distances; dam-break inner relations do without). */
+int sphx_relation_keep_distances(sphx_relation rel);
+/* InteractionWithUpdate<DensitySummationInner> (density_summation.hpp, Inner<> update:
+ * rho = rho_sum, no free-surface bound). */
+int sphx_density_summation_inner(sphx_relation inner, const sphx_fluid_params *p);
+/* InteractionWithUpdate<ViscousForceInner> (viscous_dynamics.hpp:25-53 with the ForcePrior
+ * update of force_prior.hpp:22-26): ViscousForce from the configuration-time r, e, dW
+ * (needs sphx_relation_keep_distances), ForcePrior += ViscousForce - PreviousViscousForce. */
+int sphx_viscous_force_inner(sphx_relation inner, double mu);
+/* InteractionWithUpdate<TransportVelocityCorrectionInner<TruncatedLinear, AllParticles>>
+ * (transport_velocity_correction.hpp:32-66): Position += coefficient h^2 min(100 h^2 |g|^2, 1) g,
+ * g = -sum 2 dW_ij V_j e_ij; the reference's coefficient default is 0.2. */
+int sphx_transport_velocity_correction_inner(sphx_relation inner, double coefficient);
+/* ReduceDynamics<MaximumSpeed> (general_reduce.h): max |v| (synchronises).  The total
+ * kinetic energy is sphx_total_mechanical_energy with zero gravity. */
+int sphx_maximum_speed(sphx_body body, double *out);
 
 /* ------------------------------------------------------------------ CK numerics
  * The particle methods of the tests_sycl dam-break drivers

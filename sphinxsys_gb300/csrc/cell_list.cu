@@ -195,6 +195,98 @@ __global__ void k_gather_sorted(size_t n, const uint32_t *__restrict__ idx, cons
     }
 }
 
+// ---------------------------------------------------------------- periodic images
+__global__ void k_entry_init(size_t n, int dim, const double *__restrict__ pos, size_t E, double *__restrict__ epos,
+                             uint32_t *__restrict__ eidx)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    for (int a = 0; a < dim; ++a)
+        epos[a * E + i] = pos[a * n + i];
+    eidx[i] = uint32_t(i);
+}
+
+// 1 for the entries that get an image on this side: lower < x < lower + rc (side 0) or
+// upper - rc < x < upper (side 1), strict as in domain_bounding.cpp:20-50
+__global__ void k_image_flags(size_t n_cur, size_t E, const double *__restrict__ epos, int axis, double lo, double hi,
+                              uint32_t *__restrict__ flag)
+{
+    size_t e = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (e >= n_cur)
+        return;
+    double x = epos[axis * E + e];
+    flag[e] = (x > lo && x < hi) ? 1u : 0u;
+}
+
+__global__ void k_image_emit(size_t n_cur, int dim, size_t E, double *__restrict__ epos, uint32_t *__restrict__ eidx,
+                             const uint32_t *__restrict__ flag, const uint32_t *__restrict__ scan, size_t base,
+                             int axis, double shift)
+{
+    size_t e = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (e >= n_cur || !flag[e])
+        return;
+    size_t k = base + scan[e];
+    for (int a = 0; a < dim; ++a)
+        epos[a * E + k] = epos[a * E + e] + (a == axis ? shift : 0.0);
+    eidx[k] = eidx[e];
+}
+
+template <int D>
+__global__ void k_entry_hash(size_t ne, size_t E, const double *__restrict__ epos, MeshDev m,
+                             uint32_t *__restrict__ cell_of, uint32_t *__restrict__ rank, uint32_t *__restrict__ count)
+{
+    size_t e = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (e >= ne)
+        return;
+    double x[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+        x[a] = epos[a * E + e];
+    int c[3];
+    cell_index<D>(m, x, c);
+    uint32_t lc = linear_cell<D>(m, c);
+    cell_of[e] = lc;
+    rank[e] = atomicAdd(&count[lc], 1u);
+}
+
+template <int D>
+__global__ void k_entry_gather(size_t ne, const uint32_t *__restrict__ perm, const uint32_t *__restrict__ cell_of,
+                               size_t E, const double *__restrict__ epos, const uint32_t *__restrict__ eidx,
+                               MeshDev m, uint32_t *__restrict__ pidx, double *__restrict__ spos,
+                               float *__restrict__ soff)
+{
+    size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= ne)
+        return;
+    uint32_t e = perm[k];
+    int c[3];
+    cell_from_linear<D>(m, cell_of[e], c);
+    pidx[k] = eidx[e];
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+    {
+        double x = epos[a * E + e];
+        spos[a * ne + k] = x;
+        soff[a * ne + k] = float(x - cell_corner(m, a, c[a]));
+    }
+}
+
+template <int D>
+__global__ void k_periodic_bounding(size_t n, double *__restrict__ pos, int axis, double lower, double upper)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    double x = pos[axis * n + i];
+    double L = upper - lower;
+    if (x < lower)
+        x += L;
+    if (x > upper)
+        x -= L;
+    pos[axis * n + i] = x;
+}
+
 template <int D>
 __global__ void k_morton_key(size_t n, const double *__restrict__ pos, MeshDev m, uint32_t *__restrict__ key)
 {
@@ -317,6 +409,42 @@ int counting_sort_by_key(sphx_ctx ctx, const uint32_t *d_key, size_t n, uint32_t
 }
 } // namespace sphx
 
+// Entry buffers of at least ne entries; the first `keep` entries survive a regrowth (the
+// SoA stride changes with the capacity).
+int sphx_cell_list_s::reserve_entries(size_t ne, size_t keep)
+{
+    if (ne <= entry_cap && entry_pos)
+        return SPHX_OK;
+    size_t cap = std::max<size_t>(ne + ne / 2, 64);
+    double *pos = nullptr;
+    uint32_t *idx = nullptr, *flag = nullptr, *scan = nullptr, *perm = nullptr;
+    SPHX_CUDA(cudaMalloc(&pos, 3 * cap * sizeof(double)));
+    SPHX_CUDA(cudaMalloc(&idx, cap * sizeof(uint32_t)));
+    SPHX_CUDA(cudaMalloc(&flag, cap * sizeof(uint32_t)));
+    SPHX_CUDA(cudaMalloc(&scan, cap * sizeof(uint32_t)));
+    SPHX_CUDA(cudaMalloc(&perm, cap * sizeof(uint32_t)));
+    if (keep && entry_pos)
+    {
+        for (int a = 0; a < mesh.dim; ++a)
+            SPHX_CUDA(cudaMemcpyAsync(pos + a * cap, entry_pos + a * entry_cap, keep * sizeof(double),
+                                      cudaMemcpyDeviceToDevice, ctx->stream));
+        SPHX_CUDA(cudaMemcpyAsync(idx, entry_idx, keep * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->stream));
+        SPHX_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    cudaFree(entry_pos);
+    cudaFree(entry_idx);
+    cudaFree(entry_flag);
+    cudaFree(entry_scan);
+    cudaFree(entry_perm);
+    entry_pos = pos;
+    entry_idx = idx;
+    entry_flag = flag;
+    entry_scan = scan;
+    entry_perm = perm;
+    entry_cap = cap;
+    return SPHX_OK;
+}
+
 int sphx_cell_list_s::reserve(size_t np)
 {
     if (np <= capacity && particle_index)
@@ -383,9 +511,152 @@ extern "C" int sphx_cell_list_destroy(sphx_cell_list cl)
     cudaFree(cl->rank);
     cudaFree(cl->sorted_pos);
     cudaFree(cl->sorted_off);
+    cudaFree(cl->entry_pos);
+    cudaFree(cl->entry_idx);
+    cudaFree(cl->entry_flag);
+    cudaFree(cl->entry_scan);
+    cudaFree(cl->entry_perm);
     sphx_ctx ctx = cl->ctx;
     delete cl;
     release(ctx);
+    return SPHX_OK;
+}
+
+namespace
+{
+// Cell list of the particles and their periodic images: entries are generated axis by axis
+// (lower-side images of all current entries, then upper-side ones, in entry order), then
+// sorted into cells by a stable counting sort of the entry numbers.
+int update_periodic(sphx_cell_list cl, sphx_body body, const double *pos)
+{
+    sphx_ctx ctx = cl->ctx;
+    cudaStream_t s = ctx->stream;
+    const int D = body->dim;
+    size_t n = body->n;
+    SPHX_TRY(cl->reserve_entries(2 * n + 64, 0));
+    if (n > 0)
+    {
+        k_entry_init<<<grid_for(n, kBlock), kBlock, 0, s>>>(n, D, pos, cl->entry_cap, cl->entry_pos, cl->entry_idx);
+        SPHX_LAUNCHED(ctx);
+    }
+    size_t n_cur = n;
+    for (int a = 0; a < D; ++a)
+    {
+        if (!(cl->periodic_mask & (1 << a)))
+            continue;
+        double lo = cl->per_lower[a], up = cl->per_upper[a], rc = cl->per_cutoff, L = up - lo;
+        size_t n_axis = n_cur; // the entries this axis images (both sides)
+        for (int side = 0; side < 2; ++side)
+        {
+            if (n_axis == 0)
+                break;
+            double band_lo = side == 0 ? lo : up - rc, band_hi = side == 0 ? lo + rc : up;
+            k_image_flags<<<grid_for(n_axis, kBlock), kBlock, 0, s>>>(n_axis, cl->entry_cap, cl->entry_pos, a,
+                                                                       band_lo, band_hi, cl->entry_flag);
+            SPHX_LAUNCHED(ctx);
+            uint32_t total = 0;
+            SPHX_TRY(exclusive_scan(ctx, cl->entry_flag, cl->entry_scan, n_axis));
+            // total = last scan value + last flag
+            uint32_t last[2] = {0, 0};
+            SPHX_CUDA(cudaMemcpyAsync(&last[0], cl->entry_scan + n_axis - 1, 4, cudaMemcpyDeviceToHost, s));
+            SPHX_CUDA(cudaMemcpyAsync(&last[1], cl->entry_flag + n_axis - 1, 4, cudaMemcpyDeviceToHost, s));
+            SPHX_CUDA(cudaStreamSynchronize(s));
+            total = last[0] + last[1];
+            if (total == 0)
+                continue;
+            if (n_cur + total > cl->entry_cap)
+            {
+                // regrowth keeps the entries generated so far; flags and scan are recomputed
+                SPHX_TRY(cl->reserve_entries(n_cur + total, n_cur));
+                k_image_flags<<<grid_for(n_axis, kBlock), kBlock, 0, s>>>(n_axis, cl->entry_cap, cl->entry_pos, a,
+                                                                           band_lo, band_hi, cl->entry_flag);
+                SPHX_LAUNCHED(ctx);
+                SPHX_TRY(exclusive_scan(ctx, cl->entry_flag, cl->entry_scan, n_axis));
+            }
+            k_image_emit<<<grid_for(n_axis, kBlock), kBlock, 0, s>>>(n_axis, D, cl->entry_cap, cl->entry_pos,
+                                                                      cl->entry_idx, cl->entry_flag, cl->entry_scan,
+                                                                      n_cur, a, side == 0 ? L : -L);
+            SPHX_LAUNCHED(ctx);
+            n_cur += total;
+        }
+    }
+    size_t ne = n_cur;
+    SPHX_TRY(cl->reserve(ne));
+    cl->n = n;
+    cl->n_entries = ne;
+    MeshDev m = mesh_dev(cl->mesh);
+    SPHX_CUDA(cudaMemsetAsync(cl->cell_count, 0, cl->ncells * sizeof(uint32_t), s));
+    if (ne > 0)
+    {
+        if (D == 2)
+            k_entry_hash<2><<<grid_for(ne, kBlock), kBlock, 0, s>>>(ne, cl->entry_cap, cl->entry_pos, m, cl->cell_of,
+                                                                    cl->rank, cl->cell_count);
+        else
+            k_entry_hash<3><<<grid_for(ne, kBlock), kBlock, 0, s>>>(ne, cl->entry_cap, cl->entry_pos, m, cl->cell_of,
+                                                                    cl->rank, cl->cell_count);
+        SPHX_LAUNCHED(ctx);
+    }
+    SPHX_TRY(exclusive_scan(ctx, cl->cell_count, cl->cell_offset, cl->ncells));
+    k_set_total<<<1, 1, 0, s>>>(cl->cell_offset, uint32_t(cl->ncells), uint32_t(ne));
+    SPHX_LAUNCHED(ctx);
+    if (ne == 0)
+        return SPHX_OK;
+    if (cl->entry_cap < ne)
+        SPHX_TRY(cl->reserve_entries(ne, ne));
+    k_scatter<<<grid_for(ne, kBlock), kBlock, 0, s>>>(ne, cl->cell_of, cl->rank, cl->cell_offset, cl->entry_perm);
+    SPHX_LAUNCHED(ctx);
+    k_sort_segments<<<grid_for(cl->ncells, kBlock), kBlock, 0, s>>>(cl->ncells, cl->cell_offset, cl->entry_perm);
+    SPHX_LAUNCHED(ctx);
+    if (D == 2)
+        k_entry_gather<2><<<grid_for(ne, kBlock), kBlock, 0, s>>>(ne, cl->entry_perm, cl->cell_of, cl->entry_cap,
+                                                                  cl->entry_pos, cl->entry_idx, m, cl->particle_index,
+                                                                  cl->sorted_pos, cl->sorted_off);
+    else
+        k_entry_gather<3><<<grid_for(ne, kBlock), kBlock, 0, s>>>(ne, cl->entry_perm, cl->cell_of, cl->entry_cap,
+                                                                  cl->entry_pos, cl->entry_idx, m, cl->particle_index,
+                                                                  cl->sorted_pos, cl->sorted_off);
+    SPHX_LAUNCHED(ctx);
+    return SPHX_OK;
+}
+} // namespace
+
+extern "C" int sphx_cell_list_set_periodic(sphx_cell_list cl, int axis, double lower, double upper, double cutoff)
+{
+    if (!cl || axis < 0 || axis >= cl->mesh.dim || !(upper > lower) || !(cutoff > 0) ||
+        !(2.0 * cutoff < upper - lower))
+        return fail(SPHX_ERR_INVALID_ARG, "invalid periodic axis (axis %d, [%g, %g], cut-off %g)", axis, lower, upper,
+                    cutoff);
+    cl->periodic_mask |= 1 << axis;
+    cl->per_lower[axis] = lower;
+    cl->per_upper[axis] = upper;
+    cl->per_cutoff = cutoff;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_cell_list_num_entries(sphx_cell_list cl, size_t *n_entries)
+{
+    if (!cl || !n_entries)
+        return fail(SPHX_ERR_INVALID_ARG, "null argument");
+    *n_entries = cl->n_entries;
+    return SPHX_OK;
+}
+
+extern "C" int sphx_periodic_bounding(sphx_body body, int axis, double lower, double upper)
+{
+    if (!body || axis < 0 || axis >= body->dim || !(upper > lower))
+        return fail(SPHX_ERR_INVALID_ARG, "invalid periodic bounding");
+    Field *pos;
+    SPHX_TRY(body->need("Position", SPHX_F64, body->dim, &pos));
+    if (body->n == 0)
+        return SPHX_OK;
+    double *p = static_cast<double *>(pos->dev);
+    if (body->dim == 2)
+        k_periodic_bounding<2><<<grid_for(body->n, kBlock), kBlock, 0, body->ctx->stream>>>(body->n, p, axis, lower,
+                                                                                           upper);
+    else
+        k_periodic_bounding<3><<<grid_for(body->n, kBlock), kBlock, 0, body->ctx->stream>>>(body->n, p, axis, lower,
+                                                                                           upper);
+    SPHX_LAUNCHED(body->ctx);
     return SPHX_OK;
 }
 
@@ -399,8 +670,11 @@ extern "C" int sphx_cell_list_update(sphx_cell_list cl, sphx_body body)
     SPHX_TRY(body->need("Position", SPHX_F64, body->dim, &pos));
     sphx_ctx ctx = cl->ctx;
     size_t n = body->n;
+    if (cl->periodic_mask)
+        return update_periodic(cl, body, static_cast<const double *>(pos->dev));
     SPHX_TRY(cl->reserve(n));
     cl->n = n;
+    cl->n_entries = n;
     cudaStream_t s = ctx->stream;
     MeshDev m = mesh_dev(cl->mesh);
     const double *p = static_cast<const double *>(pos->dev);

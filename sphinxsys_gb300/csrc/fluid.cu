@@ -88,7 +88,7 @@ struct WallVars
 __global__ void k_density_summation(size_t n, const double *__restrict__ sigma_inner,
                                     const double *__restrict__ sigma_wall, const double *__restrict__ mass,
                                     double rho0, double inv_sigma0, double *__restrict__ rho_sum,
-                                    double *__restrict__ rho)
+                                    double *__restrict__ rho, int free_surface)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -97,7 +97,8 @@ __global__ void k_density_summation(size_t n, const double *__restrict__ sigma_i
     if (sigma_wall)
         rs += sigma_wall[i] * rho0 * rho0 * inv_sigma0 / mass[i];
     rho_sum[i] = rs;
-    rho[i] = fmax(rs, rho0); // SMAX(rho_sum, rho0): FreeSurface update, Vol unchanged
+    // FreeSurface update SMAX(rho_sum, rho0) or the plain update rho = rho_sum; Vol unchanged
+    rho[i] = free_surface ? fmax(rs, rho0) : rs;
 }
 
 // ---------------------------------------------------------------- 1st half
@@ -511,6 +512,86 @@ int read_max(sphx_ctx ctx, double *out)
     return SPHX_OK;
 }
 
+// ViscousForce<Inner<>, FixedViscosity, NoKernelCorrection> (viscous_dynamics.hpp:25-53) and
+// the ForcePrior update (force_prior.hpp:22-26): the configuration-time r, e, dW of the inner
+// relation, e . (2 e) for the (absent) kernel correction.
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_viscous_inner(size_t n, Neighbors in, const double *__restrict__ vel,
+                                                          const double *__restrict__ Vol, double mu, double h,
+                                                          double *__restrict__ viscous, double *__restrict__ prev,
+                                                          double *__restrict__ force_prior)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    double f[3] = {0, 0, 0}, vi[3] = {0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+        vi[a] = vel[a * n + i];
+    const unsigned cnt = min(in.count[i], in.cap);
+    for (unsigned s = 0; s < cnt; ++s)
+    {
+        size_t slot = size_t(s) * n + i;
+        uint32_t j = in.J[slot];
+        double e[3] = {0, 0, 0};
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+            e[a] = in.E[a * in.stride + slot];
+        double ee = 0;
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+            ee += e[a] * (2.0 * e[a]);
+        double denom = in.R[slot] + 0.01 * h;
+        double dWV_factor = in.DW[slot];
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+        {
+            double vd = (vi[a] - vel[a * n + j]) / denom;
+            f[a] += ee * mu * vd * dWV_factor * Vol[j];
+        }
+    }
+    const double Vol_i = Vol[i];
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+    {
+        double v = f[a] * Vol_i;
+        force_prior[a * n + i] += v - prev[a * n + i];
+        prev[a * n + i] = v;
+        viscous[a * n + i] = v;
+    }
+}
+
+// TransportVelocityCorrection<Inner<SPHAdaptation, TruncatedLinear>> (transport_velocity_correction
+// .hpp:32-66): kernel-gradient integral from the configuration-time dW, e, then the position
+// shift with the limiter min(100 h^2 |.|^2, 1); interaction and update fused (the update
+// moves only the particle's own position, which no neighbour term reads).
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_tvc_inner(size_t n, Neighbors in, const double *__restrict__ Vol,
+                                                      double h2, double scaling, double *__restrict__ pos)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    double inc[3] = {0, 0, 0};
+    const unsigned cnt = min(in.count[i], in.cap);
+    for (unsigned s = 0; s < cnt; ++s)
+    {
+        size_t slot = size_t(s) * n + i;
+        uint32_t j = in.J[slot];
+        double w = (1.0 + 1.0) * in.DW[slot] * Vol[j];
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+            inc[a] -= w * in.E[a * in.stride + slot];
+    }
+    double sq = inc[0] * inc[0] + inc[1] * inc[1];
+    if (D == 3)
+        sq = sq + inc[2] * inc[2];
+    double lim = fmin(100.0 * (h2 * sq), 1.0);
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+        pos[a * n + i] += scaling * lim * inc[a] * 1.0 * 1.0;
+}
+
 unsigned reduce_grid(sphx_ctx ctx, size_t n)
 {
     unsigned g = grid_for(n, kBlock);
@@ -534,7 +615,7 @@ extern "C" int sphx_density_summation_complex_free_surface(sphx_relation inner, 
     sphx_ctx ctx = b->ctx;
     k_density_summation<<<grid_for(n, 256), 256, 0, ctx->stream>>>(n, inner->wsum, wall ? wall->wsum : nullptr,
                                                                    f.mass, p->rho0, 1.0 / p->sigma0, f.rho_sum,
-                                                                   f.rho);
+                                                                   f.rho, 1);
     SPHX_LAUNCHED(ctx);
     return SPHX_OK;
 }
@@ -722,6 +803,108 @@ extern "C" int sphx_total_mechanical_energy(sphx_body b, const double *g, double
     SPHX_LAUNCHED(ctx);
     SPHX_CUDA(cudaMemcpyAsync(energy, part + np, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     SPHX_CUDA(cudaStreamSynchronize(ctx->stream));
+    return SPHX_OK;
+}
+
+extern "C" int sphx_density_summation_inner(sphx_relation inner, const sphx_fluid_params *p)
+{
+    SPHX_TRY(check_pair(inner, nullptr, p));
+    sphx_body b = inner->src;
+    FluidVars f;
+    SPHX_TRY(fluid_vars(b, f));
+    size_t n = b->n;
+    if (n == 0)
+        return SPHX_OK;
+    sphx_ctx ctx = b->ctx;
+    k_density_summation<<<grid_for(n, 256), 256, 0, ctx->stream>>>(n, inner->wsum, nullptr, f.mass, p->rho0,
+                                                                   1.0 / p->sigma0, f.rho_sum, f.rho, 0);
+    SPHX_LAUNCHED(ctx);
+    return SPHX_OK;
+}
+
+extern "C" int sphx_viscous_force_inner(sphx_relation inner, double mu)
+{
+    if (!inner || !inner->inner)
+        return fail(SPHX_ERR_INVALID_ARG, "an inner relation is required");
+    if (!inner->r)
+        return fail(SPHX_ERR_INVALID_ARG, "the inner relation keeps no distances: call "
+                                          "sphx_relation_keep_distances before its update");
+    sphx_body b = inner->src;
+    if (inner->n_src != b->n)
+        return fail(SPHX_ERR_INVALID_ARG, "relation not updated for the current particle count");
+    const int D = b->dim;
+    Field *vel, *Vol, *fp, *visc, *prev;
+    SPHX_TRY(b->require("Velocity", SPHX_F64, D, &vel));
+    SPHX_TRY(b->need("VolumetricMeasure", SPHX_F64, 1, &Vol));
+    SPHX_TRY(b->require("ForcePrior", SPHX_F64, D, &fp));
+    SPHX_TRY(b->require("ViscousForce", SPHX_F64, D, &visc));
+    SPHX_TRY(b->require("PreviousViscousForce", SPHX_F64, D, &prev));
+    size_t n = b->n;
+    if (n == 0)
+        return SPHX_OK;
+    sphx_ctx ctx = b->ctx;
+    Neighbors in = neighbors_of(inner);
+    auto d = [](Field *f) { return static_cast<double *>(f->dev); };
+    if (D == 2)
+        k_viscous_inner<2><<<grid_for(n, kBlock), kBlock, 0, ctx->stream>>>(n, in, d(vel), d(Vol), mu, inner->h,
+                                                                            d(visc), d(prev), d(fp));
+    else
+        k_viscous_inner<3><<<grid_for(n, kBlock), kBlock, 0, ctx->stream>>>(n, in, d(vel), d(Vol), mu, inner->h,
+                                                                            d(visc), d(prev), d(fp));
+    SPHX_LAUNCHED(ctx);
+    return SPHX_OK;
+}
+
+extern "C" int sphx_transport_velocity_correction_inner(sphx_relation inner, double coefficient)
+{
+    if (!inner || !inner->inner)
+        return fail(SPHX_ERR_INVALID_ARG, "an inner relation is required");
+    sphx_body b = inner->src;
+    if (inner->n_src != b->n)
+        return fail(SPHX_ERR_INVALID_ARG, "relation not updated for the current particle count");
+    const int D = b->dim;
+    Field *pos, *Vol;
+    SPHX_TRY(b->need("Position", SPHX_F64, D, &pos));
+    SPHX_TRY(b->need("VolumetricMeasure", SPHX_F64, 1, &Vol));
+    size_t n = b->n;
+    if (n == 0)
+        return SPHX_OK;
+    sphx_ctx ctx = b->ctx;
+    double h2 = inner->h * inner->h;
+    Neighbors in = neighbors_of(inner);
+    double *p = static_cast<double *>(pos->dev);
+    const double *V = static_cast<const double *>(Vol->dev);
+    if (D == 2)
+        k_tvc_inner<2><<<grid_for(n, kBlock), kBlock, 0, ctx->stream>>>(n, in, V, h2, coefficient * h2, p);
+    else
+        k_tvc_inner<3><<<grid_for(n, kBlock), kBlock, 0, ctx->stream>>>(n, in, V, h2, coefficient * h2, p);
+    SPHX_LAUNCHED(ctx);
+    return SPHX_OK;
+}
+
+extern "C" int sphx_maximum_speed(sphx_body b, double *out)
+{
+    if (!b || !out)
+        return fail(SPHX_ERR_INVALID_ARG, "null argument");
+    Field *vel;
+    SPHX_TRY(b->require("Velocity", SPHX_F64, b->dim, &vel));
+    sphx_ctx ctx = b->ctx;
+    size_t n = b->n;
+    SPHX_CUDA(cudaMemsetAsync(ctx->d_red, 0, sizeof(unsigned long long), ctx->stream));
+    if (n > 0)
+    {
+        unsigned g = reduce_grid(ctx, n);
+        if (b->dim == 2)
+            k_acoustic_max<2><<<g, kBlock, 0, ctx->stream>>>(n, static_cast<const double *>(vel->dev), 0.0,
+                                                             ctx->d_red);
+        else
+            k_acoustic_max<3><<<g, kBlock, 0, ctx->stream>>>(n, static_cast<const double *>(vel->dev), 0.0,
+                                                             ctx->d_red);
+        SPHX_LAUNCHED(ctx);
+    }
+    double m = 0;
+    SPHX_TRY(read_max(ctx, &m));
+    *out = n > 0 ? m : 0.0;
     return SPHX_OK;
 }
 

@@ -183,6 +183,18 @@ int sphx_relation_s::allocate(int new_cap, size_t n)
     return SPHX_OK;
 }
 
+extern "C" int sphx_relation_keep_distances(sphx_relation rel)
+{
+    if (!rel)
+        return fail(SPHX_ERR_INVALID_ARG, "null relation");
+    if (!rel->store_r)
+    {
+        rel->store_r = true;
+        rel->n_src = size_t(-1); // storage is reallocated with distances at the next update
+    }
+    return SPHX_OK;
+}
+
 static int initial_capacity(int dim, bool inner) { return dim == 2 ? (inner ? 24 : 16) : (inner ? 96 : 64); }
 
 extern "C" int sphx_inner_relation_create(sphx_body body, sphx_cell_list cl, double h, sphx_relation *out)
@@ -248,7 +260,7 @@ static int launch_build(sphx_relation rel, unsigned int *d_max)
         SPHX_TRY(tgt->need("Mass", SPHX_F64, 1, &tmass));
     BuildArgs a{};
     a.n_src = src->n;
-    a.n_tgt = cl->n;
+    a.n_tgt = cl->n_entries; // stride of the cell-ordered entry arrays (images included)
     a.src_pos = static_cast<const double *>(spos->dev);
     a.cell_offset = cl->cell_offset;
     a.pidx = cl->particle_index;

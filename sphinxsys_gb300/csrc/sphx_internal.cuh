@@ -130,6 +130,16 @@ struct sphx_cell_list_s
     double *sorted_pos = nullptr;      // dim x capacity, cell order (FP64)
     float *sorted_off = nullptr;       // dim x capacity, cell order, offset from the cell's lower corner
     int reserve(size_t n);
+    // Periodic images (PeriodicConditionUsingCellLinkedList): with periodic axes the list
+    // holds n_entries >= n entries, the particles and their images; particle_index,
+    // sorted_pos and sorted_off then describe entries (stride n_entries).
+    size_t n_entries = 0;
+    int periodic_mask = 0;
+    double per_lower[3] = {0, 0, 0}, per_upper[3] = {0, 0, 0}, per_cutoff = 0;
+    size_t entry_cap = 0;
+    double *entry_pos = nullptr; // dim x entry_cap (SoA), entries in generation order
+    uint32_t *entry_idx = nullptr, *entry_flag = nullptr, *entry_scan = nullptr, *entry_perm = nullptr;
+    int reserve_entries(size_t ne, size_t keep);
 };
 
 struct sphx_relation_s

@@ -79,6 +79,14 @@ SIGNATURES = {
     "sphx_observe_quantity": (_i, [_vp, C.c_char_p, _pd]),
     "sphx_total_mechanical_energy": (_i, [_vp, _pd, _pd]),
     "sphx_upper_front_in_axis_direction": (_i, [_vp, _i, _pd, _pd, _pd]),
+    "sphx_cell_list_set_periodic": (_i, [_vp, _i, _d, _d, _d]),
+    "sphx_cell_list_num_entries": (_i, [_vp, _psz]),
+    "sphx_periodic_bounding": (_i, [_vp, _i, _d, _d]),
+    "sphx_relation_keep_distances": (_i, [_vp]),
+    "sphx_density_summation_inner": (_i, [_vp, C.POINTER(FluidParams)]),
+    "sphx_viscous_force_inner": (_i, [_vp, _d]),
+    "sphx_transport_velocity_correction_inner": (_i, [_vp, _d]),
+    "sphx_maximum_speed": (_i, [_vp, _pd]),
     "sphx_ck_density_regularization": (_i, [_vp, _vp, C.POINTER(FluidParams)]),
     "sphx_ck_advection_step_setup": (_i, [_vp]),
     "sphx_ck_update_particle_position": (_i, [_vp]),

@@ -367,6 +367,12 @@ class RealBody(SPHBody):
             self.cell_list = h
         N.call("sphx_cell_list_update", self.cell_list, self.handle)
 
+    def cell_list_entries(self) -> int:
+        """Entries of the cell list: the particles plus their periodic images."""
+        n = C.c_size_t()
+        N.call("sphx_cell_list_num_entries", self.cell_list, C.byref(n))
+        return n.value
+
     def cell_list_arrays(self):
         nc = C.c_size_t()
         N.call("sphx_cell_list_num_cells", self.cell_list, C.byref(nc))
@@ -746,3 +752,141 @@ class TriggerByInterval:
             self.interval = evaluator.exec()
             return True
         return False
+
+
+# ------------------------------------------------------------------ Taylor-Green pieces
+class Viscosity:
+    """addMaterialProperty<Viscosity>(mu): a fixed dynamic viscosity."""
+
+    def __init__(self, mu: float):
+        self.mu = float(mu)
+
+    def ReferenceViscosity(self) -> float:
+        return self.mu
+
+
+def addMaterialProperty(body: SPHBody, prop) -> None:
+    body.viscosity = prop
+
+
+class PeriodicAlongAxis:
+    """PeriodicAlongAxis(bounds, axis): the periodic box along one axis."""
+
+    def __init__(self, lower: Sequence[float], upper: Sequence[float], axis: int):
+        self.lower, self.upper, self.axis = float(lower[axis]), float(upper[axis]), int(axis)
+
+
+class _PeriodicBounding:
+    def __init__(self, body: RealBody, periodic: PeriodicAlongAxis):
+        self.body, self.p = body, periodic
+
+    def exec(self, dt: float = 0.0) -> None:
+        N.call("sphx_periodic_bounding", self.body.handle, self.p.axis, self.p.lower, self.p.upper)
+
+
+class _PeriodicCellLinkedList:
+    """The images are inserted by every update of the body's cell list once the axis is
+    registered; exec() is the reference's call site and does nothing further."""
+
+    def __init__(self, body: RealBody, periodic: PeriodicAlongAxis):
+        N.call("sphx_cell_list_set_periodic", body._cl_handle(), periodic.axis, periodic.lower, periodic.upper,
+               body.cutoff_radius)
+
+    def exec(self, dt: float = 0.0) -> None:
+        pass
+
+
+class PeriodicConditionUsingCellLinkedList:
+    def __init__(self, body: RealBody, periodic: PeriodicAlongAxis):
+        self.bounding_ = _PeriodicBounding(body, periodic)
+        self.update_cell_linked_list_ = _PeriodicCellLinkedList(body, periodic)
+
+
+class DensitySummationInner:
+    """Tag: InteractionWithUpdate<fluid_dynamics::DensitySummationInner>."""
+
+
+class ViscousForceInner:
+    """InteractionWithUpdate<fluid_dynamics::ViscousForceInner>(inner)."""
+
+    def __init__(self, inner: InnerRelation):
+        self.inner = inner
+        N.call("sphx_relation_keep_distances", inner.handle)
+
+    def exec(self, dt: float = 0.0) -> None:
+        N.call("sphx_viscous_force_inner", self.inner.handle, self.inner.body.viscosity.mu)
+
+
+class TransportVelocityCorrectionInner:
+    """InteractionWithUpdate<TransportVelocityCorrectionInner<TruncatedLinear, AllParticles>>."""
+
+    def __init__(self, inner: InnerRelation, coefficient: float = 0.2):
+        self.inner, self.coefficient = inner, float(coefficient)
+
+    def exec(self, dt: float = 0.0) -> None:
+        N.call("sphx_transport_velocity_correction_inner", self.inner.handle, self.coefficient)
+
+
+class DensitySummationInnerDynamics:
+    def __init__(self, inner: InnerRelation):
+        self.inner = inner
+        self.params = fluid_params(inner.body)
+
+    def exec(self, dt: float = 0.0) -> None:
+        N.call("sphx_density_summation_inner", self.inner.handle, C.byref(self.params))
+
+
+class Integration1stHalfInnerRiemann:
+    """Dynamics1Level<Integration1stHalfInnerRiemann>(inner)."""
+
+    def __init__(self, inner: InnerRelation):
+        self.inner = inner
+        self.params = fluid_params(inner.body)
+
+    def exec(self, dt: float = 0.0) -> None:
+        N.call("sphx_integration_1st_half_with_wall_riemann", self.inner.handle, None, C.byref(self.params),
+               float(dt))
+
+
+class Integration2ndHalfInnerNoRiemann:
+    """Dynamics1Level<Integration2ndHalfInnerNoRiemann>(inner): the 2nd half without the
+    Riemann dissipation (limiter slope 0 makes DissipativePJump zero)."""
+
+    def __init__(self, inner: InnerRelation):
+        self.inner = inner
+        self.params = fluid_params(inner.body)
+        self.params.limiter_slope = 0.0
+
+    def exec(self, dt: float = 0.0) -> None:
+        N.call("sphx_integration_2nd_half_with_wall_riemann", self.inner.handle, None, C.byref(self.params),
+               float(dt))
+
+
+class AdvectionViscousTimeStep(ReduceDynamics):
+    """ReduceDynamics<AdvectionViscousTimeStep>(body, U_ref): the reference speed is
+    max(U_ref, mu / rho0 / h) (fluid_time_step.cpp:67-74)."""
+
+    def __init__(self, body: SPHBody, U_ref: float):
+        viscous_speed = body.viscosity.mu / body.material.ReferenceDensity() / body.h
+        super().__init__(AdvectionTimeStep, body, max(viscous_speed, U_ref))
+
+
+class TotalKineticEnergy:
+    def __init__(self, body: SPHBody):
+        self.body = body
+
+    def exec(self) -> float:
+        out = C.c_double()
+        g = np.zeros(3)
+        N.call("sphx_total_mechanical_energy", self.body.handle, _dptr(g), C.byref(out))
+        return out.value
+
+
+class MaximumSpeed:
+    def __init__(self, body: SPHBody):
+        self.body = body
+
+    def exec(self) -> float:
+        out = C.c_double()
+        N.call("sphx_maximum_speed", self.body.handle, C.byref(out))
+        return out.value

@@ -1,0 +1,76 @@
+"""Taylor-Green vortex (periodic box, viscous force, transport-velocity correction) on the
+CUDA execution policy against the oracle, and the reference's regression rule on the GPU.
+
+Tolerance: FP64 fields within 1e-10 relative (max |gpu - oracle| / max |oracle|) after
+several advection steps: the device sums neighbours in the same order as the oracle but
+fuses multiply-adds, so the two agree to a few ulp per step."""
+import numpy as np
+import pytest
+
+from sphinxsys_gb300 import cases, regression
+from sphinxsys_gb300.taylor_green import TaylorGreen
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def rel_err(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(np.max(np.abs(b)), 1e-300))
+
+
+def small_3d():
+    # the 3D vortex on [0, 2 pi]^3 with 20 particles per side
+    return cases.TaylorGreenCase("taylor_green3d_20", 3, 2.0 * np.pi, 2.0 * np.pi / 20, 1)
+
+
+@pytest.mark.parametrize("case", [cases.taylor_green_2d(40), small_3d()], ids=lambda c: c.name)
+def test_taylor_green_matches_oracle(case):
+    g = TaylorGreen(case)
+    o = O.OracleTGV(case)
+    # the periodic images of the cell list: one entry per particle plus one per image
+    assert int(g.water_block.cell_list_entries()) == o.cell_entries()
+    assert abs(g.kinetic_energy.exec() / o.kinetic_energy() - 1) < 1e-12
+    for step in range(8):
+        s_g, dt_g = g.advection_step()
+        s_o, dt_o = o.advection_step()
+        assert s_g == s_o, step
+        assert abs(dt_g / dt_o - 1) < 1e-12, step
+    assert abs(g.physical_time / o.physical_time.value - 1) < 1e-12
+    assert int(g.water_block.cell_list_entries()) == o.cell_entries()
+    for name in ("Position", "Velocity", "Density", "Pressure", "Force", "ForcePrior"):
+        err = rel_err(g.water_block.download(name), o.get(name))
+        assert err < TOL, (name, err)
+    assert abs(g.kinetic_energy.exec() / o.kinetic_energy() - 1) < 1e-10
+    assert abs(g.maximum_speed.exec() / o.maximum_speed() - 1) < 1e-10
+
+
+def test_periodic_bounding_keeps_particles_in_the_box():
+    case = cases.taylor_green_2d(40)
+    g = TaylorGreen(case)
+    for _ in range(30):
+        g.advection_step()
+    x = g.water_block.download("Position")
+    assert np.all(x >= 0.0) and np.all(x <= case.L)
+
+
+def test_gpu_taylor_green_passes_reference_dtw_regression(golden):
+    """taylor_green.cpp to t = 5 on the GPU: kinetic energy at t = 0 and every 0.1 and
+    maximum speed every 0.1 against every stored run, with
+    RegressionTestDynamicTimeWarping's rule."""
+    g = TaylorGreen(cases.taylor_green_2d())
+    ke, ms = [g.kinetic_energy.exec()], []
+    while g.physical_time < 5.0:
+        integ = 0.0
+        while integ < 0.1:
+            t0 = g.physical_time
+            g.advection_step()
+            integ += g.physical_time - t0
+        ke.append(g.kinetic_energy.exec())
+        ms.append(g.maximum_speed.exec())
+    for q, cur in (("WaterBody_TotalKineticEnergy", ke), ("WaterBody_MaximumSpeed", ms)):
+        runs = [golden[k] for k in golden.files if k.startswith(f"taylor_green2d/{q}/Run_")]
+        ok, d = regression.passes(runs, cur, golden[f"taylor_green2d/{q}/dtw"])
+        assert ok, (q, d)
