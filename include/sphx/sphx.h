@@ -283,6 +283,19 @@ typedef struct sphx_mp_s *sphx_mp;
 /* Builds the solver from the current FP64 state of the relations' bodies. */
 int sphx_mp_create(sphx_relation inner, sphx_relation wall_contact, const sphx_fluid_params *p,
                    const double *gravity, sphx_mp *out);
+/* Periodic viscous flow without walls, periodic along every axis of the cube
+ * [lower, upper]: the taylor_green.cpp loop (taylor_green.cpp:133-164) with
+ * DensitySummationInner, ViscousForceInner with the fixed viscosity `viscosity`
+ * (viscous_dynamics.hpp:25-53; ForcePrior = the viscous force),
+ * TransportVelocityCorrectionInner with `tvc_coefficient` (transport_velocity_correction.hpp:32-66),
+ * Integration1stHalfInnerRiemann, Integration2ndHalf with p->limiter_slope (0 gives
+ * Integration2ndHalfInnerNoRiemann), AdvectionViscousTimeStep (reference speed
+ * max(p->U_ref, viscosity / rho0 / h)) and dt = min(acoustic dt, Dt) in the sub-steps
+ * (loop_style 0 of sphx_mp_advection_step).  Sub-cells tile the cube exactly:
+ * N = floor(L / h) per axis, 5 <= N <= 32768 (2D) / 1024 (3D); at most 2^26 particles.
+ * sphx_mp_download also writes ForcePrior. */
+int sphx_mp_create_periodic(sphx_body fluid, const sphx_fluid_params *p, const double *lower, const double *upper,
+                            double viscosity, double tvc_coefficient, sphx_mp *out);
 int sphx_mp_destroy(sphx_mp mp);
 /* One advection step.  loop_style 0: acoustic dt taken before each relaxation
  * (Dambreak.cpp:181-190); 1: after it (test_3d_dambreak/dambreak.cpp:193-201).

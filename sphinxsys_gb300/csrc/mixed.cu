@@ -41,6 +41,8 @@ struct MPConst
     MPParams p;
     double gd[3];
     double acoustic_cfl, advection_cfl, U_ref;
+    int periodic;        // periodic flow in the box [lo, up] (sphx_mp_create_periodic)
+    double lo[3], up[3];
 };
 using MPFluid = MPState;
 using MPLists = MPNeighbors;
@@ -52,17 +54,28 @@ struct MPWall : MPWallData
 // ---------------------------------------------------------------- (re)hash + sort
 // From FP64 body positions (creation).
 template <int D>
-__global__ void k_mp_from_fp64(size_t n, const double *__restrict__ pos, MeshDev m, uint32_t *__restrict__ ncell,
+__global__ void k_mp_from_fp64(size_t n, const double *__restrict__ pos, MPConst k, uint32_t *__restrict__ ncell,
                                float *__restrict__ noff, uint32_t *__restrict__ key, uint32_t *__restrict__ rank,
                                uint32_t *__restrict__ count)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
+    const MeshDev &m = k.m;
     double x[3] = {0, 0, 0};
 #pragma unroll
     for (int d = 0; d < D; ++d)
+    {
         x[d] = pos[d * n + i];
+        if (k.periodic)
+        {
+            const double L = k.up[d] - k.lo[d];
+            if (x[d] < k.lo[d])
+                x[d] += L;
+            if (x[d] > k.up[d])
+                x[d] -= L;
+        }
+    }
     int c[3] = {0, 0, 0};
     cell_index<D>(m, x, c);
 #pragma unroll
@@ -75,20 +88,33 @@ __global__ void k_mp_from_fp64(size_t n, const double *__restrict__ pos, MeshDev
 }
 
 // From the current (cell, offset) state: FP64 reconstruction of the position.
+// A periodic flow wraps the position into its box first, as PeriodicBounding does at the
+// end of the advection step (domain_bounding.h:103-113).
 template <int D>
-__global__ void k_mp_rehash(size_t n, const float4 *__restrict__ geo0, const float *__restrict__ off, MeshDev m,
+__global__ void k_mp_rehash(size_t n, const float4 *__restrict__ geo0, const float *__restrict__ off, MPConst k,
                             uint32_t *__restrict__ ncell, float *__restrict__ noff, uint32_t *__restrict__ key,
                             uint32_t *__restrict__ rank, uint32_t *__restrict__ count)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
+    const MeshDev &m = k.m;
     int c0[3];
     unpack_cell<D>(__float_as_uint(geo0[i].w), c0);
     double x[3] = {0, 0, 0};
 #pragma unroll
     for (int d = 0; d < D; ++d)
+    {
         x[d] = cell_corner(m, d, c0[d]) + double(off[d * n + i]);
+        if (k.periodic)
+        {
+            const double L = k.up[d] - k.lo[d];
+            if (x[d] < k.lo[d])
+                x[d] += L;
+            if (x[d] > k.up[d])
+                x[d] -= L;
+        }
+    }
     int c[3] = {0, 0, 0};
     cell_index<D>(m, x, c);
 #pragma unroll
@@ -151,6 +177,10 @@ __global__ void k_mp_gather(size_t n, const uint32_t *__restrict__ perm, const u
     dst.drho[k] = src.drho[i];
     dst.drho_dt[k] = src.drho_dt[i];
     dst.id[k] = src.id[i];
+    if (src.fprior)
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            dst.fprior[d * n + k] = src.fprior[d * n + i];
 }
 
 // ---------------------------------------------------------------- configuration + density sums
@@ -161,6 +191,29 @@ __global__ void k_mp_build(size_t n, MPConst k, MPFluid f, const uint32_t *__res
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i < n)
         build_particle<D>(i, n, k.p, Visit{k.m, 0u, f_offset, w_offset}, f, w, in, wl, max_counts);
+}
+
+template <int D>
+__global__ void k_mp_build_periodic(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPLists in,
+                                    unsigned int *max_counts)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n)
+        build_particle_periodic<D>(i, n, k.p, k.m, f_offset, f, in, max_counts);
+}
+
+// Start of a periodic-flow advection step: rho = rho_sum (DensitySummationInner) and the
+// transport-velocity shift of the positions.
+template <int D>
+__global__ void k_mp_density_periodic(size_t n, MPFluid f)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    f.drho[i] = f.drho_sum[i];
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        f.off[d * n + i] = f.off[d * n + i] + f.shift[d * n + i];
 }
 
 // DensitySummation update with the FreeSurface rule rho = max(rho_sum, rho0), at the
@@ -209,6 +262,29 @@ __global__ void k_mp_second(size_t n, MPConst k, MPFluid f, const uint32_t *__re
     warp_max_to(adv_slot, amax);
 }
 
+template <int D, bool LISTS>
+__global__ void __launch_bounds__(256, 4) k_mp_first_periodic(size_t n, MPConst k, MPFluid f,
+                                                               const uint32_t *__restrict__ f_offset, MPLists in,
+                                                               double dt, unsigned long long *ac_slot)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    double vmax = -1.0e300;
+    if (i < n)
+        vmax = first_particle_periodic<D, LISTS>(i, n, k.p, k.m, f_offset, dt, f, in);
+    warp_max_to(ac_slot, vmax);
+}
+
+template <int D, bool LISTS>
+__global__ void k_mp_second_periodic(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset,
+                                     MPLists in, double dt, unsigned long long *adv_slot)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    double amax = -1.0e300;
+    if (i < n)
+        amax = second_particle_periodic<D, LISTS>(i, n, k.p, k.m, f_offset, dt, f, in);
+    warp_max_to(adv_slot, amax);
+}
+
 template <int D>
 __global__ void k_mp_initial_max(size_t n, MPConst k, MPFluid f, unsigned long long *ac_slot,
                                  unsigned long long *adv_slot)
@@ -224,7 +300,7 @@ __global__ void k_mp_initial_max(size_t n, MPConst k, MPFluid f, unsigned long l
 // ---------------------------------------------------------------- FP64 body -> FP32 state
 struct ImportArgs
 {
-    const double *vel, *force, *rho, *drho_dt;
+    const double *vel, *force, *rho, *drho_dt, *fprior;
     double rho0, c0_sqr;
 };
 
@@ -240,6 +316,8 @@ __global__ void k_mp_import(size_t n, ImportArgs a, MPFluid f)
     {
         v[d] = a.vel ? float(a.vel[d * n + i]) : 0.f;
         f.force[d * n + i] = a.force ? float(a.force[d * n + i]) : 0.f;
+        if (f.fprior)
+            f.fprior[d * n + i] = a.fprior ? float(a.fprior[d * n + i]) : 0.f;
     }
     float dr = float(a.rho[i] - a.rho0);
     f.drho[i] = dr;
@@ -257,7 +335,7 @@ __device__ __forceinline__ double position(const MPConst &k, const MPFluid &f, s
 template <int D>
 __global__ void k_mp_download(size_t n, MPConst k, MPFluid f, double *__restrict__ pos, double *__restrict__ vel,
                               double *__restrict__ rho, double *__restrict__ p, double *__restrict__ force,
-                              double *__restrict__ drho_dt)
+                              double *__restrict__ drho_dt, double *__restrict__ fprior)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -273,6 +351,8 @@ __global__ void k_mp_download(size_t n, MPConst k, MPFluid f, double *__restrict
         pos[d * n + o] = position(k, f, n, i, d, c);
         vel[d * n + o] = v[d];
         force[d * n + o] = f.force[d * n + i];
+        if (fprior && f.fprior)
+            fprior[d * n + o] = f.fprior[d * n + i];
     }
     rho[o] = double(k.p.rho0) + double(f.drho[i]);
     p[o] = di.w; // pressure of the last 1st-half initialisation, as the FP64 body holds it
@@ -442,6 +522,13 @@ int alloc_state(sphx_mp mp, MPFluid &s)
     s.id = mp->alloc<uint32_t>(n);
     if (!s.geo0 || !s.dyn || !s.off || !s.force || !s.drho || !s.drho_dt || !s.drho_sum || !s.id)
         return fail(SPHX_ERR_OUT_OF_MEMORY, "mixed-precision state allocation failed");
+    if (mp->k.periodic)
+    {
+        s.fprior = mp->alloc<float>(D * n);
+        s.shift = mp->alloc<float>(D * n);
+        if (!s.fprior || !s.shift)
+            return fail(SPHX_ERR_OUT_OF_MEMORY, "mixed-precision state allocation failed");
+    }
     return SPHX_OK;
 }
 
@@ -485,8 +572,11 @@ int launch_build(sphx_mp mp)
     for (int attempt = 0; attempt < 2; ++attempt)
     {
         SPHX_CUDA(cudaMemsetAsync(mc, 0, 2 * sizeof(unsigned int), s));
-        k_mp_build<D><<<grid_for(mp->n, 256), 256, 0, s>>>(mp->n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset,
-                                                          mp->in, mp->wl, mc);
+        if (mp->k.periodic)
+            k_mp_build_periodic<D><<<grid_for(mp->n, 256), 256, 0, s>>>(mp->n, mp->k, mp->a, mp->f_offset, mp->in, mc);
+        else
+            k_mp_build<D><<<grid_for(mp->n, 256), 256, 0, s>>>(mp->n, mp->k, mp->a, mp->f_offset, mp->w,
+                                                              mp->w_offset, mp->in, mp->wl, mc);
         SPHX_LAUNCHED(ctx);
         SPHX_CUDA(cudaMemcpyAsync(mp->h_slots + 3, mc, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
         SPHX_CUDA(cudaStreamSynchronize(s));
@@ -520,7 +610,7 @@ int configuration_update(sphx_mp mp, bool from_state)
         SPHX_CUDA(cudaMemsetAsync(mp->count, 0, mp->ncells * sizeof(uint32_t), s));
         if (n > 0)
         {
-            k_mp_rehash<D><<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.geo0, mp->a.off, m, mp->ncell, mp->noff,
+            k_mp_rehash<D><<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.geo0, mp->a.off, mp->k, mp->ncell, mp->noff,
                                                             mp->key, mp->rank, mp->count);
             SPHX_LAUNCHED(ctx);
         }
@@ -567,7 +657,16 @@ int substep(sphx_mp mp, double dt)
         }
     if (e[0])
         SPHX_CUDA(cudaEventRecord(e[0], s));
-    if (mp->strategy == 0)
+    if (mp->k.periodic)
+    {
+        if (mp->strategy == 0)
+            k_mp_first_periodic<D, true><<<grid_for(n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->f_offset, mp->in, dt,
+                                                                         mp->slots);
+        else
+            k_mp_first_periodic<D, false><<<grid_for(n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->f_offset, mp->in, dt,
+                                                                          mp->slots);
+    }
+    else if (mp->strategy == 0)
         k_mp_first<D, true><<<grid_for(n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset,
                                                             mp->in, mp->wl, dt, mp->slots);
     else
@@ -578,7 +677,16 @@ int substep(sphx_mp mp, double dt)
         SPHX_CUDA(cudaEventRecord(e[1], s));
     if (e[2])
         SPHX_CUDA(cudaEventRecord(e[2], s));
-    if (mp->strategy == 0)
+    if (mp->k.periodic)
+    {
+        if (mp->strategy == 0)
+            k_mp_second_periodic<D, true><<<grid_for(n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->f_offset, mp->in, dt,
+                                                                          mp->slots + 1);
+        else
+            k_mp_second_periodic<D, false><<<grid_for(n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->f_offset, mp->in,
+                                                                           dt, mp->slots + 1);
+    }
+    else if (mp->strategy == 0)
         k_mp_second<D, true><<<grid_for(n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset,
                                                              mp->in, mp->wl, dt, mp->slots + 1);
     else
@@ -598,7 +706,10 @@ int advection_step(sphx_mp mp, int loop_style, int *substeps, double *adv_dt)
     double Dt = mp->k.advection_cfl * mp->k.p.h / (std::max(std::sqrt(adv_max), mp->k.U_ref) + kTinyReal);
     if (mp->n > 0)
     {
-        k_mp_density<<<grid_for(mp->n, 256), 256, 0, mp->ctx->stream>>>(mp->n, mp->a.drho_sum, mp->a.drho);
+        if (mp->k.periodic)
+            k_mp_density_periodic<D><<<grid_for(mp->n, 256), 256, 0, mp->ctx->stream>>>(mp->n, mp->a);
+        else
+            k_mp_density<<<grid_for(mp->n, 256), 256, 0, mp->ctx->stream>>>(mp->n, mp->a.drho_sum, mp->a.drho);
         SPHX_LAUNCHED(mp->ctx);
     }
     double relaxation = 0, dt = mp->acoustic_dt;
@@ -610,6 +721,8 @@ int advection_step(sphx_mp mp, int loop_style, int *substeps, double *adv_dt)
         {
             SPHX_TRY(read_slot(mp, 0, &ac));
             dt = mp->k.acoustic_cfl * mp->k.p.h / (ac + kTinyReal);
+            if (mp->k.periodic) // dt = SMIN(acoustic dt, Dt) (taylor_green.cpp:146)
+                dt = std::min(dt, Dt);
         }
         SPHX_TRY(substep<D>(mp, dt));
         if (loop_style == 1) // after it (test_3d_dambreak/dambreak.cpp:197)
@@ -668,33 +781,24 @@ int import_fluid(sphx_mp mp, sphx_body fb, double rho0, double c0)
     SPHX_CUDA(cudaStreamSynchronize(s));
     // fluid: FP64 body state -> FP32 (body order) in `a`, then the first configuration
     Field *pos = fb->find("Position"), *vel = fb->find("Velocity"), *force = fb->find("Force"),
-          *rho = fb->find("Density"), *drho = fb->find("DensityChangeRate");
+          *rho = fb->find("Density"), *drho = fb->find("DensityChangeRate"), *fprior = fb->find("ForcePrior");
     if (!pos || !rho)
         return fail(SPHX_ERR_NOT_FOUND, "fluid Position / Density missing");
     if (n > 0)
     {
         ImportArgs ia{(const double *)(vel ? vel->dev : nullptr), (const double *)(force ? force->dev : nullptr),
-                      (const double *)rho->dev, (const double *)(drho ? drho->dev : nullptr), rho0, c0 * c0};
+                      (const double *)rho->dev, (const double *)(drho ? drho->dev : nullptr),
+                      (const double *)(fprior && fprior->dtype == SPHX_F64 && fprior->ncomp == D ? fprior->dev
+                                                                                                 : nullptr),
+                      rho0, c0 * c0};
         if (D == 2)
             k_mp_import<2><<<grid_for(n, 256), 256, 0, s>>>(n, ia, mp->a);
         else
             k_mp_import<3><<<grid_for(n, 256), 256, 0, s>>>(n, ia, mp->a);
         SPHX_LAUNCHED(ctx);
     }
-    if (cudaMemsetAsync(mp->count, 0, nc * sizeof(uint32_t), s) != cudaSuccess)
-        return fail(SPHX_ERR_CUDA, "memset failed");
-    if (n > 0)
-    {
-        if (D == 2)
-            k_mp_from_fp64<2><<<grid_for(n, 256), 256, 0, s>>>(n, (const double *)pos->dev, m, mp->ncell, mp->noff,
-                                                               mp->key, mp->rank, mp->count);
-        else
-            k_mp_from_fp64<3><<<grid_for(n, 256), 256, 0, s>>>(n, (const double *)pos->dev, m, mp->ncell, mp->noff,
-                                                               mp->key, mp->rank, mp->count);
-        ctx->launches++;
-    }
-    SPHX_TRY(D == 2 ? configuration_update<2>(mp, false) : configuration_update<3>(mp, false));
-    // initial maxima for the first time steps
+    // maxima for the first time steps, from the imported state (the configuration below
+    // only reorders it, except for the prior force a periodic flow recomputes there)
     if (cudaMemsetAsync(mp->slots, 0, 2 * sizeof(unsigned long long), s) != cudaSuccess)
         return fail(SPHX_ERR_CUDA, "memset failed");
     if (n > 0)
@@ -705,6 +809,19 @@ int import_fluid(sphx_mp mp, sphx_body fb, double rho0, double c0)
             k_mp_initial_max<3><<<grid_for(n, 256), 256, 0, s>>>(n, mp->k, mp->a, mp->slots, mp->slots + 1);
         ctx->launches++;
     }
+    if (cudaMemsetAsync(mp->count, 0, nc * sizeof(uint32_t), s) != cudaSuccess)
+        return fail(SPHX_ERR_CUDA, "memset failed");
+    if (n > 0)
+    {
+        if (D == 2)
+            k_mp_from_fp64<2><<<grid_for(n, 256), 256, 0, s>>>(n, (const double *)pos->dev, mp->k, mp->ncell, mp->noff,
+                                                               mp->key, mp->rank, mp->count);
+        else
+            k_mp_from_fp64<3><<<grid_for(n, 256), 256, 0, s>>>(n, (const double *)pos->dev, mp->k, mp->ncell, mp->noff,
+                                                               mp->key, mp->rank, mp->count);
+        ctx->launches++;
+    }
+    SPHX_TRY(D == 2 ? configuration_update<2>(mp, false) : configuration_update<3>(mp, false));
     return SPHX_OK;
 }
 } // namespace
@@ -850,6 +967,125 @@ extern "C" int sphx_mp_create(sphx_relation inner, sphx_relation wall, const sph
     if ((st = import_fluid(mp, fb, p->rho0, p->c0)) != SPHX_OK)
         return bail(st);
     if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+        return bail(fail(SPHX_ERR_CUDA, "mixed-precision set-up failed"));
+    *out = mp;
+    return SPHX_OK;
+}
+
+// Periodic viscous flow without walls: the taylor_green.cpp step (DensitySummationInner,
+// ViscousForceInner, TransportVelocityCorrectionInner, Integration1stHalfInnerRiemann,
+// Integration2ndHalf with the given limiter slope -- 0 for NoRiemann --,
+// AdvectionViscousTimeStep, dt = min(acoustic dt, Dt), PeriodicConditionUsingCellLinkedList
+// along every axis) on the mixed-precision layout.  The box must be a cube; its sub-cells
+// tile it exactly (N = floor(L / h) per axis, spacing L / N >= h).
+extern "C" int sphx_mp_create_periodic(sphx_body fb, const sphx_fluid_params *p, const double *lower,
+                                       const double *upper, double viscosity, double tvc_coefficient, sphx_mp *out)
+{
+    if (!fb || !p || !lower || !upper || !out || !(p->h > 0) || !(viscosity >= 0) || !(tvc_coefficient >= 0))
+        return fail(SPHX_ERR_INVALID_ARG, "invalid periodic-flow arguments");
+    const int D = fb->dim;
+    sphx_ctx ctx = fb->ctx;
+    const double L = upper[0] - lower[0];
+    for (int a = 0; a < D; ++a)
+        if (!(upper[a] - lower[a] > 0) || std::abs((upper[a] - lower[a]) - L) > 1e-12 * L)
+            return fail(SPHX_ERR_INVALID_ARG, "the periodic box must be a cube");
+    const int N = int(std::floor(L / p->h));
+    const int max_cells = D == 2 ? CellLanes<2>::max_cells : CellLanes<3>::max_cells;
+    if (N < 2 * kReach + 1 || N > max_cells)
+        return fail(SPHX_ERR_INVALID_ARG, "periodic box of %d sub-cells per axis (needs %d..%d)", N, 2 * kReach + 1,
+                    max_cells);
+    if (fb->n > size_t(kIndexMask) + 1)
+        return fail(SPHX_ERR_INVALID_ARG, "periodic lists index at most %u particles", kIndexMask + 1);
+    SPHX_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::vector<double> mass, vol;
+    for (auto nm : {"Mass", "VolumetricMeasure"})
+    {
+        Field *f = fb->find(nm);
+        if (!f || f->dtype != SPHX_F64)
+            return fail(SPHX_ERR_NOT_FOUND, "variable %s missing", nm);
+        std::vector<double> &v = nm[0] == 'M' ? mass : vol;
+        v.resize(fb->n);
+        if (fb->n)
+            SPHX_CUDA(cudaMemcpy(v.data(), f->dev, fb->n * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    for (size_t i = 0; i < fb->n; ++i)
+        if (mass[i] != mass[0] || vol[i] != vol[0])
+            return fail(SPHX_ERR_INVALID_ARG, "mixed precision needs uniform particle mass and volume");
+    if (fb->n == 0)
+        return fail(SPHX_ERR_INVALID_ARG, "empty fluid body");
+
+    sphx_mesh_desc mesh{};
+    mesh.dim = D;
+    mesh.grid_spacing = L / N;
+    for (int a = 0; a < D; ++a)
+    {
+        mesh.all_cells[a] = N;
+        mesh.lower[a] = lower[a];
+    }
+    sphx_mp mp = new sphx_mp_s();
+    mp->ctx = ctx;
+    ctx->retain();
+    mp->dim = D;
+    mp->n = fb->n;
+    mp->nw = 0;
+    size_t nc = 1;
+    for (int a = 0; a < D; ++a)
+        nc *= size_t(N);
+    mp->ncells = nc;
+    MPConst &k = mp->k;
+    k.m = mesh_dev(mesh);
+    k.periodic = 1;
+    for (int d = 0; d < 3; ++d)
+    {
+        k.gd[d] = 0.0;
+        k.lo[d] = d < D ? lower[d] : 0.0;
+        k.up[d] = d < D ? upper[d] : 0.0;
+    }
+    k.p = make_params(D, mesh.grid_spacing, p->h, p->rho0, p->c0, vol[0], mass[0], p->sigma0, 0.0, 0.0,
+                      p->limiter_slope, k.gd);
+    for (int d = 0; d < 3; ++d)
+        k.p.wrap[d] = d < D ? uint32_t(N) << (d * (D == 2 ? CellLanes<2>::bits : CellLanes<3>::bits)) : 0u;
+    k.p.mu2 = float(2.0 * viscosity);
+    k.p.eps_h = float(0.01 * p->h);
+    k.p.tvc_scale = float(tvc_coefficient * p->h * p->h);
+    k.p.tvc_lim = float(100.0 * p->h * p->h);
+    k.acoustic_cfl = p->acoustic_cfl;
+    k.advection_cfl = p->advection_cfl;
+    // AdvectionViscousTimeStep: reference speed max(U_ref, mu / rho0 / h) (fluid_time_step.cpp:67-74)
+    k.U_ref = std::max(p->U_ref, viscosity / p->rho0 / p->h);
+
+    int st = SPHX_OK;
+    auto bail = [&](int code) {
+        sphx_mp_destroy(mp);
+        return code;
+    };
+    if ((st = alloc_state(mp, mp->a)) != SPHX_OK || (st = alloc_state(mp, mp->b)) != SPHX_OK)
+        return bail(st);
+    size_t n = mp->n;
+    mp->f_offset = mp->alloc<uint32_t>(nc + 1);
+    mp->w_offset = mp->alloc<uint32_t>(1);
+    mp->count = mp->alloc<uint32_t>(nc);
+    mp->key = mp->alloc<uint32_t>(n);
+    mp->rank = mp->alloc<uint32_t>(n);
+    mp->perm = mp->alloc<uint32_t>(n);
+    mp->ncell = mp->alloc<uint32_t>(n);
+    mp->noff = mp->alloc<float>(3 * n);
+    mp->in.count = mp->alloc<uint32_t>(n);
+    mp->wl.count = mp->alloc<uint32_t>(n);
+    mp->slots = mp->alloc<unsigned long long>(8);
+    if (!mp->f_offset || !mp->w_offset || !mp->count || !mp->key || !mp->rank || !mp->perm || !mp->ncell ||
+        !mp->noff || !mp->in.count || !mp->wl.count || !mp->slots)
+        return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "mixed-precision allocation failed"));
+    if (cudaMallocHost(&mp->h_slots, 8 * sizeof(unsigned long long)) != cudaSuccess)
+        return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "pinned allocation failed"));
+    if ((st = alloc_lists(mp, mp->in, D == 2 ? 24 : 96)) != SPHX_OK || (st = alloc_lists(mp, mp->wl, 1)) != SPHX_OK)
+        return bail(st);
+    if (cudaMemsetAsync(mp->wl.count, 0, n * sizeof(uint32_t), ctx->stream) != cudaSuccess ||
+        cudaMemsetAsync(mp->w_offset, 0, sizeof(uint32_t), ctx->stream) != cudaSuccess)
+        return bail(fail(SPHX_ERR_CUDA, "memset failed"));
+    if ((st = import_fluid(mp, fb, p->rho0, p->c0)) != SPHX_OK)
+        return bail(st);
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess)
         return bail(fail(SPHX_ERR_CUDA, "mixed-precision set-up failed"));
     *out = mp;
     return SPHX_OK;
@@ -1069,17 +1305,21 @@ extern "C" int sphx_mp_download(sphx_mp mp, sphx_body fb)
     SPHX_TRY(fb->require("Pressure", SPHX_F64, 1, &p));
     SPHX_TRY(fb->require("Force", SPHX_F64, D, &force));
     SPHX_TRY(fb->require("DensityChangeRate", SPHX_F64, 1, &drho));
+    Field *fp = nullptr;
+    if (mp->k.periodic)
+        SPHX_TRY(fb->require("ForcePrior", SPHX_F64, D, &fp));
+    double *fprior = fp ? static_cast<double *>(fp->dev) : nullptr;
     size_t n = mp->n;
     if (n > 0)
     {
         if (D == 2)
             k_mp_download<2><<<grid_for(n, 256), 256, 0, mp->ctx->stream>>>(
                 n, mp->k, mp->a, (double *)pos->dev, (double *)vel->dev, (double *)rho->dev, (double *)p->dev,
-                (double *)force->dev, (double *)drho->dev);
+                (double *)force->dev, (double *)drho->dev, fprior);
         else
             k_mp_download<3><<<grid_for(n, 256), 256, 0, mp->ctx->stream>>>(
                 n, mp->k, mp->a, (double *)pos->dev, (double *)vel->dev, (double *)rho->dev, (double *)p->dev,
-                (double *)force->dev, (double *)drho->dev);
+                (double *)force->dev, (double *)drho->dev, fprior);
         SPHX_LAUNCHED(mp->ctx);
     }
     SPHX_CUDA(cudaStreamSynchronize(mp->ctx->stream));

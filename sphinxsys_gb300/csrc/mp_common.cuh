@@ -74,6 +74,10 @@ struct MPParams
     float inv_z, zgeo, s_lim;            // acoustic Riemann solver; s_lim = limiter slope / c0
     float g[3];
     double sigma0, c0, h;
+    // periodic flow (sphx_mp_create_periodic): wrap[d] = cells along axis d shifted into
+    // lane d (one period); 2 mu; 0.01 h; transport-velocity scaling and limiter factor
+    uint32_t wrap[3];
+    float mu2, eps_h, tvc_scale, tvc_lim;
 };
 
 // Constants of one fluid body against one static wall (same rounding for every solver).
@@ -114,6 +118,7 @@ struct MPState
     float4 *geo0, *dyn; // {offset at the last configuration update, packed cell}; {velocity, pressure}
     float *off, *force, *drho, *drho_dt, *drho_sum;
     uint32_t *id;
+    float *fprior, *shift; // periodic flow only: prior (viscous) force, transport-velocity shift
 };
 
 struct MPWallData
@@ -593,6 +598,321 @@ __device__ __forceinline__ void build_particle(size_t i, size_t n, const MPParam
     f.drho_sum[i] = float(dsig) * k.rho0_over_sigma0 + wsig.value() * k.wall_factor;
 }
 
+// ---------------------------------------------------------------- periodic flow
+// A periodic box is tiled by the sub-cells exactly (cell count per axis N_d >= 2 kReach + 1,
+// spacing >= h), so the (2 kReach + 1)^D window of a particle wraps around the box and
+// visits every sub-cell at most once.  A neighbour found through a wrapped cell is the
+// image x_j + s L (s = -1 past the upper face, +1 past the lower one, per axis); its list
+// entry carries s in two bits per axis above the particle index, and the packed cell
+// difference of the pair gets s N_d added in lane d.  The sum stays exact modulo 2^32
+// because every final lane value lies in [0, 2 kCellBias].
+constexpr int kCodeShift = 26;
+constexpr uint32_t kIndexMask = (1u << kCodeShift) - 1u;
+
+template <int D>
+__device__ __forceinline__ uint32_t wrap_corr(const MPParams &k, uint32_t e)
+{
+    uint32_t c = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        int s = int(e << (4 - 2 * d)) >> 30; // signed two-bit field of axis d
+        c += uint32_t(s) * k.wrap[d];
+    }
+    return c;
+}
+
+// Candidates of the wrapped window around sub-cell c: f(j, code) with code the per-axis
+// image shifts (two bits per axis, two's complement) of the cell j was found in.
+template <int D, class F>
+__device__ __forceinline__ void for_each_candidate_periodic(const MeshDev &m, const uint32_t *offset, const int *c,
+                                                            F &&f)
+{
+    const int NL = m.all_cells[D - 1];
+    auto last_axis = [&](uint32_t base, uint32_t code) {
+        const int lo = c[D - 1] - kReach, hi = c[D - 1] + kReach;
+        auto seg = [&](int z0, int z1, int s) {
+            const uint32_t cd = code | ((uint32_t(s) & 3u) << (2 * (D - 1)));
+            const uint32_t b = offset[base + uint32_t(z0)], e = offset[base + uint32_t(z1) + 1];
+            for (uint32_t j = b; j < e; ++j)
+                f(j, cd);
+        };
+        if (lo < 0)
+        {
+            seg(lo + NL, NL - 1, 1);
+            seg(0, hi, 0);
+        }
+        else if (hi >= NL)
+        {
+            seg(lo, NL - 1, 0);
+            seg(0, hi - NL, -1);
+        }
+        else
+            seg(lo, hi, 0);
+    };
+    for (int a = -kReach; a <= kReach; ++a)
+    {
+        int x = c[0] + a;
+        const int sx = x < 0 ? 1 : (x >= m.all_cells[0] ? -1 : 0);
+        x += sx * m.all_cells[0];
+        const uint32_t cx = uint32_t(sx) & 3u;
+        if (D == 2)
+            last_axis(uint32_t(x) * uint32_t(m.all_cells[1]), cx);
+        else
+            for (int b = -kReach; b <= kReach; ++b)
+            {
+                int y = c[1] + b;
+                const int sy = y < 0 ? 1 : (y >= m.all_cells[1] ? -1 : 0);
+                y += sy * m.all_cells[1];
+                last_axis((uint32_t(x) * uint32_t(m.all_cells[1]) + uint32_t(y)) * uint32_t(m.all_cells[2]),
+                          cx | ((uint32_t(sy) & 3u) << 2));
+            }
+    }
+}
+
+// Same visits as the stored periodic lists, by a sweep of the wrapped window.
+template <int D, class Load, class Pair, class Flush>
+__device__ __forceinline__ void cell_sweep_periodic(const MeshDev &m, const uint32_t *offset, const int *ci,
+                                                    const MPParams &k, uint32_t pib, const float *oi, size_t self,
+                                                    const float4 *geo, Load &&load, Pair &&pair, Flush &&flush)
+{
+    int g = 0;
+    for_each_candidate_periodic<D>(m, offset, ci, [&](uint32_t j, uint32_t code) {
+        if (size_t(j) == self && code == 0)
+            return;
+        const uint32_t e = j | (code << kCodeShift);
+        float dx[3];
+        geo_dx<D>(k.gs_f, pib + wrap_corr<D>(k, e), oi, geo[j], dx);
+        if (!(sq<D>(dx) < k.rc_sqr))
+            return;
+        pair(load(e));
+        if (++g == kGroup)
+        {
+            flush();
+            g = 0;
+        }
+    });
+    flush();
+}
+
+struct FirstRecP
+{
+    float4 g;
+    float p;
+    uint32_t corr;
+};
+struct SecondRecP
+{
+    float4 g, v;
+    uint32_t corr;
+};
+
+// 1st half of one particle of a periodic flow without walls (Integration1stHalfInnerRiemann):
+// pressure force, density-rate dissipation, v += (F_prior + F) / m dt, first position
+// half-step.  Returns c0 + |v|.
+template <int D, bool LISTS>
+__device__ __forceinline__ double first_particle_periodic(size_t i, size_t n, const MPParams &k, const MeshDev &m,
+                                                          const uint32_t *f_offset, double dt, const MPState &f,
+                                                          const MPNeighbors &in)
+{
+    const float4 gi = f.geo0[i];
+    const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
+    int ci[3] = {0, 0, 0};
+    if (!LISTS)
+        unpack_cell<D>(__float_as_uint(gi.w), ci);
+    const float oi[3] = {gi.x, gi.y, gi.z};
+    const float4 di = f.dyn[i];
+    const float p_i = di.w;
+    const float rho_i = k.rho0 + f.drho[i];
+    Acc force[3], rdis;
+    auto pair = [&](const FirstRecP &r) {
+        float dx[3];
+        geo_dx<D>(k.gs_f, pib + r.corr, oi, r.g, dx);
+        float r2 = sq<D>(dx);
+        float inv = inv_dist(r2);
+        float dWV = wc2_dWV(k.cW, k.inv_h, r2 * inv);
+        float sc = (p_i + r.p) * (dWV * inv);
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            force[d].add(-sc * dx[d]);
+        rdis.add((p_i - r.p) * dWV);
+    };
+    auto flush = [&]() {
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            force[d].flush();
+        rdis.flush();
+    };
+    auto load = [&](uint32_t e) {
+        const uint32_t j = e & kIndexMask;
+        return FirstRecP{__ldg(&f.geo0[j]), __ldg(&f.dyn[j].w), wrap_corr<D>(k, e)};
+    };
+    if (LISTS)
+        list_sweep<true>(i, n, in, load, pair, flush);
+    else
+        cell_sweep_periodic<D>(m, f_offset, ci, k, pib, oi, i, f.geo0, load, pair, flush);
+
+    f.drho_dt[i] = (rdis.value() * k.inv_z) * rho_i;
+    float v2 = 0.f;
+    float vn[3] = {di.x, di.y, di.z};
+    const float dt_f = float(dt);
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        float F = f.force[d * n + i] + force[d].value() * k.Vol;
+        f.force[d * n + i] = F;
+        float vo = vn[d];
+        f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vo));
+        vn[d] = vo + (f.fprior[d * n + i] + F) * k.inv_mass * dt_f;
+        v2 += vn[d] * vn[d];
+    }
+    f.dyn[i] = make_float4(vn[0], vn[1], D == 3 ? vn[2] : 0.f, p_i);
+    return k.c0 + double(sqrtf(v2));
+}
+
+// 2nd half of one particle of a periodic flow (Integration2ndHalfInnerRiemann, or
+// ...NoRiemann with limiter slope 0).  Returns max(|v|^2, 4 h |F + F_prior| / m).
+template <int D, bool LISTS>
+__device__ __forceinline__ double second_particle_periodic(size_t i, size_t n, const MPParams &k, const MeshDev &m,
+                                                           const uint32_t *f_offset, double dt, const MPState &f,
+                                                           const MPNeighbors &in)
+{
+    const float4 gi = f.geo0[i];
+    const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
+    int ci[3] = {0, 0, 0};
+    if (!LISTS)
+        unpack_cell<D>(__float_as_uint(gi.w), ci);
+    const float oi[3] = {gi.x, gi.y, gi.z};
+    const float4 di = f.dyn[i];
+    const float vi[3] = {di.x, di.y, di.z};
+    const float rho_i = k.rho0 + f.drho[i];
+    Acc rate, pdis[3];
+    auto pair = [&](const SecondRecP &r) {
+        float dx[3];
+        geo_dx<D>(k.gs_f, pib + r.corr, oi, r.g, dx);
+        float r2 = sq<D>(dx);
+        float inv = inv_dist(r2);
+        float dWV = wc2_dWV(k.cW, k.inv_h, r2 * inv);
+        const float dv[3] = {vi[0] - r.v.x, vi[1] - r.v.y, vi[2] - r.v.z};
+        float u = dot<D>(dv, dx) * inv;
+        rate.add(u * dWV);
+        float sc = p_jump(k, u) * (dWV * inv);
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            pdis[d].add(sc * dx[d]);
+    };
+    auto flush = [&]() {
+        rate.flush();
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            pdis[d].flush();
+    };
+    auto load = [&](uint32_t e) {
+        const uint32_t j = e & kIndexMask;
+        return SecondRecP{__ldg(&f.geo0[j]), __ldg(&f.dyn[j]), wrap_corr<D>(k, e)};
+    };
+    if (LISTS)
+        list_sweep<false>(i, n, in, load, pair, flush);
+    else
+        cell_sweep_periodic<D>(m, f_offset, ci, k, pib, oi, i, f.geo0, load, pair, flush);
+
+    float drho_dt = f.drho_dt[i] + rate.value() * rho_i;
+    f.drho_dt[i] = drho_dt;
+    f.drho[i] = f.drho[i] + drho_dt * float(0.5 * dt);
+    float v2 = 0.f, a2 = 0.f;
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        float F = pdis[d].value() * k.Vol;
+        f.force[d * n + i] = F;
+        f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vi[d]));
+        v2 += vi[d] * vi[d];
+        float ft = F + f.fprior[d * n + i];
+        a2 += ft * ft;
+    }
+    return double(fmaxf(v2, 4.0f * float(k.h) * sqrtf(a2) * k.inv_mass));
+}
+
+// Configuration of one particle of a periodic flow, with the interactions that use only
+// the configuration and the velocity of the step start, in the reference's order:
+// DensitySummationInner (sum only; rho = rho_sum is set at the step start),
+// ViscousForceInner (fixed viscosity; ForcePrior = the viscous force, the only prior
+// force of the flow), TransportVelocityCorrectionInner (the position shift, applied at the
+// step start so that a repeated build after a list regrowth does not apply it twice).
+template <int D>
+__device__ __forceinline__ void build_particle_periodic(size_t i, size_t n, const MPParams &k, const MeshDev &m,
+                                                        const uint32_t *f_offset, const MPState &f,
+                                                        const MPNeighbors &in, unsigned int *max_counts)
+{
+    const float4 gi = f.geo0[i];
+    const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
+    int ci[3] = {0, 0, 0};
+    unpack_cell<D>(__float_as_uint(gi.w), ci);
+    const float oi[3] = {gi.x, gi.y, gi.z};
+    const float4 di = f.dyn[i];
+    const float vi[3] = {di.x, di.y, di.z};
+    Kahan sigma;
+    Acc visc[3], tvc[3];
+    unsigned cnt = 0;
+    int g = 0;
+    for_each_candidate_periodic<D>(m, f_offset, ci, [&](uint32_t j, uint32_t code) {
+        if (j == uint32_t(i) && code == 0)
+            return;
+        const uint32_t e = j | (code << kCodeShift);
+        float dx[3];
+        geo_dx<D>(k.gs_f, pib + wrap_corr<D>(k, e), oi, f.geo0[j], dx);
+        float r2 = sq<D>(dx);
+        if (!(r2 < k.rc_sqr))
+            return;
+        if (cnt < in.cap)
+            in.J[size_t(cnt) * n + i] = e;
+        ++cnt;
+        float inv = inv_dist(r2);
+        float r = r2 * inv;
+        sigma.add(wc2_W(k.fW, k.inv_h, r));
+        float dWV = wc2_dWV(k.cW, k.inv_h, r);
+        const float4 vj = __ldg(&f.dyn[j]);
+        const float dv[3] = {vi[0] - vj.x, vi[1] - vj.y, vi[2] - vj.z};
+        // e_ij . (B_i + B_j) e_ij = 2 without kernel correction
+        float cv = k.mu2 * dWV / (r + k.eps_h);
+        float ct = dWV * inv;
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+        {
+            visc[d].add(cv * dv[d]);
+            tvc[d].add(ct * dx[d]);
+        }
+        if (++g == kGroup)
+        {
+#pragma unroll
+            for (int d = 0; d < D; ++d)
+            {
+                visc[d].flush();
+                tvc[d].flush();
+            }
+            g = 0;
+        }
+    });
+    in.count[i] = cnt;
+    atomicMax(&max_counts[0], cnt);
+    double dsig = (double(sigma.s) - k.sigma0) - double(sigma.c) + double(k.fW);
+    f.drho_sum[i] = float(dsig) * k.rho0_over_sigma0;
+    float inc[3] = {0.f, 0.f, 0.f}, inc2 = 0.f;
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        visc[d].flush();
+        tvc[d].flush();
+        f.fprior[d * n + i] = visc[d].value() * k.Vol;
+        inc[d] = -2.0f * tvc[d].value();
+        inc2 += inc[d] * inc[d];
+    }
+    const float lim = fminf(k.tvc_lim * inc2, 1.0f);
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        f.shift[d * n + i] = k.tvc_scale * lim * inc[d];
+}
+
 // Acoustic and advection maxima of the initial state (FP64).
 template <int D>
 __device__ __forceinline__ void initial_max(size_t i, size_t n, const MPParams &k, const double *gd, const MPState &f,
@@ -605,7 +925,7 @@ __device__ __forceinline__ void initial_max(size_t i, size_t n, const MPParams &
     for (int d = 0; d < D; ++d)
     {
         v2 += double(vv[d]) * double(vv[d]);
-        double ft = double(f.force[d * n + i]) + double(k.mass) * gd[d];
+        double ft = double(f.force[d * n + i]) + (f.fprior ? double(f.fprior[d * n + i]) : double(k.mass) * gd[d]);
         a2 += ft * ft;
     }
     *vm = k.c0 + sqrt(v2);

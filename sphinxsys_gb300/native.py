@@ -97,6 +97,7 @@ SIGNATURES = {
     "sphx_ck_advection_time_step": (_i, [_vp, C.POINTER(FluidParams), _pd]),
     "sphx_ck_observe_quantity": (_i, [_vp, C.c_char_p, _pd]),
     "sphx_mp_create": (_i, [_vp, _vp, C.POINTER(FluidParams), _pd, _pvp]),
+    "sphx_mp_create_periodic": (_i, [_vp, C.POINTER(FluidParams), _pd, _pd, C.c_double, C.c_double, _pvp]),
     "sphx_mp_destroy": (_i, [_vp]),
     "sphx_mp_advection_step": (_i, [_vp, _i, C.POINTER(C.c_int), _pd, _pd]),
     "sphx_mp_download": (_i, [_vp, _vp]),

@@ -90,3 +90,93 @@ class TaylorGreen:
             p.update_cell_linked_list_.exec()
         self.water_block_inner.updateConfiguration()
         return sub, Dt
+
+
+class MixedPrecisionTaylorGreen:
+    """The same periodic flow advanced by the mixed-precision solver
+    (sphx_mp_create_periodic): the FP64 body holds the initial lattice state only (no FP64
+    cell list or relation is built, so the case can be as large as the solver's own
+    memory allows); ``download`` writes the solver state into it."""
+
+    def __init__(self, case: TaylorGreenCase, device: int = 0, block: int = 128, strategy: int = 0):
+        import ctypes as C
+        from . import native as N
+        self._C, self._N = C, N
+        d = case.dim
+        self.case = case
+        lo, up = [0.0] * d, [case.L] * d
+        self.sph_system = S.SPHSystem(lo, up, case.dp, device=device, h_spacing_ratio=case.h_ratio)
+        self.water_block = S.FluidBody(self.sph_system, None, name="WaterBody")
+        self.water_block.defineMatterMaterial(S.WeaklyCompressibleFluid(case.rho0, case.c0))
+        S.addMaterialProperty(self.water_block, S.Viscosity(case.mu))
+        x = S.lattice_positions(d, lo, up, case.dp, _Box(d, case.L))
+        self.water_block.generateParticles(positions=x)
+        self.water_block.upload("Velocity", initial_velocity(case, x))
+        del x
+        params = S.fluid_params(self.water_block, U_ref=case.U)
+        params.limiter_slope = 0.0  # Integration2ndHalfInnerNoRiemann
+        self._params = params
+        l3, u3 = np.zeros(3), np.zeros(3)
+        u3[:d] = case.L
+        h = C.c_void_p()
+        N.call("sphx_mp_create_periodic", self.water_block.handle, C.byref(params),
+               l3.ctypes.data_as(C.POINTER(C.c_double)), u3.ctypes.data_as(C.POINTER(C.c_double)), case.mu, 0.2,
+               C.byref(h))
+        self.handle = h
+        N.call("sphx_mp_set_tuning", h, int(block), int(strategy))
+        self.physical_time = 0.0
+        self.number_of_iterations = 0
+        self.total_substeps = 0
+
+    @property
+    def n_fluid(self) -> int:
+        return self.water_block.n
+
+    def set_tuning(self, block: int, strategy: int) -> None:
+        self._N.call("sphx_mp_set_tuning", self.handle, int(block), int(strategy))
+
+    def autotune(self, reps: int = 3):
+        C = self._C
+        b, st, ms = C.c_int(), C.c_int(), C.c_double()
+        self._N.call("sphx_mp_autotune", self.handle, int(reps), C.byref(b), C.byref(st), C.byref(ms))
+        return b.value, st.value, ms.value
+
+    def set_profiling(self, on: bool) -> None:
+        self._N.call("sphx_mp_set_profiling", self.handle, int(on))
+
+    def kernel_times(self):
+        out = np.zeros(4)
+        self._N.call("sphx_mp_kernel_times", self.handle, out.ctypes.data_as(self._C.POINTER(self._C.c_double)))
+        return out[0] / max(out[1], 1), out[2] / max(out[3], 1), int(out[1])
+
+    def list_sizes(self):
+        out = np.zeros(6, dtype=np.uint64)
+        self._N.call("sphx_mp_list_sizes", self.handle, out.ctypes.data_as(self._C.POINTER(self._C.c_uint64)))
+        return dict(n=int(out[0]), nnz_inner=int(out[2]), cap_inner=int(out[4]))
+
+    def advection_step(self):
+        C, N = self._C, self._N
+        sub, Dt, t = C.c_int(), C.c_double(), C.c_double()
+        N.call("sphx_mp_advection_step", self.handle, 0, C.byref(sub), C.byref(Dt), C.byref(t))
+        self.physical_time = t.value
+        self.number_of_iterations += 1
+        self.total_substeps += sub.value
+        return sub.value, Dt.value
+
+    def kinetic_energy(self) -> float:
+        out = np.zeros(5)
+        self._N.call("sphx_mp_conservation", self.handle, out.ctypes.data_as(self._C.POINTER(self._C.c_double)))
+        return float(out[4])
+
+    def download(self) -> None:
+        self._N.call("sphx_mp_download", self.handle, self.water_block.handle)
+
+    def maximum_speed(self) -> float:
+        self.download()
+        v = self.water_block.download("Velocity")
+        return float(np.sqrt(np.max(np.sum(v * v, axis=1))))
+
+    def __del__(self):
+        if getattr(self, "handle", None) is not None and self._N._lib is not None:
+            self._N._lib.sphx_mp_destroy(self.handle)
+            self.handle = None

@@ -3,12 +3,15 @@ CUDA execution policy against the oracle, and the reference's regression rule on
 
 Tolerance: FP64 fields within 1e-10 relative (max |gpu - oracle| / max |oracle|) after
 several advection steps: the device sums neighbours in the same order as the oracle but
-fuses multiply-adds, so the two agree to a few ulp per step."""
+fuses multiply-adds, so the two agree to a few ulp per step.  The mixed-precision solver
+(sphx_mp_create_periodic) against the FP64 GPU run: velocity within 1e-4 relative,
+positions within 1e-6 of the box size, kinetic energy within 1e-5 relative after 20
+advection steps."""
 import numpy as np
 import pytest
 
 from sphinxsys_gb300 import cases, regression
-from sphinxsys_gb300.taylor_green import TaylorGreen
+from sphinxsys_gb300.taylor_green import MixedPrecisionTaylorGreen, TaylorGreen
 
 from oracle import oracle as O
 
@@ -70,6 +73,80 @@ def test_gpu_taylor_green_passes_reference_dtw_regression(golden):
             integ += g.physical_time - t0
         ke.append(g.kinetic_energy.exec())
         ms.append(g.maximum_speed.exec())
+    for q, cur in (("WaterBody_TotalKineticEnergy", ke), ("WaterBody_MaximumSpeed", ms)):
+        runs = [golden[k] for k in golden.files if k.startswith(f"taylor_green2d/{q}/Run_")]
+        ok, d = regression.passes(runs, cur, golden[f"taylor_green2d/{q}/dtw"])
+        assert ok, (q, d)
+
+
+def small_2d():
+    return cases.taylor_green_2d(50)
+
+
+@pytest.mark.parametrize("case", [small_2d(), small_3d()], ids=lambda c: c.name)
+def test_mixed_precision_taylor_green_tracks_fp64(case):
+    ref = TaylorGreen(case)
+    mp = MixedPrecisionTaylorGreen(case)
+    assert abs(mp.kinetic_energy() / ref.kinetic_energy.exec() - 1) < 1e-6
+    for step in range(20):
+        s_r, dt_r = ref.advection_step()
+        s_m, dt_m = mp.advection_step()
+        assert abs(s_r - s_m) <= 1, step
+        assert abs(dt_m / dt_r - 1) < 1e-5, step
+    mp.download()
+    errs = {}
+    for name in ("Velocity", "Density", "ForcePrior"):
+        errs[name] = rel_err(mp.water_block.download(name), ref.water_block.download(name))
+    d = mp.water_block.download("Position") - ref.water_block.download("Position")
+    d = (d + 0.5 * case.L) % case.L - 0.5 * case.L  # the same particle may sit on either side of a face
+    errs["Position"] = float(np.max(np.abs(d)) / case.L)
+    errs["KineticEnergy"] = abs(mp.kinetic_energy() / ref.kinetic_energy.exec() - 1)
+    print(case.name, errs)
+    assert errs["Velocity"] < 1e-4, errs
+    assert errs["Density"] < 1e-6, errs
+    assert errs["ForcePrior"] < 1e-3, errs
+    assert errs["Position"] < 1e-6, errs
+    assert errs["KineticEnergy"] < 1e-5, errs
+
+
+def test_mixed_precision_taylor_green_strategies_bitwise_equal():
+    case = small_3d()
+    outs = []
+    for block, strategy in ((128, 0), (64, 0), (256, 1), (96, 1)):
+        mp = MixedPrecisionTaylorGreen(case, block=block, strategy=strategy)
+        for _ in range(5):
+            mp.advection_step()
+        mp.download()
+        outs.append([mp.water_block.download(n) for n in ("Position", "Velocity", "Density")])
+    for other in outs[1:]:
+        for a, b in zip(outs[0], other):
+            assert np.array_equal(a, b)
+
+
+def test_mixed_precision_taylor_green_3d_early_decay_is_viscous():
+    """The 3D vortex at 32^3 to t = 0.5: kinetic energy follows exp(-6 nu t) (the decay
+    of the linearised flow, |k|^2 = 3) within 2 %, as the FP64 oracle does at this
+    resolution."""
+    case = cases.TaylorGreenCase("taylor_green3d_32", 3, 2.0 * np.pi, 2.0 * np.pi / 32, 1)
+    mp = MixedPrecisionTaylorGreen(case)
+    ke0, nu = mp.kinetic_energy(), case.mu / case.rho0
+    while mp.physical_time < 0.5:
+        mp.advection_step()
+        ratio = mp.kinetic_energy() / ke0
+        assert abs(ratio / np.exp(-6.0 * nu * mp.physical_time) - 1) < 0.02, (mp.physical_time, ratio)
+
+
+def test_mixed_precision_taylor_green_passes_reference_dtw_regression(golden):
+    g = MixedPrecisionTaylorGreen(cases.taylor_green_2d())
+    ke, ms = [g.kinetic_energy()], []
+    while g.physical_time < 5.0:
+        integ = 0.0
+        while integ < 0.1:
+            t0 = g.physical_time
+            g.advection_step()
+            integ += g.physical_time - t0
+        ke.append(g.kinetic_energy())
+        ms.append(g.maximum_speed())
     for q, cur in (("WaterBody_TotalKineticEnergy", ke), ("WaterBody_MaximumSpeed", ms)):
         runs = [golden[k] for k in golden.files if k.startswith(f"taylor_green2d/{q}/Run_")]
         ok, d = regression.passes(runs, cur, golden[f"taylor_green2d/{q}/dtw"])
