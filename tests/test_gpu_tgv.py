@@ -4,9 +4,9 @@ CUDA execution policy against the oracle, and the reference's regression rule on
 Tolerance: FP64 fields within 1e-10 relative (max |gpu - oracle| / max |oracle|) after
 several advection steps: the device sums neighbours in the same order as the oracle but
 fuses multiply-adds, so the two agree to a few ulp per step.  The mixed-precision solver
-(sphx_mp_create_periodic) against the FP64 GPU run: velocity within 1e-4 relative,
-positions within 1e-6 of the box size, kinetic energy within 1e-5 relative after 20
-advection steps."""
+(sphx_mp_create_periodic) against the FP64 GPU run: velocity within 1e-5 relative and
+positions within 1e-6 of the box size after 10 advection steps, kinetic energy within
+1e-5 relative after 20."""
 import numpy as np
 import pytest
 
@@ -85,28 +85,45 @@ def small_2d():
 
 @pytest.mark.parametrize("case", [small_2d(), small_3d()], ids=lambda c: c.name)
 def test_mixed_precision_taylor_green_tracks_fp64(case):
+    """Pointwise agreement for 10 advection steps, then norms to 20 steps.
+
+    From about the 12th step of the 2D vortex at 50 x 50 the particles near the hyperbolic
+    stagnation points amplify any rounding difference about threefold per advection step:
+    the FP64 GPU run and the FP64 oracle (equal to ~1e-16 per step) grow apart from 3e-14
+    at step 12 to 1.5e-10 at step 23 in the same way.  The mixed-precision run starts
+    from ~1e-7 differences, so the pointwise comparison stops at step 10 and the later
+    steps are checked through the kinetic energy and the RMS velocity difference."""
     ref = TaylorGreen(case)
     mp = MixedPrecisionTaylorGreen(case)
     assert abs(mp.kinetic_energy() / ref.kinetic_energy.exec() - 1) < 1e-6
+    # the viscous force of the initial state (the solver computes it in its first build)
+    probe = TaylorGreen(case)
+    probe.update_density_by_summation.exec()
+    probe.viscous_force.exec()
+    mp.download()
+    assert rel_err(mp.water_block.download("ForcePrior"), probe.water_block.download("ForcePrior")) < 1e-4
     for step in range(20):
         s_r, dt_r = ref.advection_step()
         s_m, dt_m = mp.advection_step()
         assert abs(s_r - s_m) <= 1, step
         assert abs(dt_m / dt_r - 1) < 1e-5, step
+        if step == 9:
+            mp.download()
+            errs = {n: rel_err(mp.water_block.download(n), ref.water_block.download(n))
+                    for n in ("Velocity", "Density")}
+            d = mp.water_block.download("Position") - ref.water_block.download("Position")
+            d = (d + 0.5 * case.L) % case.L - 0.5 * case.L  # a particle may sit on either side of a face
+            errs["Position"] = float(np.max(np.abs(d)) / case.L)
+            print(case.name, errs)
+            assert errs["Velocity"] < 1e-5, errs
+            assert errs["Density"] < 1e-6, errs
+            assert errs["Position"] < 1e-6, errs
     mp.download()
-    errs = {}
-    for name in ("Velocity", "Density", "ForcePrior"):
-        errs[name] = rel_err(mp.water_block.download(name), ref.water_block.download(name))
-    d = mp.water_block.download("Position") - ref.water_block.download("Position")
-    d = (d + 0.5 * case.L) % case.L - 0.5 * case.L  # the same particle may sit on either side of a face
-    errs["Position"] = float(np.max(np.abs(d)) / case.L)
-    errs["KineticEnergy"] = abs(mp.kinetic_energy() / ref.kinetic_energy.exec() - 1)
-    print(case.name, errs)
-    assert errs["Velocity"] < 1e-4, errs
-    assert errs["Density"] < 1e-6, errs
-    assert errs["ForcePrior"] < 1e-3, errs
-    assert errs["Position"] < 1e-6, errs
-    assert errs["KineticEnergy"] < 1e-5, errs
+    vm, vr = mp.water_block.download("Velocity"), ref.water_block.download("Velocity")
+    rms = np.sqrt(np.mean(np.sum((vm - vr) ** 2, axis=1)) / np.mean(np.sum(vr * vr, axis=1)))
+    ke = abs(mp.kinetic_energy() / ref.kinetic_energy.exec() - 1)
+    print(case.name, "rms", rms, "ke", ke)
+    assert rms < 1e-3 and ke < 1e-5, (rms, ke)
 
 
 def test_mixed_precision_taylor_green_strategies_bitwise_equal():
