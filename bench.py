@@ -355,6 +355,79 @@ def batch_leg(args, torch, local):
             "speedup_vs_fp64_sequential": value / (fp_ps / fp_el)}
 
 
+def bytes_mp_second_periodic(n_fluid: int, nnz: int) -> int:
+    """Mixed 2nd half of the periodic flow, 3D: per particle read geo0 (16), dyn (16),
+    off (12), drho (4), drho_dt (4), prior force (12), write off (12), drho (4), drho_dt (4),
+    force (12) = 96 B; 4 B per stored neighbour entry."""
+    return 96 * n_fluid + 4 * nnz
+
+
+def taylor_green_leg(args, torch, local):
+    """The 3D periodic Taylor-Green vortex on [0, 2 pi]^3 at args.tg_resolution^3 particles
+    (Re = 100, rho0 = 1, c0 = 10, transport-velocity correction), mixed precision: warm-up
+    and timed advection steps, the kinetic energy after each, its decay against
+    exp(-6 nu t) (the linearised decay, |k|^2 = 3), then the FP64 drop-in on the same case
+    from the same initial state for args.tg_fp64_steps steps (kinetic-energy error of mixed
+    against FP64 at equal step counts, and the FP64 throughput)."""
+    from sphinxsys_gb300 import cases
+    from sphinxsys_gb300.taylor_green import MixedPrecisionTaylorGreen, TaylorGreen
+    case = cases.taylor_green_3d(args.tg_resolution)
+    t0 = time.perf_counter()
+    mp = MixedPrecisionTaylorGreen(case, device=local)
+    setup_s = time.perf_counter() - t0
+    n = mp.n_fluid
+    ctx = mp.water_block.system.ctx
+    nu = case.mu / case.rho0
+    ke = [mp.kinetic_energy()]
+    times = [0.0]
+    tuned = mp.autotune(reps=1) if args.autotune else None
+
+    def step():
+        r = mp.advection_step()
+        return r
+
+    for _ in range(args.warmup):
+        step()
+        ke.append(mp.kinetic_energy())
+        times.append(mp.physical_time)
+    mp.set_profiling(True)
+    el, subs, launches, _ = timed_steps(torch, ctx, step, args.tg_steps, 0)
+    t1, t2, nsweeps = mp.kernel_times()
+    mp.set_profiling(False)
+    ke.append(mp.kinetic_energy())
+    times.append(mp.physical_time)
+    sizes = mp.list_sizes()
+    hbm, src = hbm_peak()
+    alg = bytes_mp_second_periodic(n, sizes["nnz_inner"])
+    achieved = alg / (t2 / 1e3) / 1e9
+    decay = {"t": times[-1], "ke_ratio": ke[-1] / ke[0], "analytic": float(np.exp(-6.0 * nu * times[-1]))}
+    decay["rel_err"] = decay["ke_ratio"] / decay["analytic"] - 1.0
+    total_steps = args.warmup + args.tg_steps
+    del mp
+    fp64 = None
+    if args.tg_fp64_steps > 0:
+        ref = TaylorGreen(case, device=local)
+        ke_fp = [ref.kinetic_energy.exec()]
+        fsteps = min(args.tg_fp64_steps, total_steps)
+        fel, fsubs, _, _ = timed_steps(torch, ref.water_block.system.ctx, ref.advection_step, fsteps, 0)
+        ke_fp.append(ref.kinetic_energy.exec())
+        # the mixed run's energy after the same number of advection steps
+        ke_mp = ke[fsteps] if fsteps <= args.warmup else None
+        fp64 = {"value": n * fsubs / fel, "ms_per_step": 1e3 * fel / fsteps, "steps": fsteps,
+                "ke_rel_err_mixed_vs_fp64": (abs(ke_mp / ke_fp[-1] - 1.0) if ke_mp is not None else None)}
+        del ref
+    return {"workload": case.name, "n_fluid": n, "dtype": "f32 pairs / f64 integration", "value": n * subs / el,
+            "unit": UNIT, "ms_per_step": 1e3 * el / args.tg_steps, "steps": args.tg_steps, "warmup": args.warmup,
+            "acoustic_substeps": subs, "gpu_launches": int(launches), "tuning": tuned, "setup_s": setup_s,
+            "kinetic_energy_decay": decay,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "kernel": "k_mp_second_periodic<3,lists>", "algorithmic_bytes": alg, "kernel_ms": t2,
+                         "first_half_ms": t1, "sweeps_timed": nsweeps, "peak_source": src,
+                         "traffic": traffic_of("k_mp_second_periodic")},
+            "fp64_same_case": fp64,
+            "speedup_vs_fp64": (n * subs / el) / fp64["value"] if fp64 else None}
+
+
 def run_cpu_sample(case, threads: int):
     """One advection step of the oracle (OpenMP FP64 restatement) on the same case."""
     from oracle import oracle as O
@@ -416,6 +489,9 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=5)
     ap.add_argument("--batch-fp64-steps", type=int, default=1)
     ap.add_argument("--batch-fp64-warmup", type=int, default=1)
+    ap.add_argument("--tg-resolution", type=int, default=256, help="Taylor-Green particles per side (0 = skip)")
+    ap.add_argument("--tg-steps", type=int, default=10)
+    ap.add_argument("--tg-fp64-steps", type=int, default=3)
     args = ap.parse_args()
     rank, world, local = dist_info()
 
@@ -442,6 +518,7 @@ def main():
         ps, el = float(t[0]), float(m[0])
     fp64 = None if args.no_fp64 else fp64_leg(args, torch, local)
     batch = batch_leg(args, torch, local) if args.batch_count > 0 else None
+    taylor_green = taylor_green_leg(args, torch, local) if args.tg_resolution > 0 else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -468,6 +545,7 @@ def main():
                                 "errors_vs_fp64": mixed["errors_vs_fp64"], "lists": mixed["lists"]},
             "fp64_drop_in": fp64,
             "batch": batch,
+            "taylor_green": taylor_green,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
