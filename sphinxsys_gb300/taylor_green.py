@@ -180,3 +180,45 @@ class MixedPrecisionTaylorGreen:
         if getattr(self, "handle", None) is not None and self._N._lib is not None:
             self._N._lib.sphx_mp_destroy(self.handle)
             self.handle = None
+
+
+def run(case: TaylorGreenCase, steps: int, precision: str = "mixed", record_every: int = 10, device: int = 0):
+    """Advances the vortex `steps` advection steps and records the kinetic energy every
+    `record_every` steps (and at the start); returns the series with the wall time."""
+    import time
+    sim = MixedPrecisionTaylorGreen(case, device=device) if precision == "mixed" else TaylorGreen(case, device=device)
+    energy = (lambda: sim.kinetic_energy()) if precision == "mixed" else (lambda: sim.kinetic_energy.exec())
+    t, ke, subs = [0.0], [energy()], 0
+    t0 = time.perf_counter()
+    for k in range(1, steps + 1):
+        s, _ = sim.advection_step()
+        subs += s
+        if k % record_every == 0 or k == steps:
+            t.append(sim.physical_time)
+            ke.append(energy())
+    wall = time.perf_counter() - t0
+    return {"workload": case.name, "precision": precision, "n_fluid": sim.water_block.n, "steps": steps,
+            "acoustic_substeps": subs, "wall_s": wall, "t": t, "kinetic_energy": ke}
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+
+    from .cases import taylor_green_2d, taylor_green_3d
+    ap = argparse.ArgumentParser(description="Taylor-Green vortex: kinetic-energy series on the CUDA policy")
+    ap.add_argument("--dim", type=int, default=3)
+    ap.add_argument("--resolution", type=int, default=256)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "both"])
+    ap.add_argument("--record-every", type=int, default=10)
+    ap.add_argument("--out", default=None, help="JSON file for the series (default: stdout)")
+    a = ap.parse_args()
+    c = taylor_green_3d(a.resolution) if a.dim == 3 else taylor_green_2d(a.resolution)
+    res = [run(c, a.steps, p, a.record_every) for p in (("mixed", "fp64") if a.precision == "both" else (a.precision,))]
+    text = json.dumps(res)
+    if a.out:
+        with open(a.out, "w") as f:
+            f.write(text)
+    else:
+        print(text)
