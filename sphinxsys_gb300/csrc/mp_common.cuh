@@ -68,6 +68,7 @@ __host__ __device__ __forceinline__ void unpack_cell(uint32_t p, int *c)
 struct MPParams
 {
     float gs_f, rc_sqr, inv_h, fW;
+    float rc_reach; // search reach: cut-off x (1 + 1e-4)
     float cW, cWw; // Wendland dW prefactor x 5/8 x particle volume (fluid, wall)
     float rho0, p0_over_rho0, Vol, mass, inv_mass;
     float rho0_over_sigma0, wall_factor; // wall_factor = rho0^2 m_w / (sigma0 m rho0_w)
@@ -89,6 +90,7 @@ inline MPParams make_params(int dim, double grid_spacing, double h, double rho0,
     MPParams k{};
     k.gs_f = float(grid_spacing);
     k.rc_sqr = float(wk.rc_sqr);
+    k.rc_reach = float(std::sqrt(wk.rc_sqr) * (1.0 + 1e-4));
     k.inv_h = float(wk.inv_h);
     k.fW = float(wk.factor_W);
     k.cW = float(wk.factor_dW * 0.625 * vol);
@@ -113,18 +115,35 @@ inline MPParams make_params(int dim, double grid_spacing, double h, double rho0,
     return k;
 }
 
+// A particle's neighbour record is 32 bytes, {geo0, dyn}: geo0 = {offset at the last
+// configuration update (x, y, z), packed cell}, dyn = {velocity, pressure}.  Both sweeps
+// read the whole record of a neighbour with one 256-bit load.
 struct MPState
 {
-    float4 *geo0, *dyn; // {offset at the last configuration update, packed cell}; {velocity, pressure}
+    float4 *rec; // 2 float4 per particle, 32-byte aligned
     float *off, *force, *drho, *drho_dt, *drho_sum;
     uint32_t *id;
     float *fprior, *shift; // periodic flow only: prior (viscous) force, transport-velocity shift
+    __device__ __forceinline__ float4 &geo0(size_t i) const { return rec[2 * i]; }
+    __device__ __forceinline__ float4 &dyn(size_t i) const { return rec[2 * i + 1]; }
 };
 
+// Wall record, 32 bytes: {offset, packed cell}, {normal, 0}.
 struct MPWallData
 {
-    float4 *geo, *n;
+    float4 *rec;
+    __device__ __forceinline__ float4 &geo(size_t i) const { return rec[2 * i]; }
+    __device__ __forceinline__ float4 &n(size_t i) const { return rec[2 * i + 1]; }
 };
+
+// One 256-bit read-only load of record j (ld.global.nc.v8.f32, 32-byte aligned).
+__device__ __forceinline__ void load_rec(const float4 *rec, uint32_t j, float4 &a, float4 &b)
+{
+    const float4 *p = rec + 2 * size_t(j);
+    asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+                 : "l"(p));
+}
 
 struct MPNeighbors
 {
@@ -234,19 +253,50 @@ __device__ __forceinline__ float p_jump(const MPParams &k, float u)
     return k.zgeo * u * fminf(k.s_lim * fmaxf(u, 0.0f), 1.0f);
 }
 
-// Candidates of the (2 kReach + 1)^D sub-cells around sub-cell c; the cells of one
+// The window is pruned to the sub-cells that can hold a neighbour: for a particle at
+// offset o in its sub-cell, the slab of sub-cell c + a along an axis lies a gs - o above
+// it (a > 0) or o + (|a| - 1) gs below it (a < 0).  Columns whose gap in the leading axes
+// reaches r are skipped, and the run along the last axis is cut to the sub-cells closer
+// than sqrt(r^2 - gap^2).  r is the cut-off enlarged by 1e-4 relative, far above the
+// rounding of the offsets, so every candidate the membership test accepts is visited;
+// the order of the visited candidates is the unpruned order.
+struct Reach
+{
+    const float *o; // offsets of the particle in its sub-cell
+    float gs, r;    // sub-cell spacing, reach radius
+};
+
+__device__ __forceinline__ float slab_gap(float o, float gs, int a)
+{
+    return a > 0 ? float(a) * gs - o : (a < 0 ? o + float(-a - 1) * gs : 0.0f);
+}
+
+// Sub-cells c + a, -lo <= a <= hi, closer than r along one axis.
+__device__ __forceinline__ void axis_reach(float o, float gs, float r, int &lo, int &hi)
+{
+    hi = max(0, min(kReach, int(ceilf((r + o) / gs)) - 1));
+    lo = max(0, min(kReach, int(ceilf((r - o) / gs))));
+}
+
+// Candidates of the pruned (2 kReach + 1)^D window around sub-cell c; the cells of one
 // instance start at cell_base (columns along the last axis are contiguous in the linear
 // cell order).
 template <int D, class F>
 __device__ __forceinline__ void for_each_candidate(const MeshDev &m, uint32_t cell_base, const uint32_t *offset,
-                                                   const int *c, F &&f)
+                                                   const int *c, const Reach &q, F &&f)
 {
-    int lo0 = max(c[0] - kReach, 0), hi0 = min(c[0] + kReach, m.all_cells[0] - 1);
-    int lo1 = max(c[1] - kReach, 0), hi1 = min(c[1] + kReach, m.all_cells[1] - 1);
+    const float r2 = q.r * q.r;
+    int l0, h0;
+    axis_reach(q.o[0], q.gs, q.r, l0, h0);
+    const int lo0 = max(c[0] - l0, 0), hi0 = min(c[0] + h0, m.all_cells[0] - 1);
     if (D == 2)
     {
         for (int x = lo0; x <= hi0; ++x)
         {
+            const float gx = slab_gap(q.o[0], q.gs, x - c[0]);
+            int l1, h1;
+            axis_reach(q.o[1], q.gs, sqrtf(fmaxf(r2 - gx * gx, 0.0f)), l1, h1);
+            const int lo1 = max(c[1] - l1, 0), hi1 = min(c[1] + h1, m.all_cells[1] - 1);
             uint32_t a = cell_base + uint32_t(x) * uint32_t(m.all_cells[1]);
             uint32_t b = offset[a + uint32_t(lo1)], e = offset[a + uint32_t(hi1) + 1];
             for (uint32_t j = b; j < e; ++j)
@@ -255,16 +305,28 @@ __device__ __forceinline__ void for_each_candidate(const MeshDev &m, uint32_t ce
     }
     else
     {
-        int lo2 = max(c[2] - kReach, 0), hi2 = min(c[2] + kReach, m.all_cells[2] - 1);
+        int l1, h1;
+        axis_reach(q.o[1], q.gs, q.r, l1, h1);
+        const int lo1 = max(c[1] - l1, 0), hi1 = min(c[1] + h1, m.all_cells[1] - 1);
         for (int x = lo0; x <= hi0; ++x)
+        {
+            const float gx = slab_gap(q.o[0], q.gs, x - c[0]);
             for (int y = lo1; y <= hi1; ++y)
             {
+                const float gy = slab_gap(q.o[1], q.gs, y - c[1]);
+                const float g2 = gx * gx + gy * gy;
+                if (!(g2 < r2))
+                    continue;
+                int l2, h2;
+                axis_reach(q.o[2], q.gs, sqrtf(r2 - g2), l2, h2);
+                const int lo2 = max(c[2] - l2, 0), hi2 = min(c[2] + h2, m.all_cells[2] - 1);
                 uint32_t a = cell_base +
                              (uint32_t(x) * uint32_t(m.all_cells[1]) + uint32_t(y)) * uint32_t(m.all_cells[2]);
                 uint32_t b = offset[a + uint32_t(lo2)], e = offset[a + uint32_t(hi2) + 1];
                 for (uint32_t j = b; j < e; ++j)
                     f(j);
             }
+        }
     }
 }
 
@@ -339,15 +401,15 @@ __device__ __forceinline__ void list_sweep(size_t i, size_t n, const MPNeighbors
 // Same visits by cell sweep: accepts the candidates the build accepted.
 template <int D, class Load, class Pair, class Flush>
 __device__ __forceinline__ void cell_sweep(const Visit &v, const uint32_t *offset, const int *ci, float gs, uint32_t pib,
-                                           const float *oi, float rc_sqr, size_t self, const float4 *geo, Load &&load,
-                                           Pair &&pair, Flush &&flush)
+                                           const float *oi, float rc_sqr, float rc_reach, size_t self,
+                                           const float4 *geo, Load &&load, Pair &&pair, Flush &&flush)
 {
     int g = 0;
-    for_each_candidate<D>(v.m, v.cell_base, offset, ci, [&](uint32_t j) {
+    for_each_candidate<D>(v.m, v.cell_base, offset, ci, Reach{oi, gs, rc_reach}, [&](uint32_t j) {
         if (size_t(j) == self)
             return;
         float dx[3];
-        geo_dx<D>(gs, pib, oi, geo[j], dx);
+        geo_dx<D>(gs, pib, oi, geo[2 * size_t(j)], dx);
         if (!(sq<D>(dx) < rc_sqr))
             return;
         pair(load(j));
@@ -378,13 +440,13 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
                                                  const MPState &f, const MPWallData &w, const MPNeighbors &in,
                                                  const MPNeighbors &wl)
 {
-    const float4 gi = f.geo0[i];
+    const float4 gi = f.geo0(i);
     const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
     int ci[3] = {0, 0, 0};
     if (!LISTS)
         unpack_cell<D>(__float_as_uint(gi.w), ci);
     const float oi[3] = {gi.x, gi.y, gi.z};
-    const float4 di = f.dyn[i];
+    const float4 di = f.dyn(i);
     const float p_i = di.w;
     const float rho_i = k.rho0 + f.drho[i];
     Acc force[3], rdis;
@@ -406,11 +468,15 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
             force[d].flush();
         rdis.flush();
     };
-    auto load = [&](uint32_t j) { return FirstRec{__ldg(&f.geo0[j]), __ldg(&f.dyn[j].w)}; };
+    auto load = [&](uint32_t j) {
+        float4 g, d;
+        load_rec(f.rec, j, g, d);
+        return FirstRec{g, d.w};
+    };
     if (LISTS)
         list_sweep<true>(i, n, in, load, pair, flush);
     else
-        cell_sweep<D>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, i, f.geo0, load, pair, flush);
+        cell_sweep<D>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, i, f.rec, load, pair, flush);
 
     Acc wforce[3], wrdis;
     auto wpair = [&](const float4 &gj) {
@@ -433,11 +499,12 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
             wforce[d].flush();
         wrdis.flush();
     };
-    auto wload = [&](uint32_t j) { return __ldg(&w.geo[j]); };
+    auto wload = [&](uint32_t j) { return __ldg(&w.geo(j)); };
     if (LISTS)
         list_sweep<true>(i, n, wl, wload, wpair, wflush);
     else
-        cell_sweep<D>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, ~size_t(0), w.geo, wload, wpair, wflush);
+        cell_sweep<D>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, ~size_t(0), w.rec, wload, wpair,
+                      wflush);
 
     f.drho_dt[i] = (rdis.value() * k.inv_z) * rho_i + (wrdis.value() * k.inv_z) * rho_i;
     float v2 = 0.f;
@@ -455,7 +522,7 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
         v2 += vn[d] * vn[d];
     }
     // the pressure stays the one the neighbours of this sweep read
-    f.dyn[i] = make_float4(vn[0], vn[1], D == 3 ? vn[2] : 0.f, p_i);
+    f.dyn(i) = make_float4(vn[0], vn[1], D == 3 ? vn[2] : 0.f, p_i);
     return k.c0 + double(sqrtf(v2));
 }
 
@@ -467,13 +534,13 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
                                                   const MPState &f, const MPWallData &w, const MPNeighbors &in,
                                                   const MPNeighbors &wl)
 {
-    const float4 gi = f.geo0[i];
+    const float4 gi = f.geo0(i);
     const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
     int ci[3] = {0, 0, 0};
     if (!LISTS)
         unpack_cell<D>(__float_as_uint(gi.w), ci);
     const float oi[3] = {gi.x, gi.y, gi.z};
-    const float4 di = f.dyn[i];
+    const float4 di = f.dyn(i);
     const float vi[3] = {di.x, di.y, di.z};
     const float rho_i = k.rho0 + f.drho[i];
     Acc rate, pdis[3];
@@ -497,11 +564,15 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
         for (int d = 0; d < D; ++d)
             pdis[d].flush();
     };
-    auto load = [&](uint32_t j) { return SecondRec{__ldg(&f.geo0[j]), __ldg(&f.dyn[j])}; };
+    auto load = [&](uint32_t j) {
+        SecondRec r;
+        load_rec(f.rec, j, r.g, r.v);
+        return r;
+    };
     if (LISTS)
         list_sweep<false>(i, n, in, load, pair, flush);
     else
-        cell_sweep<D>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, i, f.geo0, load, pair, flush);
+        cell_sweep<D>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, i, f.rec, load, pair, flush);
 
     Acc wrate, wdis[3];
     auto wpair = [&](const SecondRec &r) {
@@ -526,11 +597,16 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
         for (int d = 0; d < D; ++d)
             wdis[d].flush();
     };
-    auto wload = [&](uint32_t j) { return SecondRec{__ldg(&w.geo[j]), __ldg(&w.n[j])}; };
+    auto wload = [&](uint32_t j) {
+        SecondRec r;
+        load_rec(w.rec, j, r.g, r.v);
+        return r;
+    };
     if (LISTS)
         list_sweep<false>(i, n, wl, wload, wpair, wflush);
     else
-        cell_sweep<D>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, ~size_t(0), w.geo, wload, wpair, wflush);
+        cell_sweep<D>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, ~size_t(0), w.rec, wload, wpair,
+                      wflush);
 
     float drho_dt = f.drho_dt[i] + rate.value() * rho_i + wrate.value() * rho_i;
     f.drho_dt[i] = drho_dt;
@@ -556,18 +632,18 @@ __device__ __forceinline__ void build_particle(size_t i, size_t n, const MPParam
                                                const MPState &f, const MPWallData &w, const MPNeighbors &in,
                                                const MPNeighbors &wl, unsigned int *max_counts)
 {
-    const float4 gi = f.geo0[i];
+    const float4 gi = f.geo0(i);
     const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
     int ci[3] = {0, 0, 0};
     unpack_cell<D>(__float_as_uint(gi.w), ci);
     const float oi[3] = {gi.x, gi.y, gi.z};
     Kahan sigma;
     unsigned cnt = 0;
-    for_each_candidate<D>(v.m, v.cell_base, v.f_offset, ci, [&](uint32_t j) {
+    for_each_candidate<D>(v.m, v.cell_base, v.f_offset, ci, Reach{oi, k.gs_f, k.rc_reach}, [&](uint32_t j) {
         if (j == uint32_t(i))
             return;
         float dx[3];
-        geo_dx<D>(k.gs_f, pib, oi, f.geo0[j], dx);
+        geo_dx<D>(k.gs_f, pib, oi, f.geo0(j), dx);
         float r2 = sq<D>(dx);
         if (!(r2 < k.rc_sqr))
             return;
@@ -578,9 +654,9 @@ __device__ __forceinline__ void build_particle(size_t i, size_t n, const MPParam
     });
     Kahan wsig;
     unsigned wc = 0;
-    for_each_candidate<D>(v.m, v.cell_base, v.w_offset, ci, [&](uint32_t j) {
+    for_each_candidate<D>(v.m, v.cell_base, v.w_offset, ci, Reach{oi, k.gs_f, k.rc_reach}, [&](uint32_t j) {
         float dx[3];
-        geo_dx<D>(k.gs_f, pib, oi, w.geo[j], dx);
+        geo_dx<D>(k.gs_f, pib, oi, w.geo(j), dx);
         float r2 = sq<D>(dx);
         if (!(r2 < k.rc_sqr))
             return;
@@ -622,15 +698,19 @@ __device__ __forceinline__ uint32_t wrap_corr(const MPParams &k, uint32_t e)
     return c;
 }
 
-// Candidates of the wrapped window around sub-cell c: f(j, code) with code the per-axis
-// image shifts (two bits per axis, two's complement) of the cell j was found in.
+// Candidates of the wrapped window around sub-cell c, pruned as for_each_candidate does:
+// f(j, code) with code the per-axis image shifts (two bits per axis, two's complement) of
+// the cell j was found in.
 template <int D, class F>
 __device__ __forceinline__ void for_each_candidate_periodic(const MeshDev &m, const uint32_t *offset, const int *c,
-                                                            F &&f)
+                                                            const Reach &q, F &&f)
 {
     const int NL = m.all_cells[D - 1];
-    auto last_axis = [&](uint32_t base, uint32_t code) {
-        const int lo = c[D - 1] - kReach, hi = c[D - 1] + kReach;
+    const float r2 = q.r * q.r;
+    auto last_axis = [&](uint32_t base, uint32_t code, float rl) {
+        int l, h;
+        axis_reach(q.o[D - 1], q.gs, rl, l, h);
+        const int lo = c[D - 1] - l, hi = c[D - 1] + h;
         auto seg = [&](int z0, int z1, int s) {
             const uint32_t cd = code | ((uint32_t(s) & 3u) << (2 * (D - 1)));
             const uint32_t b = offset[base + uint32_t(z0)], e = offset[base + uint32_t(z1) + 1];
@@ -650,23 +730,34 @@ __device__ __forceinline__ void for_each_candidate_periodic(const MeshDev &m, co
         else
             seg(lo, hi, 0);
     };
-    for (int a = -kReach; a <= kReach; ++a)
+    int l0, h0;
+    axis_reach(q.o[0], q.gs, q.r, l0, h0);
+    for (int a = -l0; a <= h0; ++a)
     {
+        const float gx = slab_gap(q.o[0], q.gs, a);
         int x = c[0] + a;
         const int sx = x < 0 ? 1 : (x >= m.all_cells[0] ? -1 : 0);
         x += sx * m.all_cells[0];
         const uint32_t cx = uint32_t(sx) & 3u;
         if (D == 2)
-            last_axis(uint32_t(x) * uint32_t(m.all_cells[1]), cx);
+            last_axis(uint32_t(x) * uint32_t(m.all_cells[1]), cx, sqrtf(fmaxf(r2 - gx * gx, 0.0f)));
         else
-            for (int b = -kReach; b <= kReach; ++b)
+        {
+            int l1, h1;
+            axis_reach(q.o[1], q.gs, q.r, l1, h1);
+            for (int b = -l1; b <= h1; ++b)
             {
+                const float gy = slab_gap(q.o[1], q.gs, b);
+                const float g2 = gx * gx + gy * gy;
+                if (!(g2 < r2))
+                    continue;
                 int y = c[1] + b;
                 const int sy = y < 0 ? 1 : (y >= m.all_cells[1] ? -1 : 0);
                 y += sy * m.all_cells[1];
                 last_axis((uint32_t(x) * uint32_t(m.all_cells[1]) + uint32_t(y)) * uint32_t(m.all_cells[2]),
-                          cx | ((uint32_t(sy) & 3u) << 2));
+                          cx | ((uint32_t(sy) & 3u) << 2), sqrtf(r2 - g2));
             }
+        }
     }
 }
 
@@ -677,12 +768,12 @@ __device__ __forceinline__ void cell_sweep_periodic(const MeshDev &m, const uint
                                                     const float4 *geo, Load &&load, Pair &&pair, Flush &&flush)
 {
     int g = 0;
-    for_each_candidate_periodic<D>(m, offset, ci, [&](uint32_t j, uint32_t code) {
+    for_each_candidate_periodic<D>(m, offset, ci, Reach{oi, k.gs_f, k.rc_reach}, [&](uint32_t j, uint32_t code) {
         if (size_t(j) == self && code == 0)
             return;
         const uint32_t e = j | (code << kCodeShift);
         float dx[3];
-        geo_dx<D>(k.gs_f, pib + wrap_corr<D>(k, e), oi, geo[j], dx);
+        geo_dx<D>(k.gs_f, pib + wrap_corr<D>(k, e), oi, geo[2 * size_t(j)], dx);
         if (!(sq<D>(dx) < k.rc_sqr))
             return;
         pair(load(e));
@@ -715,13 +806,13 @@ __device__ __forceinline__ double first_particle_periodic(size_t i, size_t n, co
                                                           const uint32_t *f_offset, double dt, const MPState &f,
                                                           const MPNeighbors &in)
 {
-    const float4 gi = f.geo0[i];
+    const float4 gi = f.geo0(i);
     const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
     int ci[3] = {0, 0, 0};
     if (!LISTS)
         unpack_cell<D>(__float_as_uint(gi.w), ci);
     const float oi[3] = {gi.x, gi.y, gi.z};
-    const float4 di = f.dyn[i];
+    const float4 di = f.dyn(i);
     const float p_i = di.w;
     const float rho_i = k.rho0 + f.drho[i];
     Acc force[3], rdis;
@@ -745,12 +836,14 @@ __device__ __forceinline__ double first_particle_periodic(size_t i, size_t n, co
     };
     auto load = [&](uint32_t e) {
         const uint32_t j = e & kIndexMask;
-        return FirstRecP{__ldg(&f.geo0[j]), __ldg(&f.dyn[j].w), wrap_corr<D>(k, e)};
+        float4 g, d;
+        load_rec(f.rec, j, g, d);
+        return FirstRecP{g, d.w, wrap_corr<D>(k, e)};
     };
     if (LISTS)
         list_sweep<true>(i, n, in, load, pair, flush);
     else
-        cell_sweep_periodic<D>(m, f_offset, ci, k, pib, oi, i, f.geo0, load, pair, flush);
+        cell_sweep_periodic<D>(m, f_offset, ci, k, pib, oi, i, f.rec, load, pair, flush);
 
     f.drho_dt[i] = (rdis.value() * k.inv_z) * rho_i;
     float v2 = 0.f;
@@ -766,24 +859,25 @@ __device__ __forceinline__ double first_particle_periodic(size_t i, size_t n, co
         vn[d] = vo + (f.fprior[d * n + i] + F) * k.inv_mass * dt_f;
         v2 += vn[d] * vn[d];
     }
-    f.dyn[i] = make_float4(vn[0], vn[1], D == 3 ? vn[2] : 0.f, p_i);
+    f.dyn(i) = make_float4(vn[0], vn[1], D == 3 ? vn[2] : 0.f, p_i);
     return k.c0 + double(sqrtf(v2));
 }
 
-// 2nd half of one particle of a periodic flow (Integration2ndHalfInnerRiemann, or
-// ...NoRiemann with limiter slope 0).  Returns max(|v|^2, 4 h |F + F_prior| / m).
-template <int D, bool LISTS>
+// 2nd half of one particle of a periodic flow: Integration2ndHalfInnerRiemann (RIEMANN),
+// or Integration2ndHalfInnerNoRiemann, whose pressure dissipation is zero, so the force
+// sum is left out.  Returns max(|v|^2, 4 h |F + F_prior| / m).
+template <int D, bool LISTS, bool RIEMANN>
 __device__ __forceinline__ double second_particle_periodic(size_t i, size_t n, const MPParams &k, const MeshDev &m,
                                                            const uint32_t *f_offset, double dt, const MPState &f,
                                                            const MPNeighbors &in)
 {
-    const float4 gi = f.geo0[i];
+    const float4 gi = f.geo0(i);
     const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
     int ci[3] = {0, 0, 0};
     if (!LISTS)
         unpack_cell<D>(__float_as_uint(gi.w), ci);
     const float oi[3] = {gi.x, gi.y, gi.z};
-    const float4 di = f.dyn[i];
+    const float4 di = f.dyn(i);
     const float vi[3] = {di.x, di.y, di.z};
     const float rho_i = k.rho0 + f.drho[i];
     Acc rate, pdis[3];
@@ -796,25 +890,32 @@ __device__ __forceinline__ double second_particle_periodic(size_t i, size_t n, c
         const float dv[3] = {vi[0] - r.v.x, vi[1] - r.v.y, vi[2] - r.v.z};
         float u = dot<D>(dv, dx) * inv;
         rate.add(u * dWV);
-        float sc = p_jump(k, u) * (dWV * inv);
+        if (RIEMANN)
+        {
+            float sc = p_jump(k, u) * (dWV * inv);
 #pragma unroll
-        for (int d = 0; d < D; ++d)
-            pdis[d].add(sc * dx[d]);
+            for (int d = 0; d < D; ++d)
+                pdis[d].add(sc * dx[d]);
+        }
     };
     auto flush = [&]() {
         rate.flush();
+        if (RIEMANN)
 #pragma unroll
-        for (int d = 0; d < D; ++d)
-            pdis[d].flush();
+            for (int d = 0; d < D; ++d)
+                pdis[d].flush();
     };
     auto load = [&](uint32_t e) {
         const uint32_t j = e & kIndexMask;
-        return SecondRecP{__ldg(&f.geo0[j]), __ldg(&f.dyn[j]), wrap_corr<D>(k, e)};
+        SecondRecP r;
+        load_rec(f.rec, j, r.g, r.v);
+        r.corr = wrap_corr<D>(k, e);
+        return r;
     };
     if (LISTS)
         list_sweep<false>(i, n, in, load, pair, flush);
     else
-        cell_sweep_periodic<D>(m, f_offset, ci, k, pib, oi, i, f.geo0, load, pair, flush);
+        cell_sweep_periodic<D>(m, f_offset, ci, k, pib, oi, i, f.rec, load, pair, flush);
 
     float drho_dt = f.drho_dt[i] + rate.value() * rho_i;
     f.drho_dt[i] = drho_dt;
@@ -844,23 +945,25 @@ __device__ __forceinline__ void build_particle_periodic(size_t i, size_t n, cons
                                                         const uint32_t *f_offset, const MPState &f,
                                                         const MPNeighbors &in, unsigned int *max_counts)
 {
-    const float4 gi = f.geo0[i];
+    const float4 gi = f.geo0(i);
     const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
     int ci[3] = {0, 0, 0};
     unpack_cell<D>(__float_as_uint(gi.w), ci);
     const float oi[3] = {gi.x, gi.y, gi.z};
-    const float4 di = f.dyn[i];
+    const float4 di = f.dyn(i);
     const float vi[3] = {di.x, di.y, di.z};
     Kahan sigma;
     Acc visc[3], tvc[3];
     unsigned cnt = 0;
     int g = 0;
-    for_each_candidate_periodic<D>(m, f_offset, ci, [&](uint32_t j, uint32_t code) {
+    for_each_candidate_periodic<D>(m, f_offset, ci, Reach{oi, k.gs_f, k.rc_reach}, [&](uint32_t j, uint32_t code) {
         if (j == uint32_t(i) && code == 0)
             return;
         const uint32_t e = j | (code << kCodeShift);
         float dx[3];
-        geo_dx<D>(k.gs_f, pib + wrap_corr<D>(k, e), oi, f.geo0[j], dx);
+        float4 gj, vj;
+        load_rec(f.rec, j, gj, vj);
+        geo_dx<D>(k.gs_f, pib + wrap_corr<D>(k, e), oi, gj, dx);
         float r2 = sq<D>(dx);
         if (!(r2 < k.rc_sqr))
             return;
@@ -871,7 +974,6 @@ __device__ __forceinline__ void build_particle_periodic(size_t i, size_t n, cons
         float r = r2 * inv;
         sigma.add(wc2_W(k.fW, k.inv_h, r));
         float dWV = wc2_dWV(k.cW, k.inv_h, r);
-        const float4 vj = __ldg(&f.dyn[j]);
         const float dv[3] = {vi[0] - vj.x, vi[1] - vj.y, vi[2] - vj.z};
         // e_ij . (B_i + B_j) e_ij = 2 without kernel correction
         float cv = k.mu2 * dWV / (r + k.eps_h);
@@ -918,7 +1020,7 @@ template <int D>
 __device__ __forceinline__ void initial_max(size_t i, size_t n, const MPParams &k, const double *gd, const MPState &f,
                                             double *vm, double *am)
 {
-    float4 di = f.dyn[i];
+    float4 di = f.dyn(i);
     const float vv[3] = {di.x, di.y, di.z};
     double v2 = 0, a2 = 0;
 #pragma unroll

@@ -116,3 +116,17 @@ def test_autotune_keeps_state():
     a.sync_fp64()
     b.sync_fp64()
     assert np.array_equal(a.fp64.water_block.download("Position"), b.fp64.water_block.download("Position"))
+
+
+@pytest.mark.parametrize("case", [cases.dambreak_2d(), cases.dambreak_3d(0.04)], ids=lambda c: c.name)
+def test_pruned_search_finds_every_neighbour(case):
+    """The mixed solver's lists, built by the pruned sub-cell search from the same positions,
+    hold the FP64 relations' pairs: the counts agree up to pairs within rounding of the
+    cut-off (FP32 against FP64 membership)."""
+    mp = MixedPrecisionDamBreak(case)
+    sizes = mp.list_sizes()
+    ref = mp.fp64
+    n_in = int(ref.water_block_inner.neighbors()["counts"].sum())
+    n_w = int(ref.water_wall_contact.neighbors()["counts"].sum())
+    assert abs(sizes["nnz_inner"] - n_in) <= max(2, n_in // 100000), (sizes, n_in)
+    assert abs(sizes["nnz_wall"] - n_w) <= max(2, n_w // 100000), (sizes, n_w)

@@ -168,3 +168,12 @@ def test_mixed_precision_taylor_green_passes_reference_dtw_regression(golden):
         runs = [golden[k] for k in golden.files if k.startswith(f"taylor_green2d/{q}/Run_")]
         ok, d = regression.passes(runs, cur, golden[f"taylor_green2d/{q}/dtw"])
         assert ok, (q, d)
+
+
+def test_mixed_precision_periodic_search_finds_every_neighbour():
+    """Wrapped, pruned sub-cell search against the FP64 periodic relation on the same lattice."""
+    case = small_3d()
+    mp = MixedPrecisionTaylorGreen(case)
+    ref = TaylorGreen(case)
+    n_in = int(ref.water_block_inner.neighbors()["counts"].sum())
+    assert mp.list_sizes()["nnz_inner"] == n_in == 80 * ref.water_block.n
