@@ -110,7 +110,7 @@ __global__ void k_b_from_fp64(size_t n, const double *__restrict__ pos, const ui
 }
 
 template <int D>
-__global__ void k_b_rehash(size_t n, const float4 *__restrict__ rec, const float *__restrict__ off,
+__global__ void k_b_rehash(size_t n, const float4 *__restrict__ geo0, const float *__restrict__ off,
                            const uint32_t *__restrict__ starts, int count, const BInst *__restrict__ inst,
                            uint32_t *__restrict__ ncell, float *__restrict__ noff, uint32_t *__restrict__ key,
                            uint32_t *__restrict__ rank, uint32_t *__restrict__ cnt)
@@ -120,7 +120,7 @@ __global__ void k_b_rehash(size_t n, const float4 *__restrict__ rec, const float
         return;
     const BInst &k = inst[find_instance(starts, count, uint32_t(i))];
     int c0[3];
-    unpack_cell<D>(__float_as_uint(rec[2 * i].w), c0);
+    unpack_cell<D>(__float_as_uint(geo0[i].w), c0);
     double x[3] = {0, 0, 0};
 #pragma unroll
     for (int d = 0; d < D; ++d)
@@ -173,8 +173,8 @@ __global__ void k_b_gather(size_t n, const uint32_t *__restrict__ perm, const ui
         dst.off[d * n + k] = o[d];
         dst.force[d * n + k] = src.force[d * n + i];
     }
-    dst.geo0(k) = make_float4(o[0], o[1], o[2], __uint_as_float(ncell[i]));
-    dst.dyn(k) = src.dyn(i);
+    dst.geo0[k] = make_float4(o[0], o[1], o[2], __uint_as_float(ncell[i]));
+    dst.dyn[k] = src.dyn[i];
     dst.drho[k] = src.drho[i];
     dst.drho_dt[k] = src.drho_dt[i];
     dst.id[k] = src.id[i];
@@ -183,7 +183,7 @@ __global__ void k_b_gather(size_t n, const uint32_t *__restrict__ perm, const ui
 template <int D>
 __global__ void k_b_wall_load(size_t nw, const uint32_t *__restrict__ perm, const double *__restrict__ pos,
                               const double *__restrict__ nrm, const uint32_t *__restrict__ wstarts, int count,
-                              const BInst *__restrict__ inst, float4 *__restrict__ rec)
+                              const BInst *__restrict__ inst, float4 *__restrict__ geo, float4 *__restrict__ n_out)
 {
     size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (k >= nw)
@@ -203,8 +203,8 @@ __global__ void k_b_wall_load(size_t nw, const uint32_t *__restrict__ perm, cons
         o[d] = float(x[d] - cell_corner(b.m, d, c[d]));
         nn[d] = float(nrm[d * nw + i]);
     }
-    rec[2 * k] = make_float4(o[0], o[1], o[2], __uint_as_float(pack_cell<D>(c)));
-    rec[2 * k + 1] = make_float4(nn[0], nn[1], nn[2], 0.f);
+    geo[k] = make_float4(o[0], o[1], o[2], __uint_as_float(pack_cell<D>(c)));
+    n_out[k] = make_float4(nn[0], nn[1], nn[2], 0.f);
 }
 
 template <int D>
@@ -270,7 +270,7 @@ __global__ void k_b_begin(int count, const BInst *__restrict__ inst, BRun *run)
 // ---------------------------------------------------------------- acoustic sub-step
 __global__ void k_b_init1(size_t n, const uint32_t *__restrict__ starts, int count,
                           const BInst *__restrict__ inst, const BRun *__restrict__ run, float *__restrict__ drho,
-                          const float *__restrict__ drho_dt, float4 *__restrict__ rec)
+                          const float *__restrict__ drho_dt, float4 *__restrict__ dyn)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -280,7 +280,7 @@ __global__ void k_b_init1(size_t n, const uint32_t *__restrict__ starts, int cou
         return;
     float r = drho[i] + drho_dt[i] * float(0.5 * run[b].dt);
     drho[i] = r;
-    reinterpret_cast<float *>(rec)[8 * i + 7] = inst[b].p.p0_over_rho0 * r; // pressure of dyn
+    reinterpret_cast<float *>(dyn)[4 * i + 3] = inst[b].p.p0_over_rho0 * r;
 }
 
 // at most 64 registers: 4 blocks of 256 threads per SM
@@ -391,8 +391,8 @@ __global__ void k_b_download(size_t n, const uint32_t *__restrict__ starts, int 
     const BInst &k = inst[b];
     size_t o = size_t(k.p_start) + f.id[i];
     int c[3];
-    unpack_cell<D>(__float_as_uint(f.geo0(i).w), c);
-    float4 di = f.dyn(i);
+    unpack_cell<D>(__float_as_uint(f.geo0[i].w), c);
+    float4 di = f.dyn[i];
     const float v[3] = {di.x, di.y, di.z};
 #pragma unroll
     for (int d = 0; d < D; ++d)
@@ -470,14 +470,15 @@ constexpr uint64_t kConfigLaunches = 9, kBeginLaunches = 2, kSubstepLaunches = 4
 int b_alloc_state(sphx_batch bt, MPState &s)
 {
     size_t n = bt->n, D = size_t(bt->dim);
-    s.rec = bt->alloc<float4>(2 * n);
+    s.geo0 = bt->alloc<float4>(n);
+    s.dyn = bt->alloc<float4>(n);
     s.off = bt->alloc<float>(D * n);
     s.force = bt->alloc<float>(D * n);
     s.drho = bt->alloc<float>(n);
     s.drho_dt = bt->alloc<float>(n);
     s.drho_sum = bt->alloc<float>(n);
     s.id = bt->alloc<uint32_t>(n);
-    if (!s.rec || !s.off || !s.force || !s.drho || !s.drho_dt || !s.drho_sum || !s.id)
+    if (!s.geo0 || !s.dyn || !s.off || !s.force || !s.drho || !s.drho_dt || !s.drho_sum || !s.id)
         return fail(SPHX_ERR_OUT_OF_MEMORY, "batch state allocation failed");
     return SPHX_OK;
 }
@@ -533,7 +534,7 @@ int b_enqueue_configuration(sphx_batch bt, cudaStream_t s, const MPState &src, c
     if (rehash)
     {
         SPHX_CUDA(cudaMemsetAsync(bt->cnt, 0, bt->ncells * sizeof(uint32_t), s));
-        k_b_rehash<D><<<grid_for(n, 256), 256, 0, s>>>(n, src.rec, src.off, bt->starts, bt->count, bt->inst,
+        k_b_rehash<D><<<grid_for(n, 256), 256, 0, s>>>(n, src.geo0, src.off, bt->starts, bt->count, bt->inst,
                                                        bt->ncell, bt->noff, bt->key, bt->rank, bt->cnt);
         SPHX_CUDA(cudaGetLastError());
     }
@@ -589,7 +590,7 @@ int b_enqueue_substep(sphx_batch bt, cudaStream_t s, const MPState &cur, int use
     size_t n = bt->n;
     unsigned blk = unsigned(bt->block);
     k_b_init1<<<grid_for(n, 256), 256, 0, s>>>(n, bt->starts, bt->count, bt->inst, bt->run, cur.drho, cur.drho_dt,
-                                               cur.rec);
+                                               cur.dyn);
     SPHX_CUDA(cudaGetLastError());
     k_b_first<D><<<grid_for(n, blk), blk, 0, s>>>(n, bt->starts, bt->count, bt->inst, bt->run, cur, bt->w, bt->in,
                                                   bt->wl);
@@ -734,7 +735,7 @@ int b_setup(sphx_batch bt, const double *d_fpos, const double *d_wpos, const dou
     if (nw > 0)
     {
         k_b_wall_load<D><<<grid_for(nw, 256), 256, 0, s>>>(nw, bt->perm, d_wpos, d_wnrm, bt->wstarts, bt->count,
-                                                           bt->inst, bt->w.rec);
+                                                           bt->inst, bt->w.geo, bt->w.n);
         SPHX_LAUNCHED(ctx);
     }
     // fluid: hashed from the FP64 positions, then ordered with lists and density sums
@@ -836,14 +837,15 @@ extern "C" int sphx_batch_create(sphx_ctx ctx, int dim, int count, const sphx_ba
     bt->perm = bt->alloc<uint32_t>(big);
     bt->ncell = bt->alloc<uint32_t>(n);
     bt->noff = bt->alloc<float>(3 * n);
-    bt->w.rec = bt->alloc<float4>(2 * nw);
+    bt->w.geo = bt->alloc<float4>(nw);
+    bt->w.n = bt->alloc<float4>(nw);
     bt->in.count = bt->alloc<uint32_t>(n);
     bt->wl.count = bt->alloc<uint32_t>(n);
     bt->d_max = bt->alloc<unsigned int>(2);
     bt->d_any = bt->alloc<int>(1);
     int st;
     if (!bt->inst || !bt->run || !bt->starts || !bt->wstarts || !bt->f_offset || !bt->w_offset || !bt->cnt ||
-        !bt->scan_tiles || !bt->key || !bt->rank || !bt->perm || !bt->ncell || !bt->noff || !bt->w.rec ||
+        !bt->scan_tiles || !bt->key || !bt->rank || !bt->perm || !bt->ncell || !bt->noff || !bt->w.geo || !bt->w.n ||
         !bt->in.count || !bt->wl.count || !bt->d_max || !bt->d_any)
         return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "batch allocation failed"));
     if ((st = b_alloc_state(bt, bt->st[0])) != SPHX_OK || (st = b_alloc_state(bt, bt->st[1])) != SPHX_OK)
@@ -903,7 +905,7 @@ extern "C" int sphx_batch_create(sphx_ctx ctx, int dim, int count, const sphx_ba
         cudaMemcpy(bt->wstarts, wstarts.data(), wstarts.size() * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
         cudaMemcpy(a0.id, ids.data(), n * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
         // fluid at rest with rho = rho0 and no pressure force yet
-        cudaMemset(a0.rec, 0, 2 * n * sizeof(float4)) == cudaSuccess &&
+        cudaMemset(a0.dyn, 0, n * sizeof(float4)) == cudaSuccess &&
         cudaMemset(a0.force, 0, size_t(D) * n * 4) == cudaSuccess &&
         cudaMemset(a0.drho, 0, n * 4) == cudaSuccess && cudaMemset(a0.drho_dt, 0, n * 4) == cudaSuccess;
     if (!ok)

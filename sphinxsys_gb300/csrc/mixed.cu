@@ -91,7 +91,7 @@ __global__ void k_mp_from_fp64(size_t n, const double *__restrict__ pos, MPConst
 // A periodic flow wraps the position into its box first, as PeriodicBounding does at the
 // end of the advection step (domain_bounding.h:103-113).
 template <int D>
-__global__ void k_mp_rehash(size_t n, const float4 *__restrict__ rec, const float *__restrict__ off, MPConst k,
+__global__ void k_mp_rehash(size_t n, const float4 *__restrict__ geo0, const float *__restrict__ off, MPConst k,
                             uint32_t *__restrict__ ncell, float *__restrict__ noff, uint32_t *__restrict__ key,
                             uint32_t *__restrict__ rank, uint32_t *__restrict__ count)
 {
@@ -100,7 +100,7 @@ __global__ void k_mp_rehash(size_t n, const float4 *__restrict__ rec, const floa
         return;
     const MeshDev &m = k.m;
     int c0[3];
-    unpack_cell<D>(__float_as_uint(rec[2 * i].w), c0);
+    unpack_cell<D>(__float_as_uint(geo0[i].w), c0);
     double x[3] = {0, 0, 0};
 #pragma unroll
     for (int d = 0; d < D; ++d)
@@ -172,8 +172,8 @@ __global__ void k_mp_gather(size_t n, const uint32_t *__restrict__ perm, const u
         dst.off[d * n + k] = o[d];
         dst.force[d * n + k] = src.force[d * n + i];
     }
-    dst.geo0(k) = make_float4(o[0], o[1], o[2], __uint_as_float(ncell[i]));
-    dst.dyn(k) = src.dyn(i);
+    dst.geo0[k] = make_float4(o[0], o[1], o[2], __uint_as_float(ncell[i]));
+    dst.dyn[k] = src.dyn[i];
     dst.drho[k] = src.drho[i];
     dst.drho_dt[k] = src.drho_dt[i];
     dst.id[k] = src.id[i];
@@ -227,14 +227,14 @@ __global__ void k_mp_density(size_t n, const float *__restrict__ drho_sum, float
 
 // ---------------------------------------------------------------- acoustic sub-step
 __global__ void k_mp_init1(size_t n, float *__restrict__ drho, const float *__restrict__ drho_dt,
-                           float4 *__restrict__ rec, float p0_over_rho0, float half_dt)
+                           float4 *__restrict__ dyn, float p0_over_rho0, float half_dt)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
     float r = drho[i] + drho_dt[i] * half_dt;
     drho[i] = r;
-    reinterpret_cast<float *>(rec)[8 * i + 7] = p0_over_rho0 * r; // pressure of dyn
+    reinterpret_cast<float *>(dyn)[4 * i + 3] = p0_over_rho0 * r;
 }
 
 // at most 64 registers: 4 blocks of 256 threads per SM
@@ -285,11 +285,6 @@ __global__ void k_mp_second_periodic(size_t n, MPConst k, MPFluid f, const uint3
     warp_max_to(adv_slot, amax);
 }
 
-// The periodic 2nd half with or without the Riemann dissipation (limiter slope 0 is the
-// reference's NoRiemannSolver).
-template <int D, bool LISTS>
-void launch_second_periodic(sphx_mp_s *mp, unsigned blk, double dt);
-
 template <int D>
 __global__ void k_mp_initial_max(size_t n, MPConst k, MPFluid f, unsigned long long *ac_slot,
                                  unsigned long long *adv_slot)
@@ -327,7 +322,7 @@ __global__ void k_mp_import(size_t n, ImportArgs a, MPFluid f)
     float dr = float(a.rho[i] - a.rho0);
     f.drho[i] = dr;
     f.drho_dt[i] = a.drho_dt ? float(a.drho_dt[i]) : 0.f;
-    f.dyn(i) = make_float4(v[0], v[1], v[2], float(a.c0_sqr) * dr);
+    f.dyn[i] = make_float4(v[0], v[1], v[2], float(a.c0_sqr) * dr);
     f.id[i] = uint32_t(i);
 }
 
@@ -347,8 +342,8 @@ __global__ void k_mp_download(size_t n, MPConst k, MPFluid f, double *__restrict
         return;
     uint32_t o = f.id[i];
     int c[3];
-    unpack_cell<D>(__float_as_uint(f.geo0(i).w), c);
-    float4 di = f.dyn(i);
+    unpack_cell<D>(__float_as_uint(f.geo0[i].w), c);
+    float4 di = f.dyn[i];
     const float v[3] = {di.x, di.y, di.z};
 #pragma unroll
     for (int d = 0; d < D; ++d)
@@ -371,8 +366,8 @@ __global__ void k_mp_conservation(size_t n, MPConst k, MPFluid f, double *__rest
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
     {
         int c[3];
-        unpack_cell<D>(__float_as_uint(f.geo0(i).w), c);
-        float4 di = f.dyn(i);
+        unpack_cell<D>(__float_as_uint(f.geo0[i].w), c);
+        float4 di = f.dyn[i];
         const float vv[3] = {di.x, di.y, di.z};
         double m = k.p.mass, v2 = 0, gx = 0;
         s[0] += m;
@@ -411,7 +406,7 @@ __global__ void k_mp_upper_front(size_t n, MPConst k, MPFluid f, int axis, doubl
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
     {
         int c[3];
-        unpack_cell<D>(__float_as_uint(f.geo0(i).w), c);
+        unpack_cell<D>(__float_as_uint(f.geo0[i].w), c);
         double x[3];
         bool in = true;
 #pragma unroll
@@ -428,7 +423,8 @@ __global__ void k_mp_upper_front(size_t n, MPConst k, MPFluid f, int axis, doubl
 
 template <int D>
 __global__ void k_wall_load(size_t nw, const uint32_t *__restrict__ perm, const double *__restrict__ pos,
-                            const double *__restrict__ nrm, MeshDev m, float4 *__restrict__ rec)
+                            const double *__restrict__ nrm, MeshDev m, float4 *__restrict__ geo,
+                            float4 *__restrict__ n_out)
 {
     size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (k >= nw)
@@ -447,8 +443,8 @@ __global__ void k_wall_load(size_t nw, const uint32_t *__restrict__ perm, const 
         o[d] = float(x[d] - cell_corner(m, d, c[d]));
         nn[d] = float(nrm[d * nw + i]);
     }
-    rec[2 * k] = make_float4(o[0], o[1], o[2], __uint_as_float(pack_cell<D>(c)));
-    rec[2 * k + 1] = make_float4(nn[0], nn[1], nn[2], 0.f);
+    geo[k] = make_float4(o[0], o[1], o[2], __uint_as_float(pack_cell<D>(c)));
+    n_out[k] = make_float4(nn[0], nn[1], nn[2], 0.f);
 }
 
 template <int D>
@@ -513,6 +509,8 @@ struct sphx_mp_s
 
 namespace
 {
+// The periodic 2nd half with or without the Riemann dissipation (limiter slope 0 is the
+// reference's NoRiemannSolver).
 template <int D, bool LISTS>
 void launch_second_periodic(sphx_mp_s *mp, unsigned blk, double dt)
 {
@@ -529,14 +527,15 @@ void launch_second_periodic(sphx_mp_s *mp, unsigned blk, double dt)
 int alloc_state(sphx_mp mp, MPFluid &s)
 {
     size_t n = mp->n, D = size_t(mp->dim);
-    s.rec = mp->alloc<float4>(2 * n);
+    s.geo0 = mp->alloc<float4>(n);
+    s.dyn = mp->alloc<float4>(n);
     s.off = mp->alloc<float>(D * n);
     s.force = mp->alloc<float>(D * n);
     s.drho = mp->alloc<float>(n);
     s.drho_dt = mp->alloc<float>(n);
     s.drho_sum = mp->alloc<float>(n);
     s.id = mp->alloc<uint32_t>(n);
-    if (!s.rec || !s.off || !s.force || !s.drho || !s.drho_dt || !s.drho_sum || !s.id)
+    if (!s.geo0 || !s.dyn || !s.off || !s.force || !s.drho || !s.drho_dt || !s.drho_sum || !s.id)
         return fail(SPHX_ERR_OUT_OF_MEMORY, "mixed-precision state allocation failed");
     if (mp->k.periodic)
     {
@@ -626,7 +625,7 @@ int configuration_update(sphx_mp mp, bool from_state)
         SPHX_CUDA(cudaMemsetAsync(mp->count, 0, mp->ncells * sizeof(uint32_t), s));
         if (n > 0)
         {
-            k_mp_rehash<D><<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.rec, mp->a.off, mp->k, mp->ncell, mp->noff,
+            k_mp_rehash<D><<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.geo0, mp->a.off, mp->k, mp->ncell, mp->noff,
                                                             mp->key, mp->rank, mp->count);
             SPHX_LAUNCHED(ctx);
         }
@@ -660,7 +659,7 @@ int substep(sphx_mp mp, double dt)
     if (n == 0)
         return SPHX_OK;
     unsigned blk = unsigned(mp->block);
-    k_mp_init1<<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.drho, mp->a.drho_dt, mp->a.rec, mp->k.p.p0_over_rho0,
+    k_mp_init1<<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.drho, mp->a.drho_dt, mp->a.dyn, mp->k.p.p0_over_rho0,
                                                 float(0.5 * dt));
     SPHX_LAUNCHED(ctx);
     SPHX_CUDA(cudaMemsetAsync(mp->slots, 0, 2 * sizeof(unsigned long long), s));
@@ -933,13 +932,14 @@ extern "C" int sphx_mp_create(sphx_relation inner, sphx_relation wall, const sph
     mp->perm = mp->alloc<uint32_t>(big);
     mp->ncell = mp->alloc<uint32_t>(n);
     mp->noff = mp->alloc<float>(3 * n);
-    mp->w.rec = mp->alloc<float4>(2 * nw);
+    mp->w.geo = mp->alloc<float4>(nw);
+    mp->w.n = mp->alloc<float4>(nw);
     mp->w.nw = nw;
     mp->in.count = mp->alloc<uint32_t>(n);
     mp->wl.count = mp->alloc<uint32_t>(n);
     mp->slots = mp->alloc<unsigned long long>(8);
     if (!mp->f_offset || !mp->w_offset || !mp->count || !mp->key || !mp->rank || !mp->perm || !mp->ncell ||
-        !mp->noff || !mp->w.rec || !mp->in.count || !mp->wl.count || !mp->slots)
+        !mp->noff || !mp->w.geo || !mp->w.n || !mp->in.count || !mp->wl.count || !mp->slots)
         return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "mixed-precision allocation failed"));
     if (cudaMallocHost(&mp->h_slots, 8 * sizeof(unsigned long long)) != cudaSuccess)
         return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "pinned allocation failed"));
@@ -971,10 +971,10 @@ extern "C" int sphx_mp_create(sphx_relation inner, sphx_relation wall, const sph
     {
         if (D == 2)
             k_wall_load<2><<<grid_for(nw, 256), 256, 0, s>>>(nw, mp->perm, (const double *)wpos->dev,
-                                                              (const double *)wn->dev, m, mp->w.rec);
+                                                              (const double *)wn->dev, m, mp->w.geo, mp->w.n);
         else
             k_wall_load<3><<<grid_for(nw, 256), 256, 0, s>>>(nw, mp->perm, (const double *)wpos->dev,
-                                                              (const double *)wn->dev, m, mp->w.rec);
+                                                              (const double *)wn->dev, m, mp->w.geo, mp->w.n);
         ctx->launches++;
     }
     if ((st = import_fluid(mp, fb, p->rho0, p->c0)) != SPHX_OK)
@@ -1191,8 +1191,8 @@ struct Snapshot
     int take(sphx_mp mp, bool restore)
     {
         size_t n = mp->n, D = size_t(mp->dim);
-        void *src[6] = {mp->a.rec, mp->a.off, mp->a.force, mp->a.drho, mp->a.drho_dt, mp->slots};
-        size_t bytes[6] = {2 * n * sizeof(float4), D * n * 4, D * n * 4, n * 4, n * 4, 2 * sizeof(unsigned long long)};
+        void *src[6] = {mp->a.dyn, mp->a.off, mp->a.force, mp->a.drho, mp->a.drho_dt, mp->slots};
+        size_t bytes[6] = {n * sizeof(float4), D * n * 4, D * n * 4, n * 4, n * 4, 2 * sizeof(unsigned long long)};
         if (!restore)
         {
             bufs.assign(6, nullptr);

@@ -115,35 +115,18 @@ inline MPParams make_params(int dim, double grid_spacing, double h, double rho0,
     return k;
 }
 
-// A particle's neighbour record is 32 bytes, {geo0, dyn}: geo0 = {offset at the last
-// configuration update (x, y, z), packed cell}, dyn = {velocity, pressure}.  Both sweeps
-// read the whole record of a neighbour with one 256-bit load.
 struct MPState
 {
-    float4 *rec; // 2 float4 per particle, 32-byte aligned
+    float4 *geo0, *dyn; // {offset at the last configuration update, packed cell}; {velocity, pressure}
     float *off, *force, *drho, *drho_dt, *drho_sum;
     uint32_t *id;
     float *fprior, *shift; // periodic flow only: prior (viscous) force, transport-velocity shift
-    __device__ __forceinline__ float4 &geo0(size_t i) const { return rec[2 * i]; }
-    __device__ __forceinline__ float4 &dyn(size_t i) const { return rec[2 * i + 1]; }
 };
 
-// Wall record, 32 bytes: {offset, packed cell}, {normal, 0}.
 struct MPWallData
 {
-    float4 *rec;
-    __device__ __forceinline__ float4 &geo(size_t i) const { return rec[2 * i]; }
-    __device__ __forceinline__ float4 &n(size_t i) const { return rec[2 * i + 1]; }
+    float4 *geo, *n;
 };
-
-// One 256-bit read-only load of record j (ld.global.nc.v8.f32, 32-byte aligned).
-__device__ __forceinline__ void load_rec(const float4 *rec, uint32_t j, float4 &a, float4 &b)
-{
-    const float4 *p = rec + 2 * size_t(j);
-    asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                 : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
-                 : "l"(p));
-}
 
 struct MPNeighbors
 {
@@ -409,7 +392,7 @@ __device__ __forceinline__ void cell_sweep(const Visit &v, const uint32_t *offse
         if (size_t(j) == self)
             return;
         float dx[3];
-        geo_dx<D>(gs, pib, oi, geo[2 * size_t(j)], dx);
+        geo_dx<D>(gs, pib, oi, geo[j], dx);
         if (!(sq<D>(dx) < rc_sqr))
             return;
         pair(load(j));
@@ -440,13 +423,13 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
                                                  const MPState &f, const MPWallData &w, const MPNeighbors &in,
                                                  const MPNeighbors &wl)
 {
-    const float4 gi = f.geo0(i);
+    const float4 gi = f.geo0[i];
     const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
     int ci[3] = {0, 0, 0};
     if (!LISTS)
         unpack_cell<D>(__float_as_uint(gi.w), ci);
     const float oi[3] = {gi.x, gi.y, gi.z};
-    const float4 di = f.dyn(i);
+    const float4 di = f.dyn[i];
     const float p_i = di.w;
     const float rho_i = k.rho0 + f.drho[i];
     Acc force[3], rdis;
@@ -468,15 +451,11 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
             force[d].flush();
         rdis.flush();
     };
-    auto load = [&](uint32_t j) {
-        float4 g, d;
-        load_rec(f.rec, j, g, d);
-        return FirstRec{g, d.w};
-    };
+    auto load = [&](uint32_t j) { return FirstRec{__ldg(&f.geo0[j]), __ldg(&f.dyn[j].w)}; };
     if (LISTS)
         list_sweep<true>(i, n, in, load, pair, flush);
     else
-        cell_sweep<D>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, i, f.rec, load, pair, flush);
+        cell_sweep<D>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, i, f.geo0, load, pair, flush);
 
     Acc wforce[3], wrdis;
     auto wpair = [&](const float4 &gj) {
@@ -499,11 +478,11 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
             wforce[d].flush();
         wrdis.flush();
     };
-    auto wload = [&](uint32_t j) { return __ldg(&w.geo(j)); };
+    auto wload = [&](uint32_t j) { return __ldg(&w.geo[j]); };
     if (LISTS)
         list_sweep<true>(i, n, wl, wload, wpair, wflush);
     else
-        cell_sweep<D>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, ~size_t(0), w.rec, wload, wpair,
+        cell_sweep<D>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, ~size_t(0), w.geo, wload, wpair,
                       wflush);
 
     f.drho_dt[i] = (rdis.value() * k.inv_z) * rho_i + (wrdis.value() * k.inv_z) * rho_i;
@@ -522,7 +501,7 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
         v2 += vn[d] * vn[d];
     }
     // the pressure stays the one the neighbours of this sweep read
-    f.dyn(i) = make_float4(vn[0], vn[1], D == 3 ? vn[2] : 0.f, p_i);
+    f.dyn[i] = make_float4(vn[0], vn[1], D == 3 ? vn[2] : 0.f, p_i);
     return k.c0 + double(sqrtf(v2));
 }
 
@@ -534,13 +513,13 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
                                                   const MPState &f, const MPWallData &w, const MPNeighbors &in,
                                                   const MPNeighbors &wl)
 {
-    const float4 gi = f.geo0(i);
+    const float4 gi = f.geo0[i];
     const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
     int ci[3] = {0, 0, 0};
     if (!LISTS)
         unpack_cell<D>(__float_as_uint(gi.w), ci);
     const float oi[3] = {gi.x, gi.y, gi.z};
-    const float4 di = f.dyn(i);
+    const float4 di = f.dyn[i];
     const float vi[3] = {di.x, di.y, di.z};
     const float rho_i = k.rho0 + f.drho[i];
     Acc rate, pdis[3];
@@ -564,15 +543,11 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
         for (int d = 0; d < D; ++d)
             pdis[d].flush();
     };
-    auto load = [&](uint32_t j) {
-        SecondRec r;
-        load_rec(f.rec, j, r.g, r.v);
-        return r;
-    };
+    auto load = [&](uint32_t j) { return SecondRec{__ldg(&f.geo0[j]), __ldg(&f.dyn[j])}; };
     if (LISTS)
         list_sweep<false>(i, n, in, load, pair, flush);
     else
-        cell_sweep<D>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, i, f.rec, load, pair, flush);
+        cell_sweep<D>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, i, f.geo0, load, pair, flush);
 
     Acc wrate, wdis[3];
     auto wpair = [&](const SecondRec &r) {
@@ -597,15 +572,11 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
         for (int d = 0; d < D; ++d)
             wdis[d].flush();
     };
-    auto wload = [&](uint32_t j) {
-        SecondRec r;
-        load_rec(w.rec, j, r.g, r.v);
-        return r;
-    };
+    auto wload = [&](uint32_t j) { return SecondRec{__ldg(&w.geo[j]), __ldg(&w.n[j])}; };
     if (LISTS)
         list_sweep<false>(i, n, wl, wload, wpair, wflush);
     else
-        cell_sweep<D>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, ~size_t(0), w.rec, wload, wpair,
+        cell_sweep<D>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, ~size_t(0), w.geo, wload, wpair,
                       wflush);
 
     float drho_dt = f.drho_dt[i] + rate.value() * rho_i + wrate.value() * rho_i;
@@ -632,7 +603,7 @@ __device__ __forceinline__ void build_particle(size_t i, size_t n, const MPParam
                                                const MPState &f, const MPWallData &w, const MPNeighbors &in,
                                                const MPNeighbors &wl, unsigned int *max_counts)
 {
-    const float4 gi = f.geo0(i);
+    const float4 gi = f.geo0[i];
     const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
     int ci[3] = {0, 0, 0};
     unpack_cell<D>(__float_as_uint(gi.w), ci);
@@ -643,7 +614,7 @@ __device__ __forceinline__ void build_particle(size_t i, size_t n, const MPParam
         if (j == uint32_t(i))
             return;
         float dx[3];
-        geo_dx<D>(k.gs_f, pib, oi, f.geo0(j), dx);
+        geo_dx<D>(k.gs_f, pib, oi, f.geo0[j], dx);
         float r2 = sq<D>(dx);
         if (!(r2 < k.rc_sqr))
             return;
@@ -656,7 +627,7 @@ __device__ __forceinline__ void build_particle(size_t i, size_t n, const MPParam
     unsigned wc = 0;
     for_each_candidate<D>(v.m, v.cell_base, v.w_offset, ci, Reach{oi, k.gs_f, k.rc_reach}, [&](uint32_t j) {
         float dx[3];
-        geo_dx<D>(k.gs_f, pib, oi, w.geo(j), dx);
+        geo_dx<D>(k.gs_f, pib, oi, w.geo[j], dx);
         float r2 = sq<D>(dx);
         if (!(r2 < k.rc_sqr))
             return;
@@ -773,7 +744,7 @@ __device__ __forceinline__ void cell_sweep_periodic(const MeshDev &m, const uint
             return;
         const uint32_t e = j | (code << kCodeShift);
         float dx[3];
-        geo_dx<D>(k.gs_f, pib + wrap_corr<D>(k, e), oi, geo[2 * size_t(j)], dx);
+        geo_dx<D>(k.gs_f, pib + wrap_corr<D>(k, e), oi, geo[j], dx);
         if (!(sq<D>(dx) < k.rc_sqr))
             return;
         pair(load(e));
@@ -806,13 +777,13 @@ __device__ __forceinline__ double first_particle_periodic(size_t i, size_t n, co
                                                           const uint32_t *f_offset, double dt, const MPState &f,
                                                           const MPNeighbors &in)
 {
-    const float4 gi = f.geo0(i);
+    const float4 gi = f.geo0[i];
     const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
     int ci[3] = {0, 0, 0};
     if (!LISTS)
         unpack_cell<D>(__float_as_uint(gi.w), ci);
     const float oi[3] = {gi.x, gi.y, gi.z};
-    const float4 di = f.dyn(i);
+    const float4 di = f.dyn[i];
     const float p_i = di.w;
     const float rho_i = k.rho0 + f.drho[i];
     Acc force[3], rdis;
@@ -836,14 +807,12 @@ __device__ __forceinline__ double first_particle_periodic(size_t i, size_t n, co
     };
     auto load = [&](uint32_t e) {
         const uint32_t j = e & kIndexMask;
-        float4 g, d;
-        load_rec(f.rec, j, g, d);
-        return FirstRecP{g, d.w, wrap_corr<D>(k, e)};
+        return FirstRecP{__ldg(&f.geo0[j]), __ldg(&f.dyn[j].w), wrap_corr<D>(k, e)};
     };
     if (LISTS)
         list_sweep<true>(i, n, in, load, pair, flush);
     else
-        cell_sweep_periodic<D>(m, f_offset, ci, k, pib, oi, i, f.rec, load, pair, flush);
+        cell_sweep_periodic<D>(m, f_offset, ci, k, pib, oi, i, f.geo0, load, pair, flush);
 
     f.drho_dt[i] = (rdis.value() * k.inv_z) * rho_i;
     float v2 = 0.f;
@@ -859,7 +828,7 @@ __device__ __forceinline__ double first_particle_periodic(size_t i, size_t n, co
         vn[d] = vo + (f.fprior[d * n + i] + F) * k.inv_mass * dt_f;
         v2 += vn[d] * vn[d];
     }
-    f.dyn(i) = make_float4(vn[0], vn[1], D == 3 ? vn[2] : 0.f, p_i);
+    f.dyn[i] = make_float4(vn[0], vn[1], D == 3 ? vn[2] : 0.f, p_i);
     return k.c0 + double(sqrtf(v2));
 }
 
@@ -871,13 +840,13 @@ __device__ __forceinline__ double second_particle_periodic(size_t i, size_t n, c
                                                            const uint32_t *f_offset, double dt, const MPState &f,
                                                            const MPNeighbors &in)
 {
-    const float4 gi = f.geo0(i);
+    const float4 gi = f.geo0[i];
     const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
     int ci[3] = {0, 0, 0};
     if (!LISTS)
         unpack_cell<D>(__float_as_uint(gi.w), ci);
     const float oi[3] = {gi.x, gi.y, gi.z};
-    const float4 di = f.dyn(i);
+    const float4 di = f.dyn[i];
     const float vi[3] = {di.x, di.y, di.z};
     const float rho_i = k.rho0 + f.drho[i];
     Acc rate, pdis[3];
@@ -907,15 +876,12 @@ __device__ __forceinline__ double second_particle_periodic(size_t i, size_t n, c
     };
     auto load = [&](uint32_t e) {
         const uint32_t j = e & kIndexMask;
-        SecondRecP r;
-        load_rec(f.rec, j, r.g, r.v);
-        r.corr = wrap_corr<D>(k, e);
-        return r;
+        return SecondRecP{__ldg(&f.geo0[j]), __ldg(&f.dyn[j]), wrap_corr<D>(k, e)};
     };
     if (LISTS)
         list_sweep<false>(i, n, in, load, pair, flush);
     else
-        cell_sweep_periodic<D>(m, f_offset, ci, k, pib, oi, i, f.rec, load, pair, flush);
+        cell_sweep_periodic<D>(m, f_offset, ci, k, pib, oi, i, f.geo0, load, pair, flush);
 
     float drho_dt = f.drho_dt[i] + rate.value() * rho_i;
     f.drho_dt[i] = drho_dt;
@@ -945,12 +911,12 @@ __device__ __forceinline__ void build_particle_periodic(size_t i, size_t n, cons
                                                         const uint32_t *f_offset, const MPState &f,
                                                         const MPNeighbors &in, unsigned int *max_counts)
 {
-    const float4 gi = f.geo0(i);
+    const float4 gi = f.geo0[i];
     const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
     int ci[3] = {0, 0, 0};
     unpack_cell<D>(__float_as_uint(gi.w), ci);
     const float oi[3] = {gi.x, gi.y, gi.z};
-    const float4 di = f.dyn(i);
+    const float4 di = f.dyn[i];
     const float vi[3] = {di.x, di.y, di.z};
     Kahan sigma;
     Acc visc[3], tvc[3];
@@ -961,9 +927,7 @@ __device__ __forceinline__ void build_particle_periodic(size_t i, size_t n, cons
             return;
         const uint32_t e = j | (code << kCodeShift);
         float dx[3];
-        float4 gj, vj;
-        load_rec(f.rec, j, gj, vj);
-        geo_dx<D>(k.gs_f, pib + wrap_corr<D>(k, e), oi, gj, dx);
+        geo_dx<D>(k.gs_f, pib + wrap_corr<D>(k, e), oi, f.geo0[j], dx);
         float r2 = sq<D>(dx);
         if (!(r2 < k.rc_sqr))
             return;
@@ -974,6 +938,7 @@ __device__ __forceinline__ void build_particle_periodic(size_t i, size_t n, cons
         float r = r2 * inv;
         sigma.add(wc2_W(k.fW, k.inv_h, r));
         float dWV = wc2_dWV(k.cW, k.inv_h, r);
+        const float4 vj = __ldg(&f.dyn[j]);
         const float dv[3] = {vi[0] - vj.x, vi[1] - vj.y, vi[2] - vj.z};
         // e_ij . (B_i + B_j) e_ij = 2 without kernel correction
         float cv = k.mu2 * dWV / (r + k.eps_h);
@@ -1020,7 +985,7 @@ template <int D>
 __device__ __forceinline__ void initial_max(size_t i, size_t n, const MPParams &k, const double *gd, const MPState &f,
                                             double *vm, double *am)
 {
-    float4 di = f.dyn(i);
+    float4 di = f.dyn[i];
     const float vv[3] = {di.x, di.y, di.z};
     double v2 = 0, a2 = 0;
 #pragma unroll
