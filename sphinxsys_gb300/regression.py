@@ -33,8 +33,13 @@ def dtw_distance(a: Sequence[float], b: Sequence[float], window: int = 5) -> flo
     return float(d[la - 1, lb - 1])
 
 
-def passes(stored_runs, current, stored_dtw) -> tuple:
-    """Returns (ok, distances) for a (observations x snapshots) series against stored runs."""
+def passes(stored_runs, current, stored_dtw, both_orders: bool = False) -> tuple:
+    """Returns (ok, distances) for a (observations x snapshots) series against stored runs.
+
+    The reference measures dtw(stored, current).  When the current series is longer than a
+    stored one by the window or more, the last cell of that table lies outside the band
+    and keeps its zero, so the distance is zero whatever the data; ``both_orders`` also
+    requires dtw(current, stored), whose last cell is inside the band, to pass."""
     current = np.atleast_2d(np.asarray(current, dtype=np.float64))
     dists = []
     ok = True
@@ -44,6 +49,8 @@ def passes(stored_runs, current, stored_dtw) -> tuple:
         for k in range(current.shape[0]):
             ref = run[k][~np.isnan(run[k])]
             dk = dtw_distance(ref, current[k])
+            if both_orders:
+                dk = max(dk, dtw_distance(current[k], ref))
             row.append(dk)
             if dk > 1.01 * stored_dtw[k]:
                 ok = False

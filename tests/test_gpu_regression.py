@@ -96,3 +96,25 @@ def test_mixed_precision_dambreak_2d_passes_reference_regression(golden):
         print("realization", k, "pressure DTW", d_p.ravel(), "energy DTW", d_e.ravel())
         passed += int(ok_p)
     assert passed >= 2, passed
+
+
+def test_fp64_gpu_dambreak_3d_passes_reference_regression(golden):
+    """test_3d_dambreak/dambreak.cpp on the GPU (FP64 drop-in): the six wall probes after
+    every configuration update and the energy every unit of time to t = 20, against the
+    stored runs in both orders of the DTW table (a longer current run makes the
+    reference's own order vacuous)."""
+    sim = DamBreak(cases.dambreak_3d_reference())
+    pressure, energy = [], [sim.mechanical_energy.exec()]
+    while sim.physical_time < 20.0:
+        integration_time = 0.0
+        while integration_time < 1.0:
+            t0 = sim.physical_time
+            sim.advection_step()
+            integration_time += sim.physical_time - t0
+            pressure.append(sim.recorded_pressure.exec())
+        energy.append(sim.mechanical_energy.exec())
+    assert len(energy) == 21 and 0.8 * 2180 <= len(pressure) <= 1.2 * 2180
+    for q, cur in (("FluidObserver_Pressure", np.array(pressure).T), ("WaterBody_TotalMechanicalEnergy", [energy])):
+        runs = [golden[k] for k in golden.files if k.startswith(f"dambreak3d/{q}/Run_")]
+        ok, d = regression.passes(runs, cur, golden[f"dambreak3d/{q}/dtw"], both_orders=True)
+        assert ok, (q, d)

@@ -68,6 +68,30 @@ def test_oracle_2d_dambreak_passes_reference_dtw_regression(golden):
         assert ok, (q, d)
 
 
+@pytest.mark.slow
+def test_oracle_3d_dambreak_passes_reference_dtw_regression(golden):
+    """test_3d_dambreak/dambreak.cpp (tank 5.366 x 2 x 0.5, dp = 0.05, acoustic dt after the
+    relaxation, six wall probes recorded every advection step, energy every unit of time)
+    to t = 20 against its stored runs, in both orders of the DTW table (the stored runs hold
+    2180 / 2181 probe samples; a longer current run makes the reference's own order
+    vacuous)."""
+    oc = O.OracleCase(cases.dambreak_3d_reference())
+    pressure, energy = [], [oc.total_mechanical_energy()]
+    while oc.physical_time.value < 20.0:
+        integration_time = 0.0
+        while integration_time < 1.0:
+            t0 = oc.physical_time.value
+            _, _, obs, _ = oc.advection_step(observe=True)
+            integration_time += oc.physical_time.value - t0
+            pressure.append(obs.copy())
+        energy.append(oc.total_mechanical_energy())
+    assert len(energy) == 21 and 0.8 * 2180 <= len(pressure) <= 1.2 * 2180
+    for q, cur in (("FluidObserver_Pressure", np.array(pressure).T), ("WaterBody_TotalMechanicalEnergy", [energy])):
+        ok, d = regression.passes(series_keys(golden, "dambreak3d/" + q), cur, golden[f"dambreak3d/{q}/dtw"],
+                                  both_orders=True)
+        assert ok, (q, d)
+
+
 def test_ck_tabulated_kernel_matches_analytic_wendland():
     """KernelTabulatedCK's cubic interpolation on 24 entries (dq = 0.1) against the
     analytic Wendland C2 of the same smoothing length: exact at table nodes, within 1e-3
