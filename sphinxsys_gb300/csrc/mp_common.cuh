@@ -245,8 +245,11 @@ __device__ __forceinline__ float p_jump(const MPParams &k, float u)
 // the order of the visited candidates is the unpruned order.
 struct Reach
 {
-    const float *o; // offsets of the particle in its sub-cell
-    float gs, r;    // sub-cell spacing, reach radius
+    const float *o;      // offsets of the particle in its sub-cell
+    float gs, r, inv_gs; // sub-cell spacing, reach radius, 1 / spacing
+    __device__ __forceinline__ Reach(const float *o_, float gs_, float r_) : o(o_), gs(gs_), r(r_), inv_gs(1.0f / gs_)
+    {
+    }
 };
 
 __device__ __forceinline__ float slab_gap(float o, float gs, int a)
@@ -254,23 +257,53 @@ __device__ __forceinline__ float slab_gap(float o, float gs, int a)
     return a > 0 ? float(a) * gs - o : (a < 0 ? o + float(-a - 1) * gs : 0.0f);
 }
 
-// Sub-cells c + a, -lo <= a <= hi, closer than r along one axis.
-__device__ __forceinline__ void axis_reach(float o, float gs, float r, int &lo, int &hi)
+// Sub-cells c + a, -lo <= a <= hi, closer than r along one axis (inv_gs = 1 / gs; the
+// reach margin covers the rounding of the product).
+__device__ __forceinline__ void axis_reach(float o, float inv_gs, float r, int &lo, int &hi)
 {
-    hi = max(0, min(kReach, int(ceilf((r + o) / gs)) - 1));
-    lo = max(0, min(kReach, int(ceilf((r - o) / gs))));
+    hi = max(0, min(kReach, int(ceilf((r + o) * inv_gs)) - 1));
+    lo = max(0, min(kReach, int(ceilf((r - o) * inv_gs))));
 }
 
 // Candidates of the pruned (2 kReach + 1)^D window around sub-cell c; the cells of one
 // instance start at cell_base (columns along the last axis are contiguous in the linear
 // cell order).
-template <int D, class F>
+template <int D, bool PRUNE, class F>
 __device__ __forceinline__ void for_each_candidate(const MeshDev &m, uint32_t cell_base, const uint32_t *offset,
                                                    const int *c, const Reach &q, F &&f)
 {
+    if (!PRUNE)
+    {
+        const int lo0 = max(c[0] - kReach, 0), hi0 = min(c[0] + kReach, m.all_cells[0] - 1);
+        const int lo1 = max(c[1] - kReach, 0), hi1 = min(c[1] + kReach, m.all_cells[1] - 1);
+        if (D == 2)
+        {
+            for (int x = lo0; x <= hi0; ++x)
+            {
+                uint32_t a = cell_base + uint32_t(x) * uint32_t(m.all_cells[1]);
+                uint32_t b = offset[a + uint32_t(lo1)], e = offset[a + uint32_t(hi1) + 1];
+                for (uint32_t j = b; j < e; ++j)
+                    f(j);
+            }
+        }
+        else
+        {
+            const int lo2 = max(c[2] - kReach, 0), hi2 = min(c[2] + kReach, m.all_cells[2] - 1);
+            for (int x = lo0; x <= hi0; ++x)
+                for (int y = lo1; y <= hi1; ++y)
+                {
+                    uint32_t a = cell_base +
+                                 (uint32_t(x) * uint32_t(m.all_cells[1]) + uint32_t(y)) * uint32_t(m.all_cells[2]);
+                    uint32_t b = offset[a + uint32_t(lo2)], e = offset[a + uint32_t(hi2) + 1];
+                    for (uint32_t j = b; j < e; ++j)
+                        f(j);
+                }
+        }
+        return;
+    }
     const float r2 = q.r * q.r;
     int l0, h0;
-    axis_reach(q.o[0], q.gs, q.r, l0, h0);
+    axis_reach(q.o[0], q.inv_gs, q.r, l0, h0);
     const int lo0 = max(c[0] - l0, 0), hi0 = min(c[0] + h0, m.all_cells[0] - 1);
     if (D == 2)
     {
@@ -278,7 +311,7 @@ __device__ __forceinline__ void for_each_candidate(const MeshDev &m, uint32_t ce
         {
             const float gx = slab_gap(q.o[0], q.gs, x - c[0]);
             int l1, h1;
-            axis_reach(q.o[1], q.gs, sqrtf(fmaxf(r2 - gx * gx, 0.0f)), l1, h1);
+            axis_reach(q.o[1], q.inv_gs, sqrtf(fmaxf(r2 - gx * gx, 0.0f)), l1, h1);
             const int lo1 = max(c[1] - l1, 0), hi1 = min(c[1] + h1, m.all_cells[1] - 1);
             uint32_t a = cell_base + uint32_t(x) * uint32_t(m.all_cells[1]);
             uint32_t b = offset[a + uint32_t(lo1)], e = offset[a + uint32_t(hi1) + 1];
@@ -289,7 +322,7 @@ __device__ __forceinline__ void for_each_candidate(const MeshDev &m, uint32_t ce
     else
     {
         int l1, h1;
-        axis_reach(q.o[1], q.gs, q.r, l1, h1);
+        axis_reach(q.o[1], q.inv_gs, q.r, l1, h1);
         const int lo1 = max(c[1] - l1, 0), hi1 = min(c[1] + h1, m.all_cells[1] - 1);
         for (int x = lo0; x <= hi0; ++x)
         {
@@ -301,7 +334,7 @@ __device__ __forceinline__ void for_each_candidate(const MeshDev &m, uint32_t ce
                 if (!(g2 < r2))
                     continue;
                 int l2, h2;
-                axis_reach(q.o[2], q.gs, sqrtf(r2 - g2), l2, h2);
+                axis_reach(q.o[2], q.inv_gs, sqrtf(r2 - g2), l2, h2);
                 const int lo2 = max(c[2] - l2, 0), hi2 = min(c[2] + h2, m.all_cells[2] - 1);
                 uint32_t a = cell_base +
                              (uint32_t(x) * uint32_t(m.all_cells[1]) + uint32_t(y)) * uint32_t(m.all_cells[2]);
@@ -382,13 +415,13 @@ __device__ __forceinline__ void list_sweep(size_t i, size_t n, const MPNeighbors
 }
 
 // Same visits by cell sweep: accepts the candidates the build accepted.
-template <int D, class Load, class Pair, class Flush>
+template <int D, bool PRUNE, class Load, class Pair, class Flush>
 __device__ __forceinline__ void cell_sweep(const Visit &v, const uint32_t *offset, const int *ci, float gs, uint32_t pib,
                                            const float *oi, float rc_sqr, float rc_reach, size_t self,
                                            const float4 *geo, Load &&load, Pair &&pair, Flush &&flush)
 {
     int g = 0;
-    for_each_candidate<D>(v.m, v.cell_base, offset, ci, Reach{oi, gs, rc_reach}, [&](uint32_t j) {
+    for_each_candidate<D, PRUNE>(v.m, v.cell_base, offset, ci, Reach(oi, gs, rc_reach), [&](uint32_t j) {
         if (size_t(j) == self)
             return;
         float dx[3];
@@ -455,7 +488,7 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
     if (LISTS)
         list_sweep<true>(i, n, in, load, pair, flush);
     else
-        cell_sweep<D>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, i, f.geo0, load, pair, flush);
+        cell_sweep<D, true>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, i, f.geo0, load, pair, flush);
 
     Acc wforce[3], wrdis;
     auto wpair = [&](const float4 &gj) {
@@ -482,8 +515,8 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
     if (LISTS)
         list_sweep<true>(i, n, wl, wload, wpair, wflush);
     else
-        cell_sweep<D>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, ~size_t(0), w.geo, wload, wpair,
-                      wflush);
+        cell_sweep<D, false>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, ~size_t(0), w.geo, wload,
+                             wpair, wflush);
 
     f.drho_dt[i] = (rdis.value() * k.inv_z) * rho_i + (wrdis.value() * k.inv_z) * rho_i;
     float v2 = 0.f;
@@ -547,7 +580,7 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
     if (LISTS)
         list_sweep<false>(i, n, in, load, pair, flush);
     else
-        cell_sweep<D>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, i, f.geo0, load, pair, flush);
+        cell_sweep<D, true>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, i, f.geo0, load, pair, flush);
 
     Acc wrate, wdis[3];
     auto wpair = [&](const SecondRec &r) {
@@ -576,8 +609,8 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
     if (LISTS)
         list_sweep<false>(i, n, wl, wload, wpair, wflush);
     else
-        cell_sweep<D>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, ~size_t(0), w.geo, wload, wpair,
-                      wflush);
+        cell_sweep<D, false>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, ~size_t(0), w.geo, wload,
+                             wpair, wflush);
 
     float drho_dt = f.drho_dt[i] + rate.value() * rho_i + wrate.value() * rho_i;
     f.drho_dt[i] = drho_dt;
@@ -610,7 +643,7 @@ __device__ __forceinline__ void build_particle(size_t i, size_t n, const MPParam
     const float oi[3] = {gi.x, gi.y, gi.z};
     Kahan sigma;
     unsigned cnt = 0;
-    for_each_candidate<D>(v.m, v.cell_base, v.f_offset, ci, Reach{oi, k.gs_f, k.rc_reach}, [&](uint32_t j) {
+    for_each_candidate<D, true>(v.m, v.cell_base, v.f_offset, ci, Reach(oi, k.gs_f, k.rc_reach), [&](uint32_t j) {
         if (j == uint32_t(i))
             return;
         float dx[3];
@@ -625,7 +658,7 @@ __device__ __forceinline__ void build_particle(size_t i, size_t n, const MPParam
     });
     Kahan wsig;
     unsigned wc = 0;
-    for_each_candidate<D>(v.m, v.cell_base, v.w_offset, ci, Reach{oi, k.gs_f, k.rc_reach}, [&](uint32_t j) {
+    for_each_candidate<D, false>(v.m, v.cell_base, v.w_offset, ci, Reach(oi, k.gs_f, k.rc_reach), [&](uint32_t j) {
         float dx[3];
         geo_dx<D>(k.gs_f, pib, oi, w.geo[j], dx);
         float r2 = sq<D>(dx);
@@ -680,7 +713,7 @@ __device__ __forceinline__ void for_each_candidate_periodic(const MeshDev &m, co
     const float r2 = q.r * q.r;
     auto last_axis = [&](uint32_t base, uint32_t code, float rl) {
         int l, h;
-        axis_reach(q.o[D - 1], q.gs, rl, l, h);
+        axis_reach(q.o[D - 1], q.inv_gs, rl, l, h);
         const int lo = c[D - 1] - l, hi = c[D - 1] + h;
         auto seg = [&](int z0, int z1, int s) {
             const uint32_t cd = code | ((uint32_t(s) & 3u) << (2 * (D - 1)));
@@ -702,7 +735,7 @@ __device__ __forceinline__ void for_each_candidate_periodic(const MeshDev &m, co
             seg(lo, hi, 0);
     };
     int l0, h0;
-    axis_reach(q.o[0], q.gs, q.r, l0, h0);
+    axis_reach(q.o[0], q.inv_gs, q.r, l0, h0);
     for (int a = -l0; a <= h0; ++a)
     {
         const float gx = slab_gap(q.o[0], q.gs, a);
@@ -715,7 +748,7 @@ __device__ __forceinline__ void for_each_candidate_periodic(const MeshDev &m, co
         else
         {
             int l1, h1;
-            axis_reach(q.o[1], q.gs, q.r, l1, h1);
+            axis_reach(q.o[1], q.inv_gs, q.r, l1, h1);
             for (int b = -l1; b <= h1; ++b)
             {
                 const float gy = slab_gap(q.o[1], q.gs, b);
@@ -739,7 +772,7 @@ __device__ __forceinline__ void cell_sweep_periodic(const MeshDev &m, const uint
                                                     const float4 *geo, Load &&load, Pair &&pair, Flush &&flush)
 {
     int g = 0;
-    for_each_candidate_periodic<D>(m, offset, ci, Reach{oi, k.gs_f, k.rc_reach}, [&](uint32_t j, uint32_t code) {
+    for_each_candidate_periodic<D>(m, offset, ci, Reach(oi, k.gs_f, k.rc_reach), [&](uint32_t j, uint32_t code) {
         if (size_t(j) == self && code == 0)
             return;
         const uint32_t e = j | (code << kCodeShift);
@@ -922,7 +955,7 @@ __device__ __forceinline__ void build_particle_periodic(size_t i, size_t n, cons
     Acc visc[3], tvc[3];
     unsigned cnt = 0;
     int g = 0;
-    for_each_candidate_periodic<D>(m, f_offset, ci, Reach{oi, k.gs_f, k.rc_reach}, [&](uint32_t j, uint32_t code) {
+    for_each_candidate_periodic<D>(m, f_offset, ci, Reach(oi, k.gs_f, k.rc_reach), [&](uint32_t j, uint32_t code) {
         if (j == uint32_t(i) && code == 0)
             return;
         const uint32_t e = j | (code << kCodeShift);
