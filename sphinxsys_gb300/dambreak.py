@@ -326,3 +326,92 @@ class DamBreakCK:
 
     def mechanical_energy(self) -> float:
         return self.fp64.mechanical_energy.exec()
+
+
+def _by_original_id(body, name: str) -> np.ndarray:
+    """A variable in creation order (undoes the Morton re-sorts)."""
+    v = body.download(name)
+    out = np.empty_like(v)
+    out[body.download("OriginalID").astype(np.int64)] = v
+    return out
+
+
+def mixed_vs_fp64(case: DamBreakCase, t_end: float, device: int = 0, fp64_realizations: int = 2) -> dict:
+    """Runs the mixed-precision solver until t_end, then the FP64 path the same number of
+    advection steps from the same initial state, and reports the differences: wall-probe
+    pressure, free-surface height over the initial water column, mechanical energy and the
+    max-norm field errors (relative to the field maximum).  A second FP64 realization,
+    re-sorted once before its first step (same physics, another neighbour summation
+    order), gives the rounding-driven spread of the flow itself at the same step count."""
+    import time
+    mp = MixedPrecisionDamBreak(case, device=device)
+    vert = case.vertical_axis
+    lo, up = list(case.sys_lower[: case.dim]), list(case.sys_upper[: case.dim])
+    lo[0] = case.water_center[0] - case.water_halfsize[0]
+    up[0] = case.water_center[0] + case.water_halfsize[0]
+    t0 = time.perf_counter()
+    steps = 0
+    while mp.physical_time < t_end:
+        mp.advection_step()
+        steps += 1
+    mp_wall = time.perf_counter() - t0
+    out = {"workload": case.name, "t_end": t_end, "advection_steps": steps, "n_fluid": mp.n_fluid,
+           "mixed": {"t": mp.physical_time, "wall_s": mp_wall, "substeps": mp.total_substeps,
+                     "probe_pressure": [float(x) for x in mp.observe_pressure_view()],
+                     "free_surface_height": mp.upper_front(vert, lo, up),
+                     "mechanical_energy": float(mp.conservation()[4])}}
+    fields = ("Position", "Velocity", "Density", "Pressure")
+    mp_fields = {nm: mp.fp64_view(nm) for nm in fields}  # creation order
+
+    def run_fp64(sim, resort: bool):
+        if resort:
+            sim.particle_sorting.exec()
+            sim.update_configuration()
+            sim.number_of_iterations = 0
+        t1 = time.perf_counter()
+        for _ in range(steps):
+            sim.advection_step()
+        res = {"t": sim.physical_time, "wall_s": time.perf_counter() - t1, "substeps": sim.total_substeps,
+               "probe_pressure": [float(x) for x in sim.recorded_pressure.exec()],
+               "free_surface_height": S.UpperFrontInAxisDirection(sim.water_block, lo, up, vert).exec(),
+               "mechanical_energy": sim.mechanical_energy.exec()}
+        return res, {nm: _by_original_id(sim.water_block, nm) for nm in fields}
+
+    def diff(a, fa, b, fb):
+        d = {"probe_pressure_abs": [abs(x - y) for x, y in zip(a["probe_pressure"], b["probe_pressure"])],
+             "free_surface_rel": abs(a["free_surface_height"] / b["free_surface_height"] - 1.0),
+             "mechanical_energy_rel": abs(a["mechanical_energy"] / b["mechanical_energy"] - 1.0)}
+        for nm in fields:
+            d[nm + "_max_rel"] = float(np.max(np.abs(fa[nm] - fb[nm])) / max(np.max(np.abs(fb[nm])), 1e-300))
+        return d
+
+    ref, f_ref = run_fp64(mp.fp64, False)
+    out["fp64"] = ref
+    out["mixed_vs_fp64"] = diff(out["mixed"], mp_fields, ref, f_ref)
+    del mp
+    if fp64_realizations > 1:
+        other, f_other = run_fp64(DamBreak(case, device=device), True)
+        out["fp64_resorted"] = other
+        out["fp64_resorted_vs_fp64"] = diff(other, f_other, ref, f_ref)
+    return out
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+
+    from .cases import dambreak_2d, dambreak_3d
+    ap = argparse.ArgumentParser(description="Dam break: mixed precision against FP64 at a given time")
+    ap.add_argument("--dim", type=int, default=3)
+    ap.add_argument("--dp", type=float, default=0.006)
+    ap.add_argument("--t-end", type=float, default=2.0)
+    ap.add_argument("--fp64-realizations", type=int, default=2)
+    ap.add_argument("--out", default=None)
+    a = ap.parse_args()
+    c = dambreak_3d(a.dp) if a.dim == 3 else dambreak_2d(a.dp)
+    text = json.dumps(mixed_vs_fp64(c, a.t_end, fp64_realizations=a.fp64_realizations))
+    if a.out:
+        with open(a.out, "w") as f:
+            f.write(text)
+    else:
+        print(text)
