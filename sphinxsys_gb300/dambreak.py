@@ -336,64 +336,87 @@ def _by_original_id(body, name: str) -> np.ndarray:
     return out
 
 
-def mixed_vs_fp64(case: DamBreakCase, t_end: float, device: int = 0, fp64_realizations: int = 2) -> dict:
+def mixed_vs_fp64(case: DamBreakCase, t_end: float, device: int = 0, record_every: int = 100,
+                  realizations=("resorted", "perturbed")) -> dict:
     """Runs the mixed-precision solver until t_end, then the FP64 path the same number of
-    advection steps from the same initial state, and reports the differences: wall-probe
-    pressure, free-surface height over the initial water column, mechanical energy and the
-    max-norm field errors (relative to the field maximum).  A second FP64 realization,
-    re-sorted once before its first step (same physics, another neighbour summation
-    order), gives the rounding-driven spread of the flow itself at the same step count."""
+    advection steps from the same initial state, recording every `record_every` steps the
+    wall-probe pressure, the free-surface height over the initial water column and the
+    mechanical energy, and at the end the max-norm field errors (relative to the field
+    maximum).  Further FP64 realizations give the spread of the flow itself at the same
+    step count: "resorted" re-sorts the particles once before the first step (same
+    physics, another neighbour summation order: perturbations at FP64 rounding),
+    "perturbed" moves every initial position by up to 1e-7 h (seeded), the size of the
+    FP32 rounding of the solver's in-cell offsets."""
     import time
     mp = MixedPrecisionDamBreak(case, device=device)
     vert = case.vertical_axis
     lo, up = list(case.sys_lower[: case.dim]), list(case.sys_upper[: case.dim])
     lo[0] = case.water_center[0] - case.water_halfsize[0]
     up[0] = case.water_center[0] + case.water_halfsize[0]
+    fields = ("Position", "Velocity", "Density", "Pressure")
+
+    def sample_mixed():
+        return {"t": mp.physical_time, "probe_pressure": [float(x) for x in mp.observe_pressure_view()],
+                "free_surface_height": mp.upper_front(vert, lo, up),
+                "mechanical_energy": float(mp.conservation()[4])}
+
+    series = {"mixed": [sample_mixed()]}
     t0 = time.perf_counter()
     steps = 0
     while mp.physical_time < t_end:
         mp.advection_step()
         steps += 1
-    mp_wall = time.perf_counter() - t0
-    out = {"workload": case.name, "t_end": t_end, "advection_steps": steps, "n_fluid": mp.n_fluid,
-           "mixed": {"t": mp.physical_time, "wall_s": mp_wall, "substeps": mp.total_substeps,
-                     "probe_pressure": [float(x) for x in mp.observe_pressure_view()],
-                     "free_surface_height": mp.upper_front(vert, lo, up),
-                     "mechanical_energy": float(mp.conservation()[4])}}
-    fields = ("Position", "Velocity", "Density", "Pressure")
-    mp_fields = {nm: mp.fp64_view(nm) for nm in fields}  # creation order
+        if steps % record_every == 0:
+            series["mixed"].append(sample_mixed())
+    wall = {"mixed": time.perf_counter() - t0}
+    if steps % record_every:
+        series["mixed"].append(sample_mixed())
+    end = {"mixed": {nm: mp.fp64_view(nm) for nm in fields}}  # creation order
 
-    def run_fp64(sim, resort: bool):
-        if resort:
+    def sample_fp64(sim):
+        return {"t": sim.physical_time, "probe_pressure": [float(x) for x in sim.recorded_pressure.exec()],
+                "free_surface_height": S.UpperFrontInAxisDirection(sim.water_block, lo, up, vert).exec(),
+                "mechanical_energy": sim.mechanical_energy.exec()}
+
+    def run_fp64(name, sim):
+        if name == "resorted":
             sim.particle_sorting.exec()
+        elif name == "perturbed":
+            x = sim.water_block.download("Position")
+            rng = np.random.default_rng(0)
+            sim.water_block.upload("Position", x + 1e-7 * case.h * rng.uniform(-1.0, 1.0, x.shape))
+        if name != "fp64":
             sim.update_configuration()
             sim.number_of_iterations = 0
+        series[name] = [sample_fp64(sim)]
         t1 = time.perf_counter()
-        for _ in range(steps):
+        for k in range(1, steps + 1):
             sim.advection_step()
-        res = {"t": sim.physical_time, "wall_s": time.perf_counter() - t1, "substeps": sim.total_substeps,
-               "probe_pressure": [float(x) for x in sim.recorded_pressure.exec()],
-               "free_surface_height": S.UpperFrontInAxisDirection(sim.water_block, lo, up, vert).exec(),
-               "mechanical_energy": sim.mechanical_energy.exec()}
-        return res, {nm: _by_original_id(sim.water_block, nm) for nm in fields}
+            if k % record_every == 0:
+                series[name].append(sample_fp64(sim))
+        wall[name] = time.perf_counter() - t1
+        if steps % record_every:
+            series[name].append(sample_fp64(sim))
+        end[name] = {nm: _by_original_id(sim.water_block, nm) for nm in fields}
 
-    def diff(a, fa, b, fb):
-        d = {"probe_pressure_abs": [abs(x - y) for x, y in zip(a["probe_pressure"], b["probe_pressure"])],
-             "free_surface_rel": abs(a["free_surface_height"] / b["free_surface_height"] - 1.0),
-             "mechanical_energy_rel": abs(a["mechanical_energy"] / b["mechanical_energy"] - 1.0)}
-        for nm in fields:
-            d[nm + "_max_rel"] = float(np.max(np.abs(fa[nm] - fb[nm])) / max(np.max(np.abs(fb[nm])), 1e-300))
-        return d
-
-    ref, f_ref = run_fp64(mp.fp64, False)
-    out["fp64"] = ref
-    out["mixed_vs_fp64"] = diff(out["mixed"], mp_fields, ref, f_ref)
+    run_fp64("fp64", mp.fp64)
     del mp
-    if fp64_realizations > 1:
-        other, f_other = run_fp64(DamBreak(case, device=device), True)
-        out["fp64_resorted"] = other
-        out["fp64_resorted_vs_fp64"] = diff(other, f_other, ref, f_ref)
-    return out
+    for name in realizations:
+        run_fp64(name, DamBreak(case, device=device))
+
+    def diff(a, b):
+        sa, sb = series[a], series[b]
+        rows = [{"t": x["t"], "probe_pressure_abs": [abs(p - q) for p, q in zip(x["probe_pressure"], y["probe_pressure"])],
+                 "free_surface_rel": abs(x["free_surface_height"] / y["free_surface_height"] - 1.0),
+                 "mechanical_energy_rel": abs(x["mechanical_energy"] / y["mechanical_energy"] - 1.0)}
+                for x, y in zip(sa, sb)]
+        fe = {nm + "_max_rel": float(np.max(np.abs(end[a][nm] - end[b][nm])) / max(np.max(np.abs(end[b][nm])), 1e-300))
+              for nm in fields}
+        return {"series": rows, "end_fields": fe}
+
+    return {"workload": case.name, "t_end": t_end, "advection_steps": steps, "record_every": record_every,
+            "wall_s": wall, "series": series,
+            "vs_fp64": {name: diff(name, "fp64") for name in ("mixed",) + tuple(realizations)}}
 
 
 if __name__ == "__main__":
@@ -405,11 +428,11 @@ if __name__ == "__main__":
     ap.add_argument("--dim", type=int, default=3)
     ap.add_argument("--dp", type=float, default=0.006)
     ap.add_argument("--t-end", type=float, default=2.0)
-    ap.add_argument("--fp64-realizations", type=int, default=2)
+    ap.add_argument("--record-every", type=int, default=100)
     ap.add_argument("--out", default=None)
     a = ap.parse_args()
     c = dambreak_3d(a.dp) if a.dim == 3 else dambreak_2d(a.dp)
-    text = json.dumps(mixed_vs_fp64(c, a.t_end, fp64_realizations=a.fp64_realizations))
+    text = json.dumps(mixed_vs_fp64(c, a.t_end, record_every=a.record_every))
     if a.out:
         with open(a.out, "w") as f:
             f.write(text)
