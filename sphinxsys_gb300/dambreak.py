@@ -429,10 +429,25 @@ if __name__ == "__main__":
     ap.add_argument("--dp", type=float, default=0.006)
     ap.add_argument("--t-end", type=float, default=2.0)
     ap.add_argument("--record-every", type=int, default=100)
+    ap.add_argument("--run", default=None, choices=["fp64", "mixed"],
+                    help="only advance one solver to t_end and report its throughput")
     ap.add_argument("--out", default=None)
     a = ap.parse_args()
     c = dambreak_3d(a.dp) if a.dim == 3 else dambreak_2d(a.dp)
-    text = json.dumps(mixed_vs_fp64(c, a.t_end, record_every=a.record_every))
+    if a.run:
+        import time
+        sim = MixedPrecisionDamBreak(c) if a.run == "mixed" else DamBreak(c)
+        n = sim.n_fluid if a.run == "mixed" else sim.water_block.n
+        t0, steps, subs = time.perf_counter(), 0, 0
+        while sim.physical_time < a.t_end:
+            subs += sim.advection_step()[0]
+            steps += 1
+        wall = time.perf_counter() - t0
+        text = json.dumps({"workload": c.name, "solver": a.run, "n_fluid": n, "t": sim.physical_time,
+                           "advection_steps": steps, "acoustic_substeps": subs, "wall_s": wall,
+                           "particle_steps_per_s": n * subs / wall})
+    else:
+        text = json.dumps(mixed_vs_fp64(c, a.t_end, record_every=a.record_every))
     if a.out:
         with open(a.out, "w") as f:
             f.write(text)
