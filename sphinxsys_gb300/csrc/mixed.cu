@@ -619,7 +619,6 @@ int configuration_update(sphx_mp mp, bool from_state)
     sphx_ctx ctx = mp->ctx;
     cudaStream_t s = ctx->stream;
     size_t n = mp->n;
-    MeshDev m = mp->k.m;
     if (from_state)
     {
         SPHX_CUDA(cudaMemsetAsync(mp->count, 0, mp->ncells * sizeof(uint32_t), s));
@@ -790,7 +789,6 @@ int import_fluid(sphx_mp mp, sphx_body fb, double rho0, double c0)
     const size_t nc = mp->ncells;
     sphx_ctx ctx = mp->ctx;
     cudaStream_t s = ctx->stream;
-    MeshDev m = mp->k.m;
     SPHX_CUDA(cudaStreamSynchronize(s));
     // fluid: FP64 body state -> FP32 (body order) in `a`, then the first configuration
     Field *pos = fb->find("Position"), *vel = fb->find("Velocity"), *force = fb->find("Force"),
