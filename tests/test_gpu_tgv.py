@@ -177,3 +177,35 @@ def test_mixed_precision_periodic_search_finds_every_neighbour():
     ref = TaylorGreen(case)
     n_in = int(ref.water_block_inner.neighbors()["counts"].sum())
     assert mp.list_sizes()["nnz_inner"] == n_in == 80 * ref.water_block.n
+
+
+def test_periodic_set_up_rejects_invalid_boxes():
+    """The periodic cell list needs 2 cut-offs < L; the mixed periodic solver a cube with at
+    least 5 sub-cells per axis; both refuse with SPHX_ERR_INVALID_ARG and keep the context
+    usable."""
+    import ctypes as C
+    from sphinxsys_gb300 import native as N
+    g = TaylorGreen(cases.taylor_green_2d(40))
+    cl = g.water_block._cl_handle()
+    with pytest.raises(N.SphxError) as e:
+        N.call("sphx_cell_list_set_periodic", cl, 0, 0.0, 0.1, 0.05)  # 2 x 0.05 is not below 0.1
+    assert e.value.code == 1
+    with pytest.raises(N.SphxError) as e:
+        N.call("sphx_cell_list_set_periodic", cl, 2, 0.0, 1.0, 0.05)  # no third axis in 2D
+    assert e.value.code == 1
+    p = g.pressure_relaxation.params
+    h = C.c_void_p()
+    pd = C.POINTER(C.c_double)
+    lo, up = np.zeros(3), np.array([1.0, 0.5, 0.0])
+    with pytest.raises(N.SphxError) as e:  # not a cube
+        N.call("sphx_mp_create_periodic", g.water_block.handle, C.byref(p), lo.ctypes.data_as(pd),
+               up.ctypes.data_as(pd), 0.01, 0.2, C.byref(h))
+    assert e.value.code == 1
+    up = np.array([0.1, 0.1, 0.0])  # 0.1 / h = 3 sub-cells per axis
+    with pytest.raises(N.SphxError) as e:
+        N.call("sphx_mp_create_periodic", g.water_block.handle, C.byref(p), lo.ctypes.data_as(pd),
+               up.ctypes.data_as(pd), 0.01, 0.2, C.byref(h))
+    assert e.value.code == 1
+    # the context still runs the flow
+    g.advection_step()
+    assert np.all(np.isfinite(g.water_block.download("Velocity")))
