@@ -246,6 +246,11 @@ int sphx_ck_advection_step_setup(sphx_body fluid);
 int sphx_ck_update_particle_position(sphx_body fluid);
 /* LinearCorrectionMatrix<Inner<WithUpdate>> + <Contact> (kernel_correction_ck.hpp:25-80). */
 int sphx_ck_linear_correction_matrix(sphx_relation inner, sphx_relation wall_contact, double alpha);
+/* FreeSurfaceIndicationCK<Inner<WithUpdate>, Contact<>> (surface_indication_ck.hpp:49-150,
+ * the boundary indicator of the 3D SYCL dam break): PositionDivergence = -sum dW V r with
+ * the spatial-temporal rule, Indicator (I32, 1 at the free surface) and
+ * PreviousSurfaceIndicator (I32, registered with 1), threshold 0.75 dim. */
+int sphx_ck_free_surface_indication(sphx_relation inner, sphx_relation wall_contact);
 /* AcousticStep1stHalf / 2ndHalf <Inner<OneLevel, AcousticRiemannSolverCK, LinearCorrectionCK>>
  * + <Contact<Wall, ...>> (acoustic_step_1st_half.hpp, acoustic_step_2nd_half.hpp). */
 int sphx_ck_acoustic_step_1st_half(sphx_relation inner, sphx_relation wall_contact, const sphx_fluid_params *p,

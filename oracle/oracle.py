@@ -102,6 +102,9 @@ def lib() -> C.CDLL:
         L.orc_ck_acoustic_step.restype = i
         L.orc_ck_acoustic_step.argtypes = [vp, dp_]
         L.orc_ck_configuration.argtypes = [vp]
+        L.orc_ck_free_surface_indication.argtypes = [vp]
+        L.orc_ck_nested_advection_step.restype = i
+        L.orc_ck_nested_advection_step.argtypes = [vp, dp_, dp_]
         L.orc_ck_density_regularization.argtypes = [vp]
         L.orc_ck_advection_step_setup.argtypes = [vp]
         L.orc_ck_linear_correction_matrix.argtypes = [vp, d]
@@ -288,7 +291,7 @@ class OracleCase:
 
     # ------------------------------------------------------------------ CK numerics
     CK_FIELDS = ("Compression", "CompressionRate", "VolumetricMeasureRef", "CompressionSummation",
-                 "Displacement", "LinearCorrectionMatrix")
+                 "Displacement", "LinearCorrectionMatrix", "PositionDivergence", "Indicator")
 
     def ck_kernel(self, which: str, r: float = 0.0) -> float:
         """Tabulated Wendland C2 of this case: which in ("W", "dW", "W0")."""
@@ -305,6 +308,17 @@ class OracleCase:
     def ck_configuration(self) -> None:
         lib().orc_ck_configuration(self.h)
 
+    def ck_free_surface_indication(self) -> None:
+        lib().orc_ck_free_surface_indication(self.h)
+
+    def ck_nested_advection_step(self):
+        """One advection step of the 3D SYCL dam-break loop (nested advection / acoustic
+        loops, acoustic dt first); returns (sub-steps, advection dt)."""
+        Dt = C.c_double()
+        sub = lib().orc_ck_nested_advection_step(self.h, C.byref(self.physical_time), C.byref(Dt))
+        self.iteration += 1
+        return sub, Dt.value
+
     def ck_advection_steps(self) -> int:
         return int(lib().orc_ck_advection_steps(self.h))
 
@@ -316,11 +330,12 @@ class OracleCase:
     def ck_get(self, name: str) -> np.ndarray:
         which = self.CK_FIELDS.index(name)
         n, d = self.n(FLUID), self.dim
-        size = n * (1 if which < 4 else (d if which == 4 else d * d))
+        scalar = which < 4 or which >= 6
+        size = n * (1 if scalar else (d if which == 4 else d * d))
         out = np.zeros(max(size, 1))
         lib().orc_ck_get(self.h, which, _p(out))
         out = out[:size]
-        return out if which < 4 else (out.reshape(n, d) if which == 4 else out.reshape(n, d, d))
+        return out if scalar else (out.reshape(n, d) if which == 4 else out.reshape(n, d, d))
 
 
 class OracleTGV(OracleCase):

@@ -519,6 +519,8 @@ struct CKState
     std::vector<Real> compression, compression_rate, Vol_ref, compression_sum, wall_Vol_ref;
     std::vector<V3> dpos;
     std::vector<M3> B;
+    std::vector<Real> pos_div;              // "PositionDivergence"
+    std::vector<int> indicator, prev_indicator; // "Indicator", "PreviousSurfaceIndicator" (initial 1)
     Real present_time = 0, interval = 0; // TimeStepper::TriggerByInterval of the advection step
     long advection_steps = 0;
     bool ready = false;
@@ -947,6 +949,9 @@ void ckEnsureState(Case &cs)
     ck.B.assign(n, M3::identity(cs.D)); // "LinearCorrectionMatrix", identity
     ck.Vol_ref = cs.fluid.Vol;           // registerStateVariableFrom("VolumetricMeasureRef", ...)
     ck.wall_Vol_ref = cs.wall.Vol;
+    ck.pos_div.assign(n, 0.0);
+    ck.indicator.assign(n, 0);
+    ck.prev_indicator.assign(n, 1);
     ck.ready = true;
 }
 
@@ -1282,6 +1287,112 @@ int ckAcousticStep(Case &cs, Real *physical_time)
         return 1;
     }
     return 0;
+}
+
+// FreeSurfaceIndicationCK<Inner<WithUpdate>, Contact<>> (surface_indication_ck.hpp:49-150;
+// threshold 0.75 d, h the reference smoothing length): inner interaction with the
+// spatial-temporal rule, contact interaction, then the update over all particles.
+void ckFreeSurfaceIndication(Case &cs)
+{
+    ckEnsureState(cs);
+    const int D = cs.D;
+    Body &f = cs.fluid;
+    CKState &ck = cs.ck;
+    const Real thr = 0.75 * D;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)f.n; ++i)
+    {
+        Real pos_div = 0.0;
+        const Neighborhood &nb = cs.inner[i];
+        for (size_t k = 0; k < nb.size(); ++k)
+        {
+            UInt j = nb.j[k];
+            Real r = std::sqrt(sqnorm(sub3(f.pos[i], f.pos[j], D), D));
+            pos_div -= cs.tk.dW(r) * f.Vol[j] * r;
+        }
+        if (pos_div < thr && ck.prev_indicator[i] != 1)
+        {
+            bool near_previous = false;
+            for (size_t k = 0; k < nb.size(); ++k)
+                if (ck.prev_indicator[nb.j[k]] == 1)
+                {
+                    near_previous = true;
+                    break;
+                }
+            if (!near_previous)
+                pos_div = 2.0 * thr;
+        }
+        ck.pos_div[i] = pos_div;
+    }
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)f.n; ++i)
+    {
+        Real pos_div = 0.0;
+        const Neighborhood &nw = cs.contact[i];
+        for (size_t k = 0; k < nw.size(); ++k)
+        {
+            UInt j = nw.j[k];
+            Real r = std::sqrt(sqnorm(sub3(f.pos[i], cs.wall.pos[j], D), D));
+            pos_div -= cs.tk.dW(r) * cs.wall.Vol[j] * r;
+        }
+        ck.pos_div[i] += pos_div;
+    }
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)f.n; ++i)
+    {
+        int ind = 1;
+        if (ck.pos_div[i] > thr)
+        {
+            bool very_near = false;
+            const Neighborhood &nb = cs.inner[i];
+            for (size_t k = 0; k < nb.size(); ++k)
+            {
+                UInt j = nb.j[k];
+                Real r = std::sqrt(sqnorm(sub3(f.pos[i], f.pos[j], D), D));
+                if (ck.pos_div[j] < thr && r < cs.h)
+                {
+                    very_near = true;
+                    break;
+                }
+            }
+            if (!very_near)
+                ind = 0;
+        }
+        ck.indicator[i] = ind;
+    }
+    ck.prev_indicator = ck.indicator;
+}
+
+// One advection step of tests_sycl/3d_examples/test_3d_dambreak_sycl/dambreak.cpp:186-224:
+// compression summation + regularization, advection-step set-up, advection dt,
+// free-surface indication, correction matrices, the acoustic sub-steps (acoustic dt
+// first), the position update, cell list and relations (the Morton re-sort of the driver
+// only permutes particles and is not applied).  Returns the number of sub-steps.
+int ckNestedAdvectionStep(Case &cs, Real *physical_time, Real *advection_dt)
+{
+    ckDensityRegularization(cs);
+    ckAdvectionStepSetup(cs);
+    Real Dt = ckAdvectionTimeStep(cs);
+    ckFreeSurfaceIndication(cs);
+    ckLinearCorrectionMatrix(cs, 0.5);
+    Real relaxation = 0;
+    int sub = 0;
+    while (relaxation < Dt)
+    {
+        Real dt = ckAcousticTimeStep(cs);
+        ckAcousticStep1stHalf(cs, dt);
+        ckAcousticStep2ndHalf(cs, dt);
+        relaxation += dt;
+        *physical_time += dt;
+        ++sub;
+    }
+    ckUpdateParticlePosition(cs);
+    cs.ck.advection_steps++;
+    cs.fluid_cells.update(cs.fluid, &cs.periodic);
+    updateConfiguration(cs);
+    if (advection_dt)
+        *advection_dt = Dt;
+    return sub;
 }
 
 // dambreak_sycl.cpp:230-245: cell list, relations, density regularization, advection-step
@@ -1880,6 +1991,11 @@ extern "C"
         return ckAcousticStep(*static_cast<Case *>(h), physical_time);
     }
     void orc_ck_configuration(void *h) { ckConfiguration(*static_cast<Case *>(h)); }
+    void orc_ck_free_surface_indication(void *h) { ckFreeSurfaceIndication(*static_cast<Case *>(h)); }
+    int orc_ck_nested_advection_step(void *h, double *physical_time, double *advection_dt)
+    {
+        return ckNestedAdvectionStep(*static_cast<Case *>(h), physical_time, advection_dt);
+    }
     void orc_ck_density_regularization(void *h) { ckDensityRegularization(*static_cast<Case *>(h)); }
     void orc_ck_advection_step_setup(void *h) { ckAdvectionStepSetup(*static_cast<Case *>(h)); }
     void orc_ck_linear_correction_matrix(void *h, double alpha)
@@ -1905,7 +2021,7 @@ extern "C"
     }
     // CK variables of the fluid: 0 Compression, 1 CompressionRate, 2 VolumetricMeasureRef,
     // 3 CompressionSummation (n values); 4 Displacement (n x dim); 5 LinearCorrectionMatrix
-    // (n x dim x dim, row-major).
+    // (n x dim x dim, row-major); 6 PositionDivergence, 7 Indicator (n values).
     void orc_ck_get(void *h, int which, double *out)
     {
         Case *cs = static_cast<Case *>(h);
@@ -1917,9 +2033,13 @@ extern "C"
                                      : which == 1 ? &ck.compression_rate
                                      : which == 2 ? &ck.Vol_ref
                                      : which == 3 ? &ck.compression_sum
+                                     : which == 6 ? &ck.pos_div
                                                   : nullptr;
         if (v)
             std::copy(v->begin(), v->end(), out);
+        else if (which == 7)
+            for (size_t i = 0; i < n; ++i)
+                out[i] = ck.indicator[i];
         else if (which == 4)
             for (size_t i = 0; i < n; ++i)
                 for (int a = 0; a < D; ++a)

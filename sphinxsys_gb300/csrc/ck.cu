@@ -481,6 +481,81 @@ __device__ __forceinline__ void block_max(unsigned long long *slot, double v)
         atomicMax(slot, b);
 }
 
+// FreeSurfaceIndicationCK<Inner<WithUpdate>, Contact<>> (surface_indication_ck.hpp:49-150):
+// position divergence -sum dW V r over the inner neighbours with the spatial-temporal rule
+// (a particle below the threshold that was not a surface particle and has no previous
+// surface particle among its neighbours is lifted to twice the threshold), the wall
+// neighbours added, then the indicator: 0 above the threshold unless a neighbour closer
+// than h lies below it; the previous indicator takes the new value.
+template <int D>
+__global__ void k_ck_indication_inner(size_t n, CKFluid f, Lists in, TabK t, const int *__restrict__ prev,
+                                      double *__restrict__ pos_div, double thr)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    double pd = 0.0, r[3], e[3];
+    const unsigned c = min(in.count[i], in.cap);
+    for (unsigned s = 0; s < c; ++s)
+    {
+        uint32_t j = in.J[size_t(s) * n + i];
+        double len = geometry<D>(f.pos, n, i, f.pos, n, j, r, e);
+        pd -= tdW(t, len) * f.Vol[j] * len;
+    }
+    if (pd < thr && prev[i] != 1)
+    {
+        bool near_previous = false;
+        for (unsigned s = 0; s < c && !near_previous; ++s)
+            near_previous = prev[in.J[size_t(s) * n + i]] == 1;
+        if (!near_previous)
+            pd = 2.0 * thr;
+    }
+    pos_div[i] = pd;
+}
+
+template <int D>
+__global__ void k_ck_indication_contact(size_t n, CKFluid f, CKWall w, Lists wl, TabK t, double *__restrict__ pos_div)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    double pd = 0.0, r[3], e[3];
+    const unsigned c = min(wl.count[i], wl.cap);
+    for (unsigned s = 0; s < c; ++s)
+    {
+        uint32_t j = wl.J[size_t(s) * n + i];
+        double len = geometry<D>(f.pos, n, i, w.pos, w.nw, j, r, e);
+        pd -= tdW(t, len) * w.Vol[j] * len;
+    }
+    pos_div[i] += pd;
+}
+
+template <int D>
+__global__ void k_ck_indication_update(size_t n, CKFluid f, Lists in, const double *__restrict__ pos_div,
+                                       int *__restrict__ indicator, int *__restrict__ prev, double thr, double h)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    int v = 1;
+    if (pos_div[i] > thr)
+    {
+        bool very_near = false;
+        double r[3], e[3];
+        const unsigned c = min(in.count[i], in.cap);
+        for (unsigned s = 0; s < c && !very_near; ++s)
+        {
+            uint32_t j = in.J[size_t(s) * n + i];
+            double len = geometry<D>(f.pos, n, i, f.pos, n, j, r, e);
+            very_near = pos_div[j] < thr && len < h;
+        }
+        if (!very_near)
+            v = 0;
+    }
+    indicator[i] = v;
+    prev[i] = v;
+}
+
 template <int D>
 __global__ void k_ck_acoustic_max(size_t n, CKFluid f, double c0, double h_min, unsigned long long *slot)
 {
@@ -725,6 +800,41 @@ extern "C" int sphx_ck_linear_correction_matrix(sphx_relation inner, sphx_relati
         return SPHX_OK;
     CK_DISPATCH(b, k_ck_correction, grid_for(n, kBlock), n, f, w, lists_of(inner), lists_of(wall),
                 make_tab(b->dim, inner->h), alpha);
+    return SPHX_OK;
+}
+
+extern "C" int sphx_ck_free_surface_indication(sphx_relation inner, sphx_relation wall)
+{
+    SPHX_TRY(ck_check(inner, wall));
+    sphx_body b = inner->src;
+    CKFluid f;
+    CKWall w;
+    SPHX_TRY(ck_fluid(b, f));
+    SPHX_TRY(ck_wall(wall, w));
+    Field *pd, *ind, *prev;
+    SPHX_TRY(b->require("PositionDivergence", SPHX_F64, 1, &pd));
+    SPHX_TRY(b->require("Indicator", SPHX_I32, 1, &ind));
+    const bool fresh = b->find("PreviousSurfaceIndicator") == nullptr;
+    SPHX_TRY(b->require("PreviousSurfaceIndicator", SPHX_I32, 1, &prev));
+    size_t n = b->n;
+    if (n == 0)
+        return SPHX_OK;
+    sphx_ctx ctx = b->ctx;
+    if (fresh) // registerStateVariable<int>("PreviousSurfaceIndicator", 1)
+    {
+        std::vector<int> ones(n, 1);
+        SPHX_CUDA(cudaMemcpyAsync(prev->dev, ones.data(), n * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+        SPHX_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    const double thr = 0.75 * b->dim;
+    TabK t = make_tab(b->dim, inner->h);
+    double *pos_div = f64(pd);
+    int *indicator = static_cast<int *>(ind->dev), *previous = static_cast<int *>(prev->dev);
+    CK_DISPATCH(b, k_ck_indication_inner, grid_for(n, kBlock), n, f, lists_of(inner), t, previous, pos_div, thr);
+    if (wall)
+        CK_DISPATCH(b, k_ck_indication_contact, grid_for(n, kBlock), n, f, w, lists_of(wall), t, pos_div);
+    CK_DISPATCH(b, k_ck_indication_update, grid_for(n, kBlock), n, f, lists_of(inner), pos_div, indicator, previous,
+                thr, inner->h);
     return SPHX_OK;
 }
 

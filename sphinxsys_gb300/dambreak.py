@@ -328,6 +328,65 @@ class DamBreakCK:
         return self.fp64.mechanical_energy.exec()
 
 
+class DamBreakCKNested:
+    """The dam break with the CK particle methods in the nested-loop form of
+    tests/tests_sycl/3d_examples/test_3d_dambreak_sycl/dambreak.cpp:155-224 (FP64 on the
+    CUDA policy): per advection step CompressionSummation + DensityRegularization,
+    AdvectionStepSetup, AdvectionTimeStepCK, the free-surface indicator, the correction
+    matrices, then acoustic sub-steps (acoustic dt first) until the advection dt is
+    covered, UpdateParticlePosition, cell list and relations.  The driver's Morton re-sort
+    only permutes particles and is not applied."""
+
+    def __init__(self, case: DamBreakCase, device: int = 0):
+        self.fp64 = DamBreak(case, device=device)
+        self.case = case
+        sim = self.fp64
+        f, inner, contact = sim.water_block, sim.water_block_inner, sim.water_wall_contact
+        self.water_block = f
+        self.regularization = S.DensityRegularizationCK(inner, contact)
+        self.setup = S.AdvectionStepSetupCK(f)
+        self.advection_dt = S.AdvectionTimeStepCK(f, case.U_ref)
+        self.indication = S.FreeSurfaceIndicationCK(inner, contact)
+        self.correction = S.LinearCorrectionMatrixCK(inner, contact, 0.5)
+        self.acoustic_dt = S.AcousticTimeStepCK(f)
+        self.first_half = S.AcousticStep1stHalfCK(inner, contact)
+        self.second_half = S.AcousticStep2ndHalfCK(inner, contact)
+        self.update_position = S.UpdateParticlePositionCK(f)
+        self.observe = S.ObservingQuantityCK(sim.fluid_observer_contact, "Pressure")
+        self.physical_time = 0.0
+        self.number_of_iterations = 0
+
+    def advection_step(self):
+        sim = self.fp64
+        self.regularization.exec()
+        self.setup.exec()
+        Dt = self.advection_dt.exec()
+        self.indication.exec()
+        self.correction.exec()
+        relaxation, sub = 0.0, 0
+        while relaxation < Dt:
+            dt = self.acoustic_dt.exec()
+            self.first_half.exec(dt)
+            self.second_half.exec(dt)
+            relaxation += dt
+            self.physical_time += dt
+            sub += 1
+        self.update_position.exec()
+        self.number_of_iterations += 1
+        self.water_block.updateCellLinkedList()
+        sim.water_block_inner.updateConfiguration()
+        sim.water_wall_contact.updateConfiguration()
+        if sim.fluid_observer.n:
+            sim.fluid_observer_contact.updateConfiguration()
+        return sub, Dt
+
+    def observe_pressure(self) -> np.ndarray:
+        return self.observe.exec()
+
+    def mechanical_energy(self) -> float:
+        return self.fp64.mechanical_energy.exec()
+
+
 def _by_original_id(body, name: str) -> np.ndarray:
     """A variable in creation order (undoes the Morton re-sorts)."""
     v = body.download(name)

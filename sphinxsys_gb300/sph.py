@@ -685,6 +685,17 @@ class DensityRegularizationCK(_CKFluidDynamics):
     _fn = "sphx_ck_density_regularization"
 
 
+class FreeSurfaceIndicationCK:
+    """InteractionDynamicsCK<FreeSurfaceIndicationComplexSpatialTemporalCK>(inner, contact):
+    PositionDivergence and Indicator (1 at the free surface) of the fluid."""
+
+    def __init__(self, inner: InnerRelation, contact: Optional[ContactRelation]):
+        self.inner, self.contact = inner, contact
+
+    def exec(self, dt: float = 0.0) -> None:
+        N.call("sphx_ck_free_surface_indication", self.inner.handle, self.contact.handle if self.contact else None)
+
+
 class AdvectionStepSetupCK:
     def __init__(self, body: SPHBody):
         self.body = body

@@ -28,8 +28,7 @@ CASES = {
     "still_water2d_ck": "tests/tests_sycl/2d_examples/test_2d_still_water_sycl/regression_test_tool",
     "taylor_green2d": "tests/2d_examples/test_2d_taylor_green/regression_test_tool",
 }
-# the CK 3D pressure series (6 probes x ~2300 samples per run) is not used by the tests
-SKIP = {("dambreak3d_ck", "FluidObserver_Pressure")}
+SKIP = set()
 SCAN_TEST = ("tests/tests_sycl/unit_test_src/shared/particle_dynamics/configuration_dynamics/"
              "test_exclusive_scan_sycl/test_exclusive_scan.cpp")
 
