@@ -6,7 +6,10 @@ by the mixed-precision solver (FP32 pair arithmetic with compensated sums, FP64 
 integration, dt reductions and conservation sums), timed beside the FP64 path on the same
 case from the same initial state, with the field / probe / free-surface errors of mixed
 against FP64.  The FP64 drop-in is also measured on dp = 0.0075 (1,702,400 fluid
-particles) through the reference-shaped API (``fp64_drop_in``).
+particles) through the reference-shaped API (``fp64_drop_in``), a seeded batch of 64
+independent dam breaks against the same instances run one by one in FP64 (``batch``), and
+the 3D periodic Taylor-Green vortex at 256^3 in mixed precision with its kinetic-energy
+decay and a few FP64 steps of the same case (``taylor_green``).
 
 One bench step is one advection step of the Dambreak.cpp loop: advection dt, density
 summation, the acoustic sub-steps (1st + 2nd half each) and the cell-list / configuration
