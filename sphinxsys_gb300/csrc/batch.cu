@@ -38,6 +38,7 @@ struct BInst
     uint32_t cell_base, ncells;
     uint32_t p_start, p_count, w_start, w_count;
     double acoustic_cfl, advection_cfl, U_ref;
+    double inv_gs; // 1 / sub-cell spacing
 };
 
 struct BRun
@@ -82,7 +83,7 @@ __device__ __forceinline__ void hash_position(const BInst &k, const double *x, u
                                               size_t i, uint32_t *key, uint32_t *rank, uint32_t *cnt)
 {
     int c[3] = {0, 0, 0};
-    cell_index<D>(k.m, x, c);
+    sub_cell_index<D>(k.m, k.inv_gs, x, c);
 #pragma unroll
     for (int d = 0; d < D; ++d)
         noff[d * n + i] = float(x[d] - cell_corner(k.m, d, c[d]));
@@ -796,6 +797,7 @@ extern "C" int sphx_batch_create(sphx_ctx ctx, int dim, int count, const sphx_ba
         BInst &k = bt->h_inst[q];
         k = BInst{};
         k.m = mesh_dev(mesh);
+        k.inv_gs = 1.0 / mesh.grid_spacing;
         k.cell_base = uint32_t(nc);
         k.ncells = uint32_t(cells);
         k.p_start = uint32_t(n);

@@ -43,6 +43,7 @@ struct MPConst
     double acoustic_cfl, advection_cfl, U_ref;
     int periodic;        // periodic flow in the box [lo, up] (sphx_mp_create_periodic)
     double lo[3], up[3];
+    double inv_gs;       // 1 / sub-cell spacing
 };
 using MPFluid = MPState;
 using MPLists = MPNeighbors;
@@ -77,7 +78,7 @@ __global__ void k_mp_from_fp64(size_t n, const double *__restrict__ pos, MPConst
         }
     }
     int c[3] = {0, 0, 0};
-    cell_index<D>(m, x, c);
+    sub_cell_index<D>(m, k.inv_gs, x, c);
 #pragma unroll
     for (int d = 0; d < D; ++d)
         noff[d * n + i] = float(x[d] - cell_corner(m, d, c[d]));
@@ -116,7 +117,7 @@ __global__ void k_mp_rehash(size_t n, const float4 *__restrict__ geo0, const flo
         }
     }
     int c[3] = {0, 0, 0};
-    cell_index<D>(m, x, c);
+    sub_cell_index<D>(m, k.inv_gs, x, c);
 #pragma unroll
     for (int d = 0; d < D; ++d)
         noff[d * n + i] = float(x[d] - cell_corner(m, d, c[d]));
@@ -905,6 +906,7 @@ extern "C" int sphx_mp_create(sphx_relation inner, sphx_relation wall, const sph
     mp->ncells = nc;
     MPConst &k = mp->k;
     k.m = mesh_dev(mesh);
+    k.inv_gs = 1.0 / mesh.grid_spacing;
     double wm = wmass.empty() ? 0.0 : wmass[0];
     for (int d = 0; d < 3; ++d)
         k.gd[d] = d < D ? gravity[d] : 0.0;
@@ -1045,6 +1047,7 @@ extern "C" int sphx_mp_create_periodic(sphx_body fb, const sphx_fluid_params *p,
     mp->ncells = nc;
     MPConst &k = mp->k;
     k.m = mesh_dev(mesh);
+    k.inv_gs = 1.0 / mesh.grid_spacing;
     k.periodic = 1;
     for (int d = 0; d < 3; ++d)
     {

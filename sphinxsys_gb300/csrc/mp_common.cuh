@@ -53,6 +53,22 @@ struct CellLanes
                                                (uint32_t(kCellBias) << 20));
 };
 
+// Sub-cell of a position for the mixed solvers: floor((x - lower) * (1 / gs)) clamped as
+// cell_index clamps.  The product replaces cell_index's FP64 division (three divisions per
+// particle were most of the re-hash on the slow FP64 pipe); a position within rounding of
+// a cell face may land in the neighbouring cell, whose offset then lies within rounding of
+// 0 or gs, which the search reach covers.
+template <int D>
+__device__ __forceinline__ void sub_cell_index(const MeshDev &m, double inv_gs, const double *x, int *c)
+{
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+    {
+        double f = floor((x[a] - m.lower[a]) * inv_gs);
+        c[a] = f < 0.0 ? 0 : (f > double(m.grid_points[a] - 2) ? m.grid_points[a] - 2 : int(f));
+    }
+}
+
 template <int D>
 __host__ __device__ __forceinline__ uint32_t pack_cell(const int *c)
 {
