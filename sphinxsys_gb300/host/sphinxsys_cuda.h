@@ -11,8 +11,17 @@
 // InteractionWithUpdate<fluid_dynamics::DensitySummationComplexFreeSurface>,
 // ReduceDynamics<fluid_dynamics::AdvectionTimeStep / AcousticTimeStep>,
 // SimpleDynamics<GravityForce<Gravity>>, SimpleDynamics<NormalDirectionFromBodyShape>,
-// ParticleSorting.  Output classes (VTP, restart, regression databases) are not part of
-// this layer; ObservedQuantity / TotalMechanicalEnergy return their values instead.
+// ParticleSorting; and for the periodic viscous flow of
+// tests/2d_examples/test_2d_taylor_green/taylor_green.cpp: addMaterialProperty<Viscosity>,
+// PeriodicAlongAxis / PeriodicConditionUsingCellLinkedList,
+// Dynamics1Level<fluid_dynamics::Integration1stHalfInnerRiemann / 2ndHalfInnerNoRiemann>,
+// InteractionWithUpdate<fluid_dynamics::DensitySummationInner / ViscousForceInner /
+// TransportVelocityCorrectionInner<TruncatedLinear, AllParticles>>,
+// ReduceDynamics<fluid_dynamics::AdvectionViscousTimeStep>, and an initial condition
+// through SimpleDynamics<T> for a T with a static velocity(position) (run once, on the
+// host).  Output classes (VTP, restart, regression databases) are not part of this layer;
+// ObservedQuantity / TotalMechanicalEnergy / TotalKineticEnergy / MaximumSpeed return
+// their values instead.
 //
 // Errors: a failing C-ABI call throws SPH::SphxException carrying the status and the
 // library message (the reference prints and calls exit(1)).
@@ -21,6 +30,7 @@
 // reference builds its 2D and 3D libraries separately.
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -260,6 +270,14 @@ struct BaseParticles
 struct ObserverParticles
 {
 };
+class Viscosity
+{
+  public:
+    Real mu_;
+    explicit Viscosity(Real mu) : mu_(mu) {}
+    Real ReferenceViscosity() const { return mu_; }
+};
+
 struct Lattice
 {
 };
@@ -310,7 +328,7 @@ class SPHBody
     SPHSystem &system_;
     std::shared_ptr<Shape> shape_;
     std::string name_;
-    Real h_, rho0_ = 1.0, c0_ = 0.0;
+    Real h_, rho0_ = 1.0, c0_ = 0.0, mu_ = 0.0;
     bool is_fluid_ = false;
     sphx_body body_ = nullptr;
     size_t n_ = 0;
@@ -338,6 +356,15 @@ class SPHBody
             is_fluid_ = true;
         }
     }
+    // addMaterialProperty<Viscosity>(mu)
+    template <class Property, typename... Args>
+    void addMaterialProperty(Args &&...args)
+    {
+        Property prop(std::forward<Args>(args)...);
+        mu_ = prop.ReferenceViscosity();
+    }
+    // the bounds of the system domain (the bodies of the supported drivers fill it)
+    BoundingBoxd getSPHBodyBounds() const { return system_.bounds_; }
     Real CutOffRadius() const { return 2.0 * h_; }
     size_t TotalRealParticles() const { return n_; }
 
@@ -535,7 +562,32 @@ struct AcousticTimeStep
 struct AdvectionTimeStep
 {
 };
+struct Integration1stHalfInnerRiemann
+{
+};
+struct Integration2ndHalfInnerNoRiemann
+{
+};
+struct DensitySummationInner
+{
+};
+struct ViscousForceInner
+{
+};
+template <class LimiterType, class ParticleScope>
+struct TransportVelocityCorrectionInner
+{
+};
+struct AdvectionViscousTimeStep
+{
+};
 } // namespace fluid_dynamics
+struct TruncatedLinear
+{
+};
+struct AllParticles
+{
+};
 template <class GravityType>
 struct GravityForce
 {
@@ -567,39 +619,84 @@ template <class LocalDynamicsType, class ExecutionPolicy = execution::CudaDevice
 class Dynamics1Level
 {
     static_assert(std::is_same<ExecutionPolicy, execution::CudaDevicePolicy>::value, "CUDA policy only");
+    static constexpr bool first =
+        std::is_same<LocalDynamicsType, fluid_dynamics::Integration1stHalfWithWallRiemann>::value ||
+        std::is_same<LocalDynamicsType, fluid_dynamics::Integration1stHalfInnerRiemann>::value;
+    static constexpr bool second =
+        std::is_same<LocalDynamicsType, fluid_dynamics::Integration2ndHalfWithWallRiemann>::value ||
+        std::is_same<LocalDynamicsType, fluid_dynamics::Integration2ndHalfInnerNoRiemann>::value;
+    static_assert(first || second, "unsupported Dynamics1Level type");
     InnerRelation &inner_;
-    ContactRelation &contact_;
+    ContactRelation *contact_;
     sphx_fluid_params p_;
 
   public:
     Dynamics1Level(InnerRelation &inner, ContactRelation &contact)
-        : inner_(inner), contact_(contact), p_(fluidParams(inner.getSPHBody())) {}
+        : inner_(inner), contact_(&contact), p_(fluidParams(inner.getSPHBody())) {}
+    // the inner-only forms (Integration1stHalfInnerRiemann, Integration2ndHalfInnerNoRiemann:
+    // NoRiemannSolver is the acoustic solver with limiter slope 0, its pressure dissipation
+    // vanishes)
+    explicit Dynamics1Level(InnerRelation &inner)
+        : inner_(inner), contact_(nullptr), p_(fluidParams(inner.getSPHBody()))
+    {
+        if (std::is_same<LocalDynamicsType, fluid_dynamics::Integration2ndHalfInnerNoRiemann>::value)
+            p_.limiter_slope = 0.0;
+    }
     void exec(Real dt = 0.0)
     {
-        if constexpr (std::is_same<LocalDynamicsType, fluid_dynamics::Integration1stHalfWithWallRiemann>::value)
-            check(sphx_integration_1st_half_with_wall_riemann(inner_.rel_, contact_.rel_, &p_, dt));
+        sphx_relation wall = contact_ ? contact_->rel_ : nullptr;
+        if constexpr (first)
+            check(sphx_integration_1st_half_with_wall_riemann(inner_.rel_, wall, &p_, dt));
         else
-        {
-            static_assert(std::is_same<LocalDynamicsType, fluid_dynamics::Integration2ndHalfWithWallRiemann>::value,
-                          "unsupported Dynamics1Level type");
-            check(sphx_integration_2nd_half_with_wall_riemann(inner_.rel_, contact_.rel_, &p_, dt));
-        }
+            check(sphx_integration_2nd_half_with_wall_riemann(inner_.rel_, wall, &p_, dt));
     }
+};
+
+template <class T>
+struct IsTransportVelocityCorrection : std::false_type
+{
+};
+template <class L, class S>
+struct IsTransportVelocityCorrection<fluid_dynamics::TransportVelocityCorrectionInner<L, S>> : std::true_type
+{
 };
 
 template <class LocalDynamicsType, class ExecutionPolicy = execution::CudaDevicePolicy>
 class InteractionWithUpdate
 {
-    static_assert(std::is_same<LocalDynamicsType, fluid_dynamics::DensitySummationComplexFreeSurface>::value,
-                  "unsupported interaction");
+    static constexpr bool complex =
+        std::is_same<LocalDynamicsType, fluid_dynamics::DensitySummationComplexFreeSurface>::value;
+    static constexpr bool inner_sum = std::is_same<LocalDynamicsType, fluid_dynamics::DensitySummationInner>::value;
+    static constexpr bool viscous = std::is_same<LocalDynamicsType, fluid_dynamics::ViscousForceInner>::value;
+    static constexpr bool tvc = IsTransportVelocityCorrection<LocalDynamicsType>::value;
+    static_assert(complex || inner_sum || viscous || tvc, "unsupported interaction");
     InnerRelation &inner_;
-    ContactRelation &contact_;
+    ContactRelation *contact_;
     sphx_fluid_params p_;
+    Real coefficient_ = 0.2;
 
   public:
     InteractionWithUpdate(InnerRelation &inner, ContactRelation &contact)
-        : inner_(inner), contact_(contact), p_(fluidParams(inner.getSPHBody())) {}
-    void exec(Real = 0.0) { check(sphx_density_summation_complex_free_surface(inner_.rel_, contact_.rel_, &p_)); }
+        : inner_(inner), contact_(&contact), p_(fluidParams(inner.getSPHBody())) {}
+    // inner forms; TransportVelocityCorrectionInner takes the correction coefficient (0.2)
+    explicit InteractionWithUpdate(InnerRelation &inner, Real coefficient = 0.2)
+        : inner_(inner), contact_(nullptr), p_(fluidParams(inner.getSPHBody())), coefficient_(coefficient)
+    {
+        if constexpr (viscous)
+            check(sphx_relation_keep_distances(inner.rel_)); // the viscous force needs r_ij
+    }
+    void exec(Real = 0.0)
+    {
+        if constexpr (complex)
+            check(sphx_density_summation_complex_free_surface(inner_.rel_, contact_ ? contact_->rel_ : nullptr,
+                                                              &p_));
+        else if constexpr (inner_sum)
+            check(sphx_density_summation_inner(inner_.rel_, &p_));
+        else if constexpr (viscous)
+            check(sphx_viscous_force_inner(inner_.rel_, inner_.getSPHBody().mu_));
+        else
+            check(sphx_transport_velocity_correction_inner(inner_.rel_, coefficient_));
+    }
 };
 
 template <class LocalDynamicsType, class ExecutionPolicy = execution::CudaDevicePolicy>
@@ -609,7 +706,12 @@ class ReduceDynamics
     sphx_fluid_params p_;
 
   public:
-    explicit ReduceDynamics(SPHBody &body, Real U_ref = 0.0) : body_(body), p_(fluidParams(body, U_ref)) {}
+    explicit ReduceDynamics(SPHBody &body, Real U_ref = 0.0) : body_(body), p_(fluidParams(body, U_ref))
+    {
+        // AdvectionViscousTimeStep: reference speed max(U_ref, mu / rho0 / h) (fluid_time_step.cpp:67-74)
+        if (std::is_same<LocalDynamicsType, fluid_dynamics::AdvectionViscousTimeStep>::value)
+            p_.U_ref = std::max(U_ref, body.mu_ / body.rho0_ / body.h_);
+    }
     Real exec(Real = 0.0)
     {
         Real dt;
@@ -619,6 +721,15 @@ class ReduceDynamics
             check(sphx_advection_time_step(body_.body_, &p_, &dt));
         return dt;
     }
+};
+
+template <class T, class = void>
+struct HasVelocityField : std::false_type
+{
+};
+template <class T>
+struct HasVelocityField<T, decltype(void(T::velocity(Vecd())))> : std::true_type
+{
 };
 
 template <class LocalDynamicsType, class ExecutionPolicy = execution::CudaDevicePolicy>
@@ -632,7 +743,22 @@ class SimpleDynamics
     SimpleDynamics(SPHBody &body, const Gravity &g) : body_(body), g_(g.g_) {}
     void exec(Real = 0.0)
     {
-        if constexpr (std::is_same<LocalDynamicsType, NormalDirectionFromBodyShape>::value)
+        if constexpr (HasVelocityField<LocalDynamicsType>::value)
+        {
+            // an initial condition: Velocity from the current Position, on the host
+            std::vector<double> x = body_.download("Position"), v(body_.n_ * Dimensions);
+            for (size_t i = 0; i < body_.n_; ++i)
+            {
+                Vecd p;
+                for (int a = 0; a < Dimensions; ++a)
+                    p[a] = x[i * Dimensions + a];
+                Vecd u = LocalDynamicsType::velocity(p);
+                for (int a = 0; a < Dimensions; ++a)
+                    v[i * Dimensions + a] = u[a];
+            }
+            body_.upload("Velocity", v, Dimensions);
+        }
+        else if constexpr (std::is_same<LocalDynamicsType, NormalDirectionFromBodyShape>::value)
         {
             std::vector<double> n(body_.n_ * Dimensions);
             for (size_t i = 0; i < body_.n_; ++i)
@@ -671,6 +797,69 @@ class ObservedQuantity
         if (!out.empty())
             check(sphx_observe_quantity(contact_.rel_, name_.c_str(), out.data()));
         return out;
+    }
+};
+
+// ------------------------------------------------------------------ periodic boundaries
+constexpr int xAxis = 0, yAxis = 1, zAxis = 2;
+
+struct PeriodicAlongAxis
+{
+    Real lower_, upper_;
+    int axis_;
+    PeriodicAlongAxis(const BoundingBoxd &bounds, int axis)
+        : lower_(bounds.lower_[axis]), upper_(bounds.upper_[axis]), axis_(axis) {}
+};
+
+// PeriodicConditionUsingCellLinkedList (domain_bounding.h:149-176): bounding_ wraps the
+// positions; the images of update_cell_linked_list_ are inserted by every later update of
+// the body's cell list once the axis is registered, so its exec() has nothing left to do.
+class PeriodicConditionUsingCellLinkedList
+{
+  public:
+    struct Bounding
+    {
+        RealBody &body_;
+        PeriodicAlongAxis axis_;
+        void exec(Real = 0.0) { check(sphx_periodic_bounding(body_.body_, axis_.axis_, axis_.lower_, axis_.upper_)); }
+    } bounding_;
+    struct UpdateCellLinkedList
+    {
+        void exec(Real = 0.0) {}
+    } update_cell_linked_list_;
+    PeriodicConditionUsingCellLinkedList(RealBody &body, PeriodicAlongAxis &periodic) : bounding_{body, periodic}
+    {
+        check(sphx_cell_list_set_periodic(body.cellLinkedList(), periodic.axis_, periodic.lower_, periodic.upper_,
+                                          body.CutOffRadius()));
+    }
+};
+
+class TotalKineticEnergy
+{
+    SPHBody &body_;
+
+  public:
+    explicit TotalKineticEnergy(SPHBody &body) : body_(body) {}
+    Real exec()
+    {
+        Real e;
+        double g[3] = {0, 0, 0};
+        check(sphx_total_mechanical_energy(body_.body_, g, &e));
+        return e;
+    }
+};
+
+class MaximumSpeed
+{
+    SPHBody &body_;
+
+  public:
+    explicit MaximumSpeed(SPHBody &body) : body_(body) {}
+    Real exec()
+    {
+        Real v;
+        check(sphx_maximum_speed(body_.body_, &v));
+        return v;
     }
 };
 

@@ -12,18 +12,19 @@ from sphinxsys_gb300 import build, cases
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def compile_example(tmp_path):
+def compile_example(tmp_path, name="dambreak_2d"):
     lib = build.build()
-    exe = str(tmp_path / "dambreak_2d")
-    cmd = ["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "sphinxsys_gb300", "host"),
-           os.path.join(ROOT, "examples", "dambreak_2d.cpp"), "-o", exe, "-L", os.path.dirname(lib), "-lsphx_cuda",
+    exe = str(tmp_path / name)
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "sphinxsys_gb300", "host"),
+           os.path.join(ROOT, "examples", name + ".cpp"), "-o", exe, "-L", os.path.dirname(lib), "-lsphx_cuda",
            f"-Wl,-rpath,{os.path.dirname(lib)}"]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     return exe
 
 
-def test_example_compiles(tmp_path):
-    assert os.path.exists(compile_example(tmp_path))
+@pytest.mark.parametrize("name", ["dambreak_2d", "taylor_green_2d"])
+def test_example_compiles(tmp_path, name):
+    assert os.path.exists(compile_example(tmp_path, name))
 
 
 @pytest.mark.gpu
@@ -51,3 +52,21 @@ def test_cpp_driver_matches_oracle(tmp_path):
     final = [r for r in rows if r[0] == "final"][0]
     assert int(final[1]) == iters
     assert abs(float(final[4]) / oc.total_mechanical_energy() - 1) < 1e-10
+
+
+@pytest.mark.gpu
+def test_cpp_taylor_green_matches_oracle(tmp_path):
+    """examples/taylor_green_2d.cpp (taylor_green.cpp's call sites) at 50 x 50 for 40
+    advection steps against the oracle: same physical time, kinetic energy within 1e-10."""
+    exe = compile_example(tmp_path, "taylor_green_2d")
+    steps = 40
+    res = subprocess.run([exe, "5", str(steps), "50"], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    final = [ln.split() for ln in res.stdout.split("\n") if ln.startswith("final")][0]
+    o = O.OracleTGV(cases.taylor_green_2d(50))
+    for _ in range(steps):
+        o.advection_step()
+    assert int(final[1]) == steps
+    assert abs(float(final[2]) / o.physical_time.value - 1) < 1e-12
+    assert abs(float(final[3]) / o.kinetic_energy() - 1) < 1e-10
+    assert abs(float(final[4]) / o.maximum_speed() - 1) < 1e-10
