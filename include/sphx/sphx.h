@@ -240,6 +240,12 @@ int sphx_maximum_speed(sphx_body body, double *out);
 /* CompressionSummation<Inner, Contact> + DensityRegularization<FreeSurface>
  * (density_regularization.hpp:40-118). */
 int sphx_ck_density_regularization(sphx_relation inner, sphx_relation wall_contact, const sphx_fluid_params *p);
+/* The two parts of the above as separate dynamics (the 3D SYCL driver constructs them
+ * separately): InteractionDynamicsCK<CompressionSummation<Inner<>, Contact<>>> writes
+ * CompressionSummation; StateDynamics<DensityRegularization<SPHBody, WeaklyCompressibleFluid,
+ * FreeSurface>> sets Compression = max(CompressionSummation, 1) and Density. */
+int sphx_ck_compression_summation(sphx_relation inner, sphx_relation wall_contact);
+int sphx_ck_free_surface_regularization(sphx_body fluid, double rho0);
 /* AdvectionStepSetup (fluid_time_step_ck.h:145-149): Vol = m / rho, Displacement = 0. */
 int sphx_ck_advection_step_setup(sphx_body fluid);
 /* UpdateParticlePosition (fluid_time_step_ck.h:173-176): Position += Displacement. */

@@ -180,8 +180,11 @@ __device__ __forceinline__ double p_jump(const CKParams &c, double u)
 }
 
 // ---------------------------------------------------------------- kernels
-template <int D>
-__global__ void k_ck_regularization(size_t n, CKFluid f, CKWall w, Lists in, Lists wl, TabK t, double rho0)
+// CompressionSummation<Inner, Contact> and, with REGULARIZE, the post-state
+// DensityRegularization<FreeSurface> in the same pass.
+template <int D, bool REGULARIZE>
+__device__ __forceinline__ void ck_summation(size_t n, const CKFluid &f, const CKWall &w, const Lists &in,
+                                             const Lists &wl, const TabK &t, double rho0)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -206,7 +209,35 @@ __global__ void k_ck_regularization(size_t n, CKFluid f, CKWall w, Lists in, Lis
         }
     }
     f.csum[i] = sum;
-    double comp = fmax(sum, 1.0);
+    if (REGULARIZE)
+    {
+        double comp = fmax(sum, 1.0);
+        f.compression[i] = comp;
+        f.rho[i] = comp * rho0;
+    }
+}
+
+template <int D>
+__global__ void k_ck_regularization(size_t n, CKFluid f, CKWall w, Lists in, Lists wl, TabK t, double rho0)
+{
+    ck_summation<D, true>(n, f, w, in, wl, t, rho0);
+}
+
+template <int D>
+__global__ void k_ck_compression_summation(size_t n, CKFluid f, CKWall w, Lists in, Lists wl, TabK t, double rho0)
+{
+    ck_summation<D, false>(n, f, w, in, wl, t, rho0);
+}
+
+// DensityRegularization<SPHBody, WeaklyCompressibleFluid, FreeSurface> alone
+// (density_regularization.h:164-180): compression = max(CompressionSummation, 1).
+template <int D>
+__global__ void k_ck_free_surface_regularization(size_t n, CKFluid f, double rho0)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    double comp = fmax(f.csum[i], 1.0);
     f.compression[i] = comp;
     f.rho[i] = comp * rho0;
 }
@@ -760,6 +791,34 @@ extern "C" int sphx_ck_density_regularization(sphx_relation inner, sphx_relation
         return SPHX_OK;
     CK_DISPATCH(b, k_ck_regularization, grid_for(n, kBlock), n, f, w, lists_of(inner), lists_of(wall),
                 make_tab(b->dim, inner->h), p->rho0);
+    return SPHX_OK;
+}
+
+extern "C" int sphx_ck_compression_summation(sphx_relation inner, sphx_relation wall)
+{
+    SPHX_TRY(ck_check(inner, wall));
+    sphx_body b = inner->src;
+    CKFluid f;
+    CKWall w;
+    SPHX_TRY(ck_fluid(b, f));
+    SPHX_TRY(ck_wall(wall, w));
+    size_t n = b->n;
+    if (n == 0)
+        return SPHX_OK;
+    CK_DISPATCH(b, k_ck_compression_summation, grid_for(n, kBlock), n, f, w, lists_of(inner), lists_of(wall),
+                make_tab(b->dim, inner->h), 0.0);
+    return SPHX_OK;
+}
+
+extern "C" int sphx_ck_free_surface_regularization(sphx_body b, double rho0)
+{
+    if (!b)
+        return fail(SPHX_ERR_INVALID_ARG, "null body");
+    CKFluid f;
+    SPHX_TRY(ck_fluid(b, f));
+    if (b->n == 0)
+        return SPHX_OK;
+    CK_DISPATCH(b, k_ck_free_surface_regularization, grid_for(b->n, kBlock), b->n, f, rho0);
     return SPHX_OK;
 }
 

@@ -310,6 +310,21 @@ class SPHSystem
     void handleCommandlineOptions(int, char *[]) {}
     inline void initializeSystemCellLinkedLists();
     inline void initializeSystemConfigurations();
+    // SingleVariable<Real> of the CK drivers: getValue / incrementValue over PhysicalTime
+    template <typename T>
+    struct SingleVariable
+    {
+        T *value_;
+        T getValue() const { return *value_; }
+        void incrementValue(T dt) { *value_ += dt; }
+    };
+    template <typename T>
+    SingleVariable<T> *getSystemVariableByName(const std::string &name)
+    {
+        single_time_.value_ = getSystemVariableDataByName<T>(name);
+        return &single_time_;
+    }
+    SingleVariable<Real> single_time_{nullptr};
     template <typename T>
     T *getSystemVariableDataByName(const std::string &name)
     {
@@ -860,6 +875,244 @@ class MaximumSpeed
         Real v;
         check(sphx_maximum_speed(body_.body_, &v));
         return v;
+    }
+};
+
+// ------------------------------------------------------------------ CK call sites
+// The computing-kernel forms of the tests_sycl drivers
+// (tests/tests_sycl/3d_examples/test_3d_dambreak_sycl/dambreak.cpp:97-148):
+// Inner<> / Contact<> relations, UpdateCellLinkedList / UpdateRelation / ParticleSortCK,
+// StateDynamics, InteractionDynamicsCK and ReduceDynamicsCK templated on the execution
+// policy, each exec() one call of the sphx_ck_* ABI.
+template <typename... Parameters>
+class Inner : public InnerRelation
+{
+  public:
+    using InnerRelation::InnerRelation;
+};
+template <typename... Parameters>
+class Contact : public ContactRelation
+{
+  public:
+    using ContactRelation::ContactRelation;
+};
+
+template <class ExecutionPolicy, class BodyType>
+class UpdateCellLinkedList
+{
+    RealBody &body_;
+
+  public:
+    explicit UpdateCellLinkedList(RealBody &body) : body_(body) {}
+    void exec(Real = 0.0) { body_.updateCellLinkedList(); }
+};
+
+template <class ExecutionPolicy, class... RelationTypes>
+class UpdateRelation
+{
+    std::vector<BaseRelation *> relations_;
+
+  public:
+    template <class... Relations>
+    explicit UpdateRelation(Relations &...relations) : relations_{&relations...} {}
+    void exec(Real = 0.0)
+    {
+        for (BaseRelation *r : relations_)
+            r->updateConfiguration();
+    }
+};
+
+// ParticleSortCK: Morton order of the cell-linked-list mesh; every registered variable is
+// permuted (the CK state included), relations must be updated afterwards as the driver does
+template <class ExecutionPolicy>
+class ParticleSortCK
+{
+    RealBody &body_;
+
+  public:
+    explicit ParticleSortCK(RealBody &body) : body_(body) {}
+    void exec(Real = 0.0) { check(sphx_particle_sorting(body_.body_, &body_.mesh_)); }
+};
+
+template <class GravityType>
+struct GravityForceCK
+{
+};
+struct NormalFromBodyShapeCK
+{
+};
+struct LinearCorrectionMatrixComplex
+{
+};
+struct FreeSurface
+{
+};
+namespace fluid_dynamics
+{
+struct AdvectionStepSetup
+{
+};
+struct UpdateParticlePosition
+{
+};
+template <class... Relations>
+struct CompressionSummation
+{
+};
+template <class BodyType, class FluidType, class FlowType>
+struct DensityRegularization
+{
+};
+struct AcousticStep1stHalfWithWallRiemannCorrectionCK
+{
+};
+struct AcousticStep2ndHalfWithWallRiemannCorrectionCK
+{
+};
+struct FreeSurfaceIndicationComplexSpatialTemporalCK
+{
+};
+struct AdvectionTimeStepCK
+{
+};
+template <class FluidType>
+struct AcousticTimeStepCK
+{
+};
+} // namespace fluid_dynamics
+
+template <class T>
+struct IsCompressionSummation : std::false_type
+{
+};
+template <class... R>
+struct IsCompressionSummation<fluid_dynamics::CompressionSummation<R...>> : std::true_type
+{
+};
+template <class T>
+struct IsDensityRegularization : std::false_type
+{
+};
+template <class B, class F, class W>
+struct IsDensityRegularization<fluid_dynamics::DensityRegularization<B, F, W>> : std::true_type
+{
+};
+template <class T>
+struct IsAcousticTimeStepCK : std::false_type
+{
+};
+template <class F>
+struct IsAcousticTimeStepCK<fluid_dynamics::AcousticTimeStepCK<F>> : std::true_type
+{
+};
+
+// DynamicsArgs(relation, parameter): a relation with its constructor argument
+struct DynamicsArgs
+{
+    InnerRelation &inner_;
+    Real value_;
+    DynamicsArgs(InnerRelation &inner, Real value) : inner_(inner), value_(value) {}
+};
+
+template <class ExecutionPolicy, class DynamicsType>
+class StateDynamics
+{
+    SPHBody &body_;
+    Vecd g_;
+
+  public:
+    explicit StateDynamics(SPHBody &body) : body_(body) {}
+    StateDynamics(SPHBody &body, const Gravity &g) : body_(body), g_(g.g_) {}
+    void exec(Real = 0.0)
+    {
+        if constexpr (std::is_same<DynamicsType, GravityForceCK<Gravity>>::value)
+            check(sphx_gravity_force(body_.body_, g_.v));
+        else if constexpr (std::is_same<DynamicsType, NormalFromBodyShapeCK>::value)
+            SimpleDynamics<NormalDirectionFromBodyShape>(body_).exec();
+        else if constexpr (std::is_same<DynamicsType, fluid_dynamics::AdvectionStepSetup>::value)
+            check(sphx_ck_advection_step_setup(body_.body_));
+        else if constexpr (std::is_same<DynamicsType, fluid_dynamics::UpdateParticlePosition>::value)
+            check(sphx_ck_update_particle_position(body_.body_));
+        else
+        {
+            static_assert(IsDensityRegularization<DynamicsType>::value, "unsupported state dynamics");
+            check(sphx_ck_free_surface_regularization(body_.body_, body_.rho0_));
+        }
+    }
+};
+
+template <class ExecutionPolicy, class DynamicsType>
+class InteractionDynamicsCK
+{
+    InnerRelation &inner_;
+    ContactRelation &contact_;
+    sphx_fluid_params p_;
+    Real alpha_ = 0.5;
+
+  public:
+    InteractionDynamicsCK(InnerRelation &inner, ContactRelation &contact)
+        : inner_(inner), contact_(contact), p_(fluidParams(inner.getSPHBody())) {}
+    InteractionDynamicsCK(DynamicsArgs args, ContactRelation &contact)
+        : inner_(args.inner_), contact_(contact), p_(fluidParams(args.inner_.getSPHBody())), alpha_(args.value_) {}
+    void exec(Real dt = 0.0)
+    {
+        if constexpr (std::is_same<DynamicsType, LinearCorrectionMatrixComplex>::value)
+            check(sphx_ck_linear_correction_matrix(inner_.rel_, contact_.rel_, alpha_));
+        else if constexpr (std::is_same<DynamicsType,
+                                        fluid_dynamics::AcousticStep1stHalfWithWallRiemannCorrectionCK>::value)
+            check(sphx_ck_acoustic_step_1st_half(inner_.rel_, contact_.rel_, &p_, dt));
+        else if constexpr (std::is_same<DynamicsType,
+                                        fluid_dynamics::AcousticStep2ndHalfWithWallRiemannCorrectionCK>::value)
+            check(sphx_ck_acoustic_step_2nd_half(inner_.rel_, contact_.rel_, &p_, dt));
+        else if constexpr (std::is_same<DynamicsType,
+                                        fluid_dynamics::FreeSurfaceIndicationComplexSpatialTemporalCK>::value)
+            check(sphx_ck_free_surface_indication(inner_.rel_, contact_.rel_));
+        else
+        {
+            static_assert(IsCompressionSummation<DynamicsType>::value, "unsupported interaction dynamics");
+            check(sphx_ck_compression_summation(inner_.rel_, contact_.rel_));
+        }
+    }
+};
+
+template <class ExecutionPolicy, class DynamicsType>
+class ReduceDynamicsCK
+{
+    SPHBody &body_;
+    sphx_fluid_params p_;
+
+  public:
+    explicit ReduceDynamicsCK(SPHBody &body, Real U_ref = 0.0) : body_(body), p_(fluidParams(body, U_ref)) {}
+    Real exec(Real = 0.0)
+    {
+        Real dt;
+        if constexpr (IsAcousticTimeStepCK<DynamicsType>::value)
+            check(sphx_ck_acoustic_time_step(body_.body_, &p_, &dt));
+        else
+        {
+            static_assert(std::is_same<DynamicsType, fluid_dynamics::AdvectionTimeStepCK>::value,
+                          "unsupported reduce dynamics");
+            check(sphx_ck_advection_time_step(body_.body_, &p_, &dt));
+        }
+        return dt;
+    }
+};
+
+// ObservedQuantityRecording<MainExecutionPolicy, Real>(name, observer contact) of the CK
+// drivers: the tabulated-kernel interpolation with the current volumes, returned.
+class ObservedQuantityCK
+{
+    ContactRelation &contact_;
+    std::string name_;
+
+  public:
+    ObservedQuantityCK(const std::string &name, ContactRelation &contact) : contact_(contact), name_(name) {}
+    std::vector<Real> exec()
+    {
+        std::vector<Real> out(contact_.getSPHBody().n_);
+        if (!out.empty())
+            check(sphx_ck_observe_quantity(contact_.rel_, name_.c_str(), out.data()));
+        return out;
     }
 };
 

@@ -91,6 +91,8 @@ SIGNATURES = {
     "sphx_ck_advection_step_setup": (_i, [_vp]),
     "sphx_ck_update_particle_position": (_i, [_vp]),
     "sphx_ck_free_surface_indication": (_i, [_vp, _vp]),
+    "sphx_ck_compression_summation": (_i, [_vp, _vp]),
+    "sphx_ck_free_surface_regularization": (_i, [_vp, C.c_double]),
     "sphx_ck_linear_correction_matrix": (_i, [_vp, _vp, _d]),
     "sphx_ck_acoustic_step_1st_half": (_i, [_vp, _vp, C.POINTER(FluidParams), _d]),
     "sphx_ck_acoustic_step_2nd_half": (_i, [_vp, _vp, C.POINTER(FluidParams), _d]),

@@ -22,7 +22,7 @@ def compile_example(tmp_path, name="dambreak_2d"):
     return exe
 
 
-@pytest.mark.parametrize("name", ["dambreak_2d", "taylor_green_2d"])
+@pytest.mark.parametrize("name", ["dambreak_2d", "taylor_green_2d", "dambreak_sycl_3d"])
 def test_example_compiles(tmp_path, name):
     assert os.path.exists(compile_example(tmp_path, name))
 
@@ -70,3 +70,26 @@ def test_cpp_taylor_green_matches_oracle(tmp_path):
     assert abs(float(final[2]) / o.physical_time.value - 1) < 1e-12
     assert abs(float(final[3]) / o.kinetic_energy() - 1) < 1e-10
     assert abs(float(final[4]) / o.maximum_speed() - 1) < 1e-10
+
+
+@pytest.mark.gpu
+def test_cpp_sycl_3d_driver_matches_oracle(tmp_path):
+    """examples/dambreak_sycl_3d.cpp (the 3D SYCL driver's CK call sites on the CUDA
+    policy) for 110 advection steps, through the particle sort at step 100, against the
+    oracle's nested CK loop: same physical time, mechanical energy within 1e-10."""
+    exe = compile_example(tmp_path, "dambreak_sycl_3d")
+    steps = 110
+    res = subprocess.run([exe, "20", str(steps)], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    lines = [ln.split() for ln in res.stdout.split("\n") if ln]
+    probes = [ln for ln in lines if ln[0] == "probe"]
+    energy = [ln for ln in lines if ln[0] == "energy"]
+    assert len(probes) == steps + 1 and int(probes[-1][1]) == steps
+    oc = O.OracleCase(cases.dambreak_3d_reference())
+    assert abs(float(energy[0][3]) / oc.total_mechanical_energy() - 1) < 1e-12
+    for _ in range(steps):
+        oc.ck_nested_advection_step()
+    assert abs(float(probes[-1][2]) / oc.physical_time.value - 1) < 1e-12
+    assert int(energy[-1][1]) == steps
+    assert abs(float(energy[-1][3]) / oc.total_mechanical_energy() - 1) < 1e-10
+    np.testing.assert_allclose([float(v) for v in probes[-1][3:]], oc.ck_observe_pressure(), rtol=1e-8, atol=1e-10)
