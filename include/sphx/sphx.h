@@ -311,7 +311,9 @@ int sphx_mp_destroy(sphx_mp mp);
 /* One advection step.  loop_style 0: acoustic dt taken before each relaxation
  * (Dambreak.cpp:181-190); 1: after it (test_3d_dambreak/dambreak.cpp:193-201).
  * Outputs (any may be null): acoustic sub-steps taken, the advection dt used, and the
- * physical time after the step. */
+ * physical time after the step.  The configuration update for the moved positions
+ * (re-hash, re-sort, neighbour lists, density sums) runs at the start of the next step,
+ * or not at all when sphx_mp_upload replaces the state first. */
 int sphx_mp_advection_step(sphx_mp mp, int loop_style, int *substeps, double *advection_dt,
                            double *physical_time);
 /* Reloads the solver from the FP64 fluid body (Position, Velocity, Force, Density,

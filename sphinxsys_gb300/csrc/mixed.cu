@@ -88,9 +88,24 @@ __global__ void k_mp_from_fp64(size_t n, const double *__restrict__ pos, MPConst
     rank[i] = atomicAdd(&count[lc], 1u);
 }
 
-// From the current (cell, offset) state: FP64 reconstruction of the position.
-// A periodic flow wraps the position into its box first, as PeriodicBounding does at the
-// end of the advection step (domain_bounding.h:103-113).
+// FP64 reconstruction of a position from its (cell, offset) pair.  A periodic flow wraps
+// it into its box, as PeriodicBounding does at the end of the advection step
+// (domain_bounding.h:103-113); between the position update and the next re-hash the
+// offset may still point outside the box.
+__device__ __forceinline__ double reconstruct(const MPConst &k, int d, int cell, float offset)
+{
+    double x = cell_corner(k.m, d, cell) + double(offset);
+    if (k.periodic)
+    {
+        const double L = k.up[d] - k.lo[d];
+        if (x < k.lo[d])
+            x += L;
+        if (x > k.up[d])
+            x -= L;
+    }
+    return x;
+}
+
 template <int D>
 __global__ void k_mp_rehash(size_t n, const float4 *__restrict__ geo0, const float *__restrict__ off, MPConst k,
                             uint32_t *__restrict__ ncell, float *__restrict__ noff, uint32_t *__restrict__ key,
@@ -105,17 +120,7 @@ __global__ void k_mp_rehash(size_t n, const float4 *__restrict__ geo0, const flo
     double x[3] = {0, 0, 0};
 #pragma unroll
     for (int d = 0; d < D; ++d)
-    {
-        x[d] = cell_corner(m, d, c0[d]) + double(off[d * n + i]);
-        if (k.periodic)
-        {
-            const double L = k.up[d] - k.lo[d];
-            if (x[d] < k.lo[d])
-                x[d] += L;
-            if (x[d] > k.up[d])
-                x[d] -= L;
-        }
-    }
+        x[d] = reconstruct(k, d, c0[d], off[d * n + i]);
     int c[3] = {0, 0, 0};
     sub_cell_index<D>(m, k.inv_gs, x, c);
 #pragma unroll
@@ -330,7 +335,7 @@ __global__ void k_mp_import(size_t n, ImportArgs a, MPFluid f)
 // ---------------------------------------------------------------- outputs
 __device__ __forceinline__ double position(const MPConst &k, const MPFluid &f, size_t n, size_t i, int d, const int *c)
 {
-    return cell_corner(k.m, d, c[d]) + double(f.off[d * n + i]);
+    return reconstruct(k, d, c[d], f.off[d * n + i]);
 }
 
 template <int D>
@@ -491,6 +496,10 @@ struct sphx_mp_s
     unsigned long long *slots = nullptr; // 0 acoustic, 1 advection, 2 misc, 3 build counts
     unsigned long long *h_slots = nullptr;
     double physical_time = 0, acoustic_dt = 0;
+    // positions moved since the last configuration update: the re-hash, re-sort and list
+    // build run at the start of the next advection step, so that a caller who replaces
+    // the state between steps (sphx_mp_upload) pays for one configuration, not two
+    bool moved = false;
     int block = 128, strategy = 0;
     // optional CUDA-event timing of the two sweep kernels (sphx_mp_set_profiling)
     bool profiling = false;
@@ -650,6 +659,17 @@ int read_slot(sphx_mp mp, int slot, double *out)
     return SPHX_OK;
 }
 
+// The configuration update deferred from the end of the last advection step.
+int settle_configuration(sphx_mp mp)
+{
+    if (mp->moved)
+    {
+        SPHX_TRY(mp->dim == 2 ? configuration_update<2>(mp, true) : configuration_update<3>(mp, true));
+        mp->moved = false;
+    }
+    return SPHX_OK;
+}
+
 template <int D>
 int substep(sphx_mp mp, double dt)
 {
@@ -714,6 +734,7 @@ int substep(sphx_mp mp, double dt)
 template <int D>
 int advection_step(sphx_mp mp, int loop_style, int *substeps, double *adv_dt)
 {
+    SPHX_TRY(settle_configuration(mp));
     double adv_max;
     SPHX_TRY(read_slot(mp, 1, &adv_max));
     double Dt = mp->k.advection_cfl * mp->k.p.h / (std::max(std::sqrt(adv_max), mp->k.U_ref) + kTinyReal);
@@ -748,7 +769,7 @@ int advection_step(sphx_mp mp, int loop_style, int *substeps, double *adv_dt)
         ++count;
     }
     mp->acoustic_dt = dt;
-    SPHX_TRY(configuration_update<D>(mp, true));
+    mp->moved = true;
     if (substeps)
         *substeps = count;
     if (adv_dt)
@@ -834,6 +855,7 @@ int import_fluid(sphx_mp mp, sphx_body fb, double rho0, double c0)
         ctx->launches++;
     }
     SPHX_TRY(D == 2 ? configuration_update<2>(mp, false) : configuration_update<3>(mp, false));
+    mp->moved = false;
     return SPHX_OK;
 }
 } // namespace
@@ -1144,6 +1166,7 @@ extern "C" int sphx_mp_list_sizes(sphx_mp mp, uint64_t *out)
 {
     if (!mp || !out)
         return fail(SPHX_ERR_INVALID_ARG, "null argument");
+    SPHX_TRY(settle_configuration(mp));
     size_t n = mp->n;
     std::vector<uint32_t> a(n), b(n);
     if (n)
@@ -1224,6 +1247,7 @@ extern "C" int sphx_mp_autotune(sphx_mp mp, int reps, int *best_block, int *best
         return fail(SPHX_ERR_INVALID_ARG, "invalid autotune arguments");
     if (mp->n == 0)
         return SPHX_OK;
+    SPHX_TRY(settle_configuration(mp));
     double ac;
     SPHX_TRY(read_slot(mp, 0, &ac));
     double dt = mp->k.acoustic_cfl * mp->k.p.h / (ac + kTinyReal);

@@ -103,6 +103,34 @@ def test_upload_restores_downloaded_state():
         assert rel_err(b.fp64.water_block.download(name), a.fp64.water_block.download(name)) < 1e-5
 
 
+def test_configuration_update_deferred_to_next_step():
+    """The configuration for the moved positions is built at the start of the next step:
+    a download in between leaves the run bit for bit unchanged, and a step that follows an
+    upload (whose import already built the configuration) launches no second one."""
+    case = cases.dambreak_2d()
+    a = MixedPrecisionDamBreak(case)
+    b = MixedPrecisionDamBreak(case)
+    for _ in range(4):
+        a.advection_step()
+        b.advection_step()
+        b.sync_fp64()
+    a.sync_fp64()
+    for name in ("Position", "Velocity", "Density"):
+        assert np.array_equal(a.fp64.water_block.download(name), b.fp64.water_block.download(name)), name
+    ctx = a.ctx
+    n0 = ctx.launch_count()
+    s_plain, _ = a.advection_step()
+    plain = ctx.launch_count() - n0
+    a.sync_fp64()
+    a.upload(a.fp64.water_block)
+    n0 = ctx.launch_count()
+    s_up, _ = a.advection_step()
+    after_upload = ctx.launch_count() - n0
+    # same sub-step count: the launch difference is the configuration update alone
+    if s_plain == s_up:
+        assert after_upload < plain, (after_upload, plain)
+
+
 def test_autotune_keeps_state():
     case = cases.dambreak_2d()
     a = MixedPrecisionDamBreak(case)
