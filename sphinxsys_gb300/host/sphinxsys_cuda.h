@@ -307,7 +307,37 @@ class SPHSystem
     ~SPHSystem() { sphx_ctx_destroy(ctx_); }
     SPHSystem(const SPHSystem &) = delete;
     SPHSystem &operator=(const SPHSystem &) = delete;
-    void handleCommandlineOptions(int, char *[]) {}
+    // the options of SPHSystem::handleCommandlineOptions (sph_system.cpp:100-200) this policy
+    // uses: --restart_step=<int>, --regression=<bool>, --state_recording=<bool>
+    // ("--name=value" or "--name value"); the others are accepted and ignored
+    void handleCommandlineOptions(int ac, char *av[])
+    {
+        for (int i = 1; i < ac; ++i)
+        {
+            std::string arg(av[i]);
+            if (arg.rfind("--", 0) != 0)
+                continue;
+            std::string name = arg.substr(2), value;
+            size_t eq = name.find('=');
+            if (eq != std::string::npos)
+            {
+                value = name.substr(eq + 1);
+                name = name.substr(0, eq);
+            }
+            else if (i + 1 < ac && std::string(av[i + 1]).rfind("--", 0) != 0)
+                value = av[++i];
+            auto flag = [&value]() { return value == "1" || value == "true" || value == "True"; };
+            if (name == "restart_step")
+                restart_step_ = std::stoi(value);
+            else if (name == "regression")
+                generate_regression_data_ = flag();
+            else if (name == "state_recording")
+                state_recording_ = flag();
+        }
+    }
+    std::string input_folder_ = "./input", output_folder_ = "./output", restart_folder_ = "./restart";
+    int restart_step_ = 0;
+    bool generate_regression_data_ = false, state_recording_ = true;
     inline void initializeSystemCellLinkedLists();
     inline void initializeSystemConfigurations();
     // SingleVariable<Real> of the CK drivers: getValue / incrementValue over PhysicalTime
@@ -333,8 +363,9 @@ class SPHSystem
             throw SphxException(SPHX_ERR_NOT_FOUND, "unknown system variable " + name);
         return &physical_time_;
     }
-    int RestartStep() const { return 0; }
-    bool GenerateRegressionData() const { return false; }
+    int RestartStep() const { return restart_step_; }
+    bool GenerateRegressionData() const { return generate_regression_data_; }
+    bool StateRecording() const { return state_recording_; }
 };
 
 class SPHBody
@@ -959,7 +990,7 @@ template <class... Relations>
 struct CompressionSummation
 {
 };
-template <class BodyType, class FluidType, class FlowType>
+template <class... Parameters> // <SPHBody, WeaklyCompressibleFluid, FreeSurface>
 struct DensityRegularization
 {
 };
@@ -993,8 +1024,8 @@ template <class T>
 struct IsDensityRegularization : std::false_type
 {
 };
-template <class B, class F, class W>
-struct IsDensityRegularization<fluid_dynamics::DensityRegularization<B, F, W>> : std::true_type
+template <class... P>
+struct IsDensityRegularization<fluid_dynamics::DensityRegularization<P...>> : std::true_type
 {
 };
 template <class T>
@@ -1004,6 +1035,15 @@ struct IsAcousticTimeStepCK : std::false_type
 template <class F>
 struct IsAcousticTimeStepCK<fluid_dynamics::AcousticTimeStepCK<F>> : std::true_type
 {
+};
+
+// BaseDynamics<ReturnType>: what containers, triggers and the time stepper hold
+template <typename ReturnType>
+class BaseDynamics
+{
+  public:
+    virtual ~BaseDynamics() = default;
+    virtual ReturnType exec(Real dt = 0.0) = 0;
 };
 
 // DynamicsArgs(relation, parameter): a relation with its constructor argument
@@ -1076,14 +1116,14 @@ class InteractionDynamicsCK
 };
 
 template <class ExecutionPolicy, class DynamicsType>
-class ReduceDynamicsCK
+class ReduceDynamicsCK : public BaseDynamics<Real>
 {
     SPHBody &body_;
     sphx_fluid_params p_;
 
   public:
     explicit ReduceDynamicsCK(SPHBody &body, Real U_ref = 0.0) : body_(body), p_(fluidParams(body, U_ref)) {}
-    Real exec(Real = 0.0)
+    Real exec(Real = 0.0) override
     {
         Real dt;
         if constexpr (IsAcousticTimeStepCK<DynamicsType>::value)
@@ -1131,3 +1171,5 @@ class TotalMechanicalEnergy
     }
 };
 } // namespace SPH
+
+#include "sph_solver_cuda.h"
