@@ -63,13 +63,21 @@ class ClockSampler:
         self.tmp = None
 
     def start(self):
+        """Starts sampling every 50 ms and returns once the first sample is written (the
+        tool takes a while to start), so that the timed region that follows is covered."""
         try:
             self.tmp = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=self.tmp, stderr=subprocess.DEVNULL)
+                 "-lms", "50"], stdout=self.tmp, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+            if os.path.getsize(self.tmp.name) > 0:
+                break
+            time.sleep(0.01)
 
     def stop(self):
         if self.proc is None:
