@@ -79,6 +79,16 @@ __device__ __forceinline__ void instance_max(BRun *run, int b, bool lane_active,
 
 // ---------------------------------------------------------------- hashing and sorting
 template <int D>
+__device__ __forceinline__ void store_hash(const BInst &k, const int *c, uint32_t *ncell, size_t i, uint32_t *key,
+                                           uint32_t *rank, uint32_t *cnt)
+{
+    ncell[i] = pack_cell<D>(c);
+    uint32_t key_i = k.cell_base + linear_cell<D>(k.m, c);
+    key[i] = key_i;
+    rank[i] = atomicAdd(&cnt[key_i], 1u);
+}
+
+template <int D>
 __device__ __forceinline__ void hash_position(const BInst &k, const double *x, uint32_t *ncell, float *noff, size_t n,
                                               size_t i, uint32_t *key, uint32_t *rank, uint32_t *cnt)
 {
@@ -87,10 +97,7 @@ __device__ __forceinline__ void hash_position(const BInst &k, const double *x, u
 #pragma unroll
     for (int d = 0; d < D; ++d)
         noff[d * n + i] = float(x[d] - cell_corner(k.m, d, c[d]));
-    ncell[i] = pack_cell<D>(c);
-    uint32_t key_i = k.cell_base + linear_cell<D>(k.m, c);
-    key[i] = key_i;
-    rank[i] = atomicAdd(&cnt[key_i], 1u);
+    store_hash<D>(k, c, ncell, i, key, rank, cnt);
 }
 
 template <int D>
@@ -122,11 +129,16 @@ __global__ void k_b_rehash(size_t n, const float4 *__restrict__ geo0, const floa
     const BInst &k = inst[find_instance(starts, count, uint32_t(i))];
     int c0[3];
     unpack_cell<D>(__float_as_uint(geo0[i].w), c0);
-    double x[3] = {0, 0, 0};
+    float o[3] = {0.f, 0.f, 0.f}, no[3];
 #pragma unroll
     for (int d = 0; d < D; ++d)
-        x[d] = cell_corner(k.m, d, c0[d]) + double(off[d * n + i]);
-    hash_position<D>(k, x, ncell, noff, n, i, key, rank, cnt);
+        o[d] = off[d * n + i];
+    int c[3] = {0, 0, 0};
+    rehash_relative<D>(k.m, k.inv_gs, false, c0, o, c, no);
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        noff[d * n + i] = no[d];
+    store_hash<D>(k, c, ncell, i, key, rank, cnt);
 }
 
 __global__ void k_b_scatter(size_t n, const uint32_t *__restrict__ key, const uint32_t *__restrict__ rank,

@@ -117,15 +117,15 @@ __global__ void k_mp_rehash(size_t n, const float4 *__restrict__ geo0, const flo
     const MeshDev &m = k.m;
     int c0[3];
     unpack_cell<D>(__float_as_uint(geo0[i].w), c0);
-    double x[3] = {0, 0, 0};
+    float o[3] = {0.f, 0.f, 0.f}, no[3];
 #pragma unroll
     for (int d = 0; d < D; ++d)
-        x[d] = reconstruct(k, d, c0[d], off[d * n + i]);
+        o[d] = off[d * n + i];
     int c[3] = {0, 0, 0};
-    sub_cell_index<D>(m, k.inv_gs, x, c);
+    rehash_relative<D>(m, k.inv_gs, k.periodic != 0, c0, o, c, no);
 #pragma unroll
     for (int d = 0; d < D; ++d)
-        noff[d * n + i] = float(x[d] - cell_corner(m, d, c[d]));
+        noff[d * n + i] = no[d];
     ncell[i] = pack_cell<D>(c);
     uint32_t lc = linear_cell<D>(m, c);
     key[i] = lc;

@@ -69,6 +69,36 @@ __device__ __forceinline__ void sub_cell_index(const MeshDev &m, double inv_gs, 
     }
 }
 
+// New (cell, offset) of a particle that moved by its FP32 offset from the corner of cell c0
+// (the offset may lie outside that cell): k = floor(offset / gs) cells along each axis,
+// then the offset re-based to the new cell in FP64 and rounded once to FP32.  A periodic
+// box wraps the cell over its all_cells cells (the position moves by one period, the offset
+// stays); otherwise the cell is clamped to the mesh as sub_cell_index does.  In exact
+// arithmetic this equals the re-hash of the absolute position (corner + offset) with half
+// its FP64 operations, which run at 1/64 of the FP32 rate on GB300.
+template <int D>
+__device__ __forceinline__ void rehash_relative(const MeshDev &m, double inv_gs, bool periodic, const int *c0,
+                                                const float *offset, int *c, float *noff)
+{
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+    {
+        const double o = double(offset[a]);
+        const int k = int(floor(o * inv_gs));
+        const int ncell = m.all_cells[a];
+        int ca = c0[a] + k, shift = k;
+        if (periodic)
+            ca = ca < 0 ? ca + ncell : (ca >= ncell ? ca - ncell : ca);
+        else
+        {
+            ca = ca < 0 ? 0 : (ca > ncell - 1 ? ncell - 1 : ca);
+            shift = ca - c0[a];
+        }
+        c[a] = ca;
+        noff[a] = float(o - double(shift) * m.gs);
+    }
+}
+
 template <int D>
 __host__ __device__ __forceinline__ uint32_t pack_cell(const int *c)
 {
