@@ -2,8 +2,9 @@
 
 Headline workload: the 3D dam break of a 3.2 x 1.0 x 1.8 tank with a 1.2 x 1.0 x 0.6
 water block at dp = 0.006 (3,340,000 fluid particles, 2,456,600 wall particles), advanced
-by the mixed-precision solver (FP32 pair arithmetic with compensated sums, FP64 position
-integration, dt reductions and conservation sums), timed beside the FP64 path on the same
+by the mixed-precision solver (FP32 pair arithmetic with compensated sums on FP32
+positions relative to integer sub-cells; FP64 re-hash, dt reductions and conservation
+sums), timed beside the FP64 path on the same
 case from the same initial state, with the field / probe / free-surface errors of mixed
 against FP64.  The FP64 drop-in is also measured on dp = 0.0075 (1,702,400 fluid
 particles) through the reference-shaped API (``fp64_drop_in``), a seeded batch of 64
@@ -37,6 +38,7 @@ import time
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
+DTYPE_MIXED = "f32 pairs and cell-relative positions / f64 re-hash, dt, sums"
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s (1 GB300): mixed-prec vs FP64 at <=1e-4 rel err; %HBM roofline"
@@ -196,7 +198,6 @@ def mixed_leg(args, torch, local, world):
     # end to end through the public API: host FP64 state in, one advection step, state out
     e2e = None
     if args.e2e_steps > 0:
-        body = ref.water_block
         names = ("Position", "Velocity", "Force", "Density", "DensityChangeRate")
 
         def pinned_like(a):
@@ -204,8 +205,9 @@ def mixed_leg(args, torch, local, world):
             t[...] = a
             return t
 
-        # the caller's state lives in pinned host memory; each step uploads it, advances,
-        # and reads the results back into the same buffers
+        # the caller's state lives in pinned host memory; each step loads it
+        # (sphx_mp_upload_host), advances, and reads the results back into the same
+        # buffers (sphx_mp_download_host)
         host = {nm: pinned_like(mp.fp64_view(nm)) for nm in names}
         pressure = pinned_like(np.zeros(n))
         outs = {"Position": host["Position"], "Velocity": host["Velocity"], "Density": host["Density"],
@@ -216,17 +218,14 @@ def mixed_leg(args, torch, local, world):
         t0 = time.perf_counter()
         esubs = 0
         for _ in range(args.e2e_steps):
-            for nm in names:
-                body.upload(nm, host[nm])
-            mp.upload(body)
+            mp.upload_host(*(host[nm] for nm in names))
             s, _ = mp.advection_step()
             esubs += s
-            mp.download(body)
-            for nm, arr in outs.items():
-                body.download(nm, out=arr)
+            mp.download_host(outs["Position"], outs["Velocity"], outs["Density"], outs["Pressure"])
         e_el = time.perf_counter() - t0
         e2e = {"value": n * esubs / e_el * world, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h)}
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * e_el / args.e2e_steps,
+               "calls": "sphx_mp_upload_host, sphx_mp_advection_step, sphx_mp_download_host"}
     out = {
         "case": case, "n": n, "n_wall": ref.wall_boundary.n, "elapsed": el, "subs": subs, "launches": launches,
         "clocks": clocks, "roofline": roofline, "e2e": e2e, "tuning": tuned,
@@ -427,7 +426,7 @@ def taylor_green_leg(args, torch, local):
         fp64 = {"value": n * fsubs / fel, "ms_per_step": 1e3 * fel / fsteps, "steps": fsteps,
                 "ke_rel_err_mixed_vs_fp64": (abs(ke_mp / ke_fp[-1] - 1.0) if ke_mp is not None else None)}
         del ref
-    return {"workload": case.name, "n_fluid": n, "dtype": "f32 pairs / f64 integration", "value": n * subs / el,
+    return {"workload": case.name, "n_fluid": n, "dtype": DTYPE_MIXED, "value": n * subs / el,
             "unit": UNIT, "ms_per_step": 1e3 * el / args.tg_steps, "steps": args.tg_steps, "warmup": args.warmup,
             "acoustic_substeps": subs, "gpu_launches": int(launches), "tuning": tuned, "setup_s": setup_s,
             "kinetic_energy_decay": decay,
@@ -544,7 +543,7 @@ def main():
         line = {
             "metric": METRIC, "value": ps / el, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 pairs / f64 integration",
+            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE_MIXED,
             "data": "synthetic dam-break lattice",
             "config": {"workload": case.name, "n_fluid": mixed["n"], "n_wall": mixed["n_wall"], "dp": args.mp_dp,
                        "precision": "mixed", "acoustic_substeps": mixed["subs"], "l2": "inputs larger than L2",

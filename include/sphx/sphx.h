@@ -323,6 +323,18 @@ int sphx_mp_upload(sphx_mp mp, sphx_body fluid);
 /* Writes Position, Velocity, Density, Pressure, Force and DensityChangeRate back into the
  * FP64 fluid body, in the body's particle order (synchronises). */
 int sphx_mp_download(sphx_mp mp, sphx_body fluid);
+/* The same load as sphx_body_upload of each row followed by sphx_mp_upload, straight from
+ * host rows in the body's particle order (position and velocity and force n x dim,
+ * density and density change rate n; FP64; page-locked memory lets the copies run
+ * asynchronously): the positions are copied first, and the copies of the other rows
+ * overlap the re-sort and the neighbour search.  The FP64 body is not written.  Dam-break
+ * solvers only (a periodic solver: SPHX_ERR_INVALID_ARG).  No counterpart in the
+ * reference: the host state of a caller that keeps it in its own arrays (synchronises). */
+int sphx_mp_upload_host(sphx_mp mp, const double *position, const double *velocity, const double *force,
+                        const double *density, const double *density_change_rate);
+/* Position and velocity (n x dim), density and pressure (n) rows in the body's particle
+ * order, the values sphx_mp_download writes into the body (synchronises). */
+int sphx_mp_download_host(sphx_mp mp, double *position, double *velocity, double *density, double *pressure);
 /* FP64 conservation sums: out[0] total mass, out[1..3] momentum, out[4] mechanical energy
  * (kinetic + potential with gravity and zero reference at the origin). */
 int sphx_mp_conservation(sphx_mp mp, double *out);

@@ -53,11 +53,12 @@ struct MPWall : MPWallData
 };
 
 // ---------------------------------------------------------------- (re)hash + sort
-// From FP64 body positions (creation).
+// From FP64 positions: component d of particle i at pos[d * comp_stride + i * row_stride]
+// (the body's SoA layout, or host rows).
 template <int D>
-__global__ void k_mp_from_fp64(size_t n, const double *__restrict__ pos, MPConst k, uint32_t *__restrict__ ncell,
-                               float *__restrict__ noff, uint32_t *__restrict__ key, uint32_t *__restrict__ rank,
-                               uint32_t *__restrict__ count)
+__global__ void k_mp_from_fp64(size_t n, const double *__restrict__ pos, size_t comp_stride, size_t row_stride,
+                               MPConst k, uint32_t *__restrict__ ncell, float *__restrict__ noff,
+                               uint32_t *__restrict__ key, uint32_t *__restrict__ rank, uint32_t *__restrict__ count)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -67,7 +68,7 @@ __global__ void k_mp_from_fp64(size_t n, const double *__restrict__ pos, MPConst
 #pragma unroll
     for (int d = 0; d < D; ++d)
     {
-        x[d] = pos[d * n + i];
+        x[d] = pos[d * comp_stride + i * row_stride];
         if (k.periodic)
         {
             const double L = k.up[d] - k.lo[d];
@@ -332,6 +333,50 @@ __global__ void k_mp_import(size_t n, ImportArgs a, MPFluid f)
     f.id[i] = uint32_t(i);
 }
 
+// Host-row import straight into cell order (sphx_mp_upload_host).  Slot k holds body
+// particle perm[k]: first its geometry from the hashed positions, then, once the other
+// rows have arrived, its state with the conversions of k_mp_import.
+template <int D>
+__global__ void k_mp_place_geometry(size_t n, const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ncell,
+                                    const float *__restrict__ noff, MPFluid dst)
+{
+    size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= n)
+        return;
+    uint32_t i = perm[k];
+    float o[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        o[d] = noff[d * n + i];
+        dst.off[d * n + k] = o[d];
+    }
+    dst.geo0[k] = make_float4(o[0], o[1], o[2], __uint_as_float(ncell[i]));
+}
+
+template <int D>
+__global__ void k_mp_place_state(size_t n, const uint32_t *__restrict__ perm, const double *__restrict__ vel,
+                                 const double *__restrict__ force, const double *__restrict__ rho,
+                                 const double *__restrict__ drho_dt, double rho0, double c0_sqr, MPFluid dst)
+{
+    size_t k = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= n)
+        return;
+    uint32_t i = perm[k];
+    float v[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        v[d] = float(vel[size_t(i) * D + d]);
+        dst.force[d * n + k] = float(force[size_t(i) * D + d]);
+    }
+    float dr = float(rho[i] - rho0);
+    dst.drho[k] = dr;
+    dst.drho_dt[k] = float(drho_dt[i]);
+    dst.dyn[k] = make_float4(v[0], v[1], v[2], float(c0_sqr) * dr);
+    dst.id[k] = i;
+}
+
 // ---------------------------------------------------------------- outputs
 __device__ __forceinline__ double position(const MPConst &k, const MPFluid &f, size_t n, size_t i, int d, const int *c)
 {
@@ -363,6 +408,30 @@ __global__ void k_mp_download(size_t n, MPConst k, MPFluid f, double *__restrict
     rho[o] = double(k.p.rho0) + double(f.drho[i]);
     p[o] = di.w; // pressure of the last 1st-half initialisation, as the FP64 body holds it
     drho_dt[o] = f.drho_dt[i];
+}
+
+// Host-row export (sphx_mp_download_host): position, velocity, density and pressure rows
+// in the body's particle order, the values k_mp_download writes.
+template <int D>
+__global__ void k_mp_export_rows(size_t n, MPConst k, MPFluid f, double *__restrict__ pos, double *__restrict__ vel,
+                                 double *__restrict__ rho, double *__restrict__ p)
+{
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    uint32_t o = f.id[i];
+    int c[3];
+    unpack_cell<D>(__float_as_uint(f.geo0[i].w), c);
+    float4 di = f.dyn[i];
+    const float v[3] = {di.x, di.y, di.z};
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        pos[size_t(o) * D + d] = position(k, f, n, i, d, c);
+        vel[size_t(o) * D + d] = v[d];
+    }
+    rho[o] = double(k.p.rho0) + double(f.drho[i]);
+    p[o] = di.w;
 }
 
 template <int D>
@@ -500,6 +569,11 @@ struct sphx_mp_s
     // build run at the start of the next advection step, so that a caller who replaces
     // the state between steps (sphx_mp_upload) pays for one configuration, not two
     bool moved = false;
+    // host-row transfers (sphx_mp_upload_host / sphx_mp_download_host): device staging
+    // rows, a side stream for the copies that overlap the configuration, two events
+    double *stage = nullptr;
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_pos = nullptr, ev_rest = nullptr;
     int block = 128, strategy = 0;
     // optional CUDA-event timing of the two sweep kernels (sphx_mp_set_profiling)
     bool profiling = false;
@@ -847,11 +921,11 @@ int import_fluid(sphx_mp mp, sphx_body fb, double rho0, double c0)
     if (n > 0)
     {
         if (D == 2)
-            k_mp_from_fp64<2><<<grid_for(n, 256), 256, 0, s>>>(n, (const double *)pos->dev, mp->k, mp->ncell, mp->noff,
-                                                               mp->key, mp->rank, mp->count);
+            k_mp_from_fp64<2><<<grid_for(n, 256), 256, 0, s>>>(n, (const double *)pos->dev, n, 1, mp->k, mp->ncell,
+                                                               mp->noff, mp->key, mp->rank, mp->count);
         else
-            k_mp_from_fp64<3><<<grid_for(n, 256), 256, 0, s>>>(n, (const double *)pos->dev, mp->k, mp->ncell, mp->noff,
-                                                               mp->key, mp->rank, mp->count);
+            k_mp_from_fp64<3><<<grid_for(n, 256), 256, 0, s>>>(n, (const double *)pos->dev, n, 1, mp->k, mp->ncell,
+                                                               mp->noff, mp->key, mp->rank, mp->count);
         ctx->launches++;
     }
     SPHX_TRY(D == 2 ? configuration_update<2>(mp, false) : configuration_update<3>(mp, false));
@@ -1127,6 +1201,130 @@ extern "C" int sphx_mp_create_periodic(sphx_body fb, const sphx_fluid_params *p,
     return SPHX_OK;
 }
 
+namespace
+{
+// Staging rows (n x (3 D + 2) doubles, enough for either direction), the side stream and
+// its events, created on first use.
+int ensure_host_io(sphx_mp mp)
+{
+    if (!mp->stage)
+    {
+        mp->stage = mp->alloc<double>(mp->n * size_t(3 * mp->dim + 2));
+        if (!mp->stage)
+            return fail(SPHX_ERR_CUDA, "cannot allocate the host-transfer staging rows");
+    }
+    if (!mp->side)
+        SPHX_CUDA(cudaStreamCreateWithFlags(&mp->side, cudaStreamNonBlocking));
+    if (!mp->ev_pos)
+        SPHX_CUDA(cudaEventCreateWithFlags(&mp->ev_pos, cudaEventDisableTiming));
+    if (!mp->ev_rest)
+        SPHX_CUDA(cudaEventCreateWithFlags(&mp->ev_rest, cudaEventDisableTiming));
+    return SPHX_OK;
+}
+
+// sphx_mp_upload_host: the positions are copied first and hashed, sorted, placed and
+// searched on the context's stream while the other rows copy on the side stream; the
+// state is placed once they have arrived.  The same state as sphx_body_upload of each row
+// followed by sphx_mp_upload.
+template <int D>
+int upload_host(sphx_mp mp, const double *pos, const double *vel, const double *force, const double *rho,
+                const double *drho_dt)
+{
+    const size_t n = mp->n;
+    sphx_ctx ctx = mp->ctx;
+    cudaStream_t s = ctx->stream;
+    SPHX_TRY(ensure_host_io(mp));
+    SPHX_CUDA(cudaStreamSynchronize(s)); // the staging rows and the state are free
+    double *spos = mp->stage, *svel = spos + n * D, *sforce = svel + n * D, *srho = sforce + n * D,
+           *sdrho = srho + n;
+    const size_t vec = n * D * sizeof(double), sca = n * sizeof(double);
+    if (n > 0)
+    {
+        SPHX_CUDA(cudaMemcpyAsync(spos, pos, vec, cudaMemcpyHostToDevice, s));
+        SPHX_CUDA(cudaEventRecord(mp->ev_pos, s));
+        SPHX_CUDA(cudaStreamWaitEvent(mp->side, mp->ev_pos, 0));
+        SPHX_CUDA(cudaMemcpyAsync(svel, vel, vec, cudaMemcpyHostToDevice, mp->side));
+        SPHX_CUDA(cudaMemcpyAsync(sforce, force, vec, cudaMemcpyHostToDevice, mp->side));
+        SPHX_CUDA(cudaMemcpyAsync(srho, rho, sca, cudaMemcpyHostToDevice, mp->side));
+        SPHX_CUDA(cudaMemcpyAsync(sdrho, drho_dt, sca, cudaMemcpyHostToDevice, mp->side));
+        SPHX_CUDA(cudaEventRecord(mp->ev_rest, mp->side));
+    }
+    SPHX_CUDA(cudaMemsetAsync(mp->count, 0, mp->ncells * sizeof(uint32_t), s));
+    if (n > 0)
+    {
+        k_mp_from_fp64<D><<<grid_for(n, 256), 256, 0, s>>>(n, spos, 1, D, mp->k, mp->ncell, mp->noff, mp->key,
+                                                           mp->rank, mp->count);
+        SPHX_LAUNCHED(ctx);
+    }
+    SPHX_TRY(sort_keys(mp, n, mp->f_offset));
+    if (n > 0)
+    {
+        k_mp_place_geometry<D><<<grid_for(n, 256), 256, 0, s>>>(n, mp->perm, mp->ncell, mp->noff, mp->b);
+        SPHX_LAUNCHED(ctx);
+    }
+    std::swap(mp->a, mp->b);
+    if (n > 0)
+    {
+        SPHX_TRY(launch_build<D>(mp)); // reads the geometry only
+        SPHX_CUDA(cudaStreamWaitEvent(s, mp->ev_rest, 0));
+        k_mp_place_state<D><<<grid_for(n, 256), 256, 0, s>>>(n, mp->perm, svel, sforce, srho, sdrho,
+                                                             double(mp->k.p.rho0), mp->k.p.c0 * mp->k.p.c0, mp->a);
+        SPHX_LAUNCHED(ctx);
+    }
+    // maxima for the first time steps, from the loaded state
+    SPHX_CUDA(cudaMemsetAsync(mp->slots, 0, 2 * sizeof(unsigned long long), s));
+    if (n > 0)
+    {
+        k_mp_initial_max<D><<<grid_for(n, 256), 256, 0, s>>>(n, mp->k, mp->a, mp->slots, mp->slots + 1);
+        SPHX_LAUNCHED(ctx);
+    }
+    mp->moved = false;
+    SPHX_CUDA(cudaStreamSynchronize(s));
+    return SPHX_OK;
+}
+
+template <int D>
+int download_host(sphx_mp mp, double *pos, double *vel, double *rho, double *p)
+{
+    const size_t n = mp->n;
+    cudaStream_t s = mp->ctx->stream;
+    SPHX_TRY(ensure_host_io(mp));
+    double *spos = mp->stage, *svel = spos + n * D, *srho = svel + n * D, *sp = srho + n;
+    if (n > 0)
+    {
+        k_mp_export_rows<D><<<grid_for(n, 256), 256, 0, s>>>(n, mp->k, mp->a, spos, svel, srho, sp);
+        SPHX_LAUNCHED(mp->ctx);
+        const size_t vec = n * D * sizeof(double), sca = n * sizeof(double);
+        SPHX_CUDA(cudaMemcpyAsync(pos, spos, vec, cudaMemcpyDeviceToHost, s));
+        SPHX_CUDA(cudaMemcpyAsync(vel, svel, vec, cudaMemcpyDeviceToHost, s));
+        SPHX_CUDA(cudaMemcpyAsync(rho, srho, sca, cudaMemcpyDeviceToHost, s));
+        SPHX_CUDA(cudaMemcpyAsync(p, sp, sca, cudaMemcpyDeviceToHost, s));
+    }
+    SPHX_CUDA(cudaStreamSynchronize(s));
+    return SPHX_OK;
+}
+} // namespace
+
+extern "C" int sphx_mp_upload_host(sphx_mp mp, const double *position, const double *velocity, const double *force,
+                                   const double *density, const double *density_change_rate)
+{
+    if (!mp || (mp->n > 0 && (!position || !velocity || !force || !density || !density_change_rate)))
+        return fail(SPHX_ERR_INVALID_ARG, "sphx_mp_upload_host needs the five host rows");
+    if (mp->k.periodic)
+        return fail(SPHX_ERR_INVALID_ARG, "a periodic solver loads its state through sphx_mp_upload");
+    return mp->dim == 2 ? upload_host<2>(mp, position, velocity, force, density, density_change_rate)
+                        : upload_host<3>(mp, position, velocity, force, density, density_change_rate);
+}
+
+extern "C" int sphx_mp_download_host(sphx_mp mp, double *position, double *velocity, double *density,
+                                     double *pressure)
+{
+    if (!mp || (mp->n > 0 && (!position || !velocity || !density || !pressure)))
+        return fail(SPHX_ERR_INVALID_ARG, "sphx_mp_download_host needs the four host rows");
+    return mp->dim == 2 ? download_host<2>(mp, position, velocity, density, pressure)
+                        : download_host<3>(mp, position, velocity, density, pressure);
+}
+
 extern "C" int sphx_mp_upload(sphx_mp mp, sphx_body fb)
 {
     if (!mp || !fb || fb->n != mp->n || fb->dim != mp->dim)
@@ -1197,6 +1395,15 @@ extern "C" int sphx_mp_destroy(sphx_mp mp)
     sphx_ctx ctx = mp->ctx;
     cudaStreamSynchronize(ctx->stream);
     collect_events(mp);
+    if (mp->side)
+    {
+        cudaStreamSynchronize(mp->side);
+        cudaStreamDestroy(mp->side);
+    }
+    if (mp->ev_pos)
+        cudaEventDestroy(mp->ev_pos);
+    if (mp->ev_rest)
+        cudaEventDestroy(mp->ev_rest);
     for (void *p : mp->owned)
         cudaFree(p);
     if (mp->h_slots)

@@ -199,6 +199,26 @@ class MixedPrecisionDamBreak:
         """Writes the solver state into an FP64 fluid body (sphx_mp_download)."""
         self._N.call("sphx_mp_download", self.handle, body.handle)
 
+    def upload_host(self, position, velocity, force, density, density_change_rate) -> None:
+        """Loads the solver from host rows in the body's particle order
+        (sphx_mp_upload_host): C-contiguous float64 arrays, n x dim for the vectors."""
+        rows = [position, velocity, force, density, density_change_rate]
+        for a, nc in zip(rows, (self.case.dim, self.case.dim, self.case.dim, 1, 1)):
+            if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"] or a.size != self.n_fluid * nc:
+                raise ValueError("host rows must be C-contiguous float64 of the fluid's size")
+        C = self._C
+        self._N.call("sphx_mp_upload_host", self.handle, *[C.c_void_p(a.ctypes.data) for a in rows])
+
+    def download_host(self, position, velocity, density, pressure) -> None:
+        """Writes position, velocity, density and pressure rows into host arrays
+        (sphx_mp_download_host)."""
+        rows = [position, velocity, density, pressure]
+        for a, nc in zip(rows, (self.case.dim, self.case.dim, 1, 1)):
+            if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"] or a.size != self.n_fluid * nc:
+                raise ValueError("host rows must be C-contiguous float64 of the fluid's size")
+        C = self._C
+        self._N.call("sphx_mp_download_host", self.handle, *[C.c_void_p(a.ctypes.data) for a in rows])
+
     def sync_fp64(self) -> None:
         sim = self.fp64
         self._N.call("sphx_mp_download", self.handle, sim.water_block.handle)

@@ -105,6 +105,8 @@ SIGNATURES = {
     "sphx_mp_advection_step": (_i, [_vp, _i, C.POINTER(C.c_int), _pd, _pd]),
     "sphx_mp_download": (_i, [_vp, _vp]),
     "sphx_mp_upload": (_i, [_vp, _vp]),
+    "sphx_mp_upload_host": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "sphx_mp_download_host": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "sphx_mp_conservation": (_i, [_vp, _pd]),
     "sphx_mp_upper_front": (_i, [_vp, _i, _pd, _pd, _pd]),
     "sphx_mp_set_tuning": (_i, [_vp, _i, _i]),

@@ -131,6 +131,36 @@ def test_configuration_update_deferred_to_next_step():
         assert after_upload < plain, (after_upload, plain)
 
 
+@pytest.mark.parametrize("case", [cases.dambreak_2d(), cases.dambreak_3d(0.04)], ids=lambda c: c.name)
+def test_host_rows_load_and_store_like_the_body_path(case):
+    """sphx_mp_upload_host loads the state sphx_body_upload + sphx_mp_upload load, and
+    sphx_mp_download_host returns the rows sphx_mp_download + sphx_body_download return,
+    bit for bit (the copies overlap the configuration build only in time)."""
+    a = MixedPrecisionDamBreak(case)
+    b = MixedPrecisionDamBreak(case)
+    for _ in range(2):  # same history: the last acoustic dt is kept across a load
+        a.advection_step()
+        b.advection_step()
+    a.sync_fp64()
+    body = a.fp64.water_block
+    rows = {nm: np.ascontiguousarray(body.download(nm)) for nm in
+            ("Position", "Velocity", "Force", "Density", "DensityChangeRate")}
+    a.upload(body)
+    b.upload_host(rows["Position"], rows["Velocity"], rows["Force"], rows["Density"], rows["DensityChangeRate"])
+    assert a.advection_step() == b.advection_step()
+    a.sync_fp64()
+    n, d = a.n_fluid, case.dim
+    out = {"Position": np.zeros((n, d)), "Velocity": np.zeros((n, d)), "Density": np.zeros(n),
+           "Pressure": np.zeros(n)}
+    b.download_host(out["Position"], out["Velocity"], out["Density"], out["Pressure"])
+    for name, v in out.items():
+        assert np.array_equal(v, a.fp64.water_block.download(name)), name
+    again = {k: np.zeros_like(v) for k, v in out.items()}
+    a.download_host(again["Position"], again["Velocity"], again["Density"], again["Pressure"])
+    for name, v in again.items():
+        assert np.array_equal(v, a.fp64.water_block.download(name)), name
+
+
 def test_autotune_keeps_state():
     case = cases.dambreak_2d()
     a = MixedPrecisionDamBreak(case)
