@@ -1,7 +1,7 @@
 """The C++ host layer's dynamic-time-warping regression test (testDTWRegression, the
 testResult of the CK drivers' addReduceRegression / addObserveRegression) against the
 Python restatement, on the stored runs of the reference written in its own file layout:
-a stored run passes, a shifted copy fails, and both restatements give the same verdict."""
+a stored run passes, a shifted copy fails, and both restatements give the same outcome."""
 import os
 import subprocess
 
