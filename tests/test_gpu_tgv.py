@@ -209,3 +209,20 @@ def test_periodic_set_up_rejects_invalid_boxes():
     # the context still runs the flow
     g.advection_step()
     assert np.all(np.isfinite(g.water_block.download("Velocity")))
+
+
+def test_host_row_load_refuses_a_periodic_solver():
+    """sphx_mp_upload_host serves the dam-break solvers; a periodic solver answers
+    SPHX_ERR_INVALID_ARG and keeps running."""
+    import ctypes as C
+    from sphinxsys_gb300 import native as N
+    case = small_3d()
+    mp = MixedPrecisionTaylorGreen(case)
+    n = mp.water_block.n
+    rows = [np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 3)), np.ones(n), np.zeros(n)]
+    with pytest.raises(N.SphxError) as e:
+        N.call("sphx_mp_upload_host", mp.handle, *[C.c_void_p(a.ctypes.data) for a in rows])
+    assert e.value.code == 1
+    ke = mp.kinetic_energy()
+    mp.advection_step()
+    assert 0 < mp.kinetic_energy() < 1.01 * ke
