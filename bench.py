@@ -473,7 +473,8 @@ def reference_arm(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * el / max(args.steps, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic dam-break lattice",
-        "config": {"workload": case.name, "n_fluid": n, "dp": args.mp_dp},
+        "config": {"workload": case.name, "n_fluid": n, "n_wall": oc.n(O.WALL), "dp": args.mp_dp,
+                   "precision": "fp64", "parallelism": "rank 0 only, OpenMP over the host cores"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} advection steps ({subs} acoustic sub-steps) of {case.name}"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
