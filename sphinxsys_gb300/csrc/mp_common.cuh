@@ -211,12 +211,6 @@ struct Acc
     __device__ __forceinline__ float value() const { return k.value(); }
 };
 
-// Position half-step x += dt/2 v on the FP32 cell offset: one fused multiply-add, rounded
-// once like the FP64 sum stored as FP32.  The FP32 step size differs from dt/2 by one
-// rounding (6e-8 relative, about 1e-12 of a displacement), far below the resolution of the
-// offset; the FP64 form costs a dozen operations of the FP64 pipe per particle.
-__device__ __forceinline__ float half_step(float off, float half_dt, float v) { return fmaf(half_dt, v, off); }
-
 // Warp max of the order-preserving bits of v, one atomicMax per warp.
 __device__ __forceinline__ void warp_max_to(unsigned long long *slot, double v)
 {
@@ -578,15 +572,15 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
     f.drho_dt[i] = (rdis.value() * k.inv_z) * rho_i + (wrdis.value() * k.inv_z) * rho_i;
     float v2 = 0.f;
     float vn[3] = {di.x, di.y, di.z};
-    const float dt_f = float(dt), half_dt = float(0.5 * dt);
+    const float dt_f = float(dt);
 #pragma unroll
     for (int d = 0; d < D; ++d)
     {
         float F = f.force[d * n + i] + force[d].value() * k.Vol + wforce[d].value() * k.Vol;
         f.force[d * n + i] = F;
         float vo = vn[d];
-        // position half-step (initialisation of the 1st half, old velocity)
-        f.off[d * n + i] = half_step(f.off[d * n + i], half_dt, vo);
+        // position half-step in FP64 (initialisation of the 1st half, old velocity)
+        f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vo));
         vn[d] = vo + (k.g[d] + F * k.inv_mass) * dt_f;
         v2 += vn[d] * vn[d];
     }
@@ -671,15 +665,14 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
 
     float drho_dt = f.drho_dt[i] + rate.value() * rho_i + wrate.value() * rho_i;
     f.drho_dt[i] = drho_dt;
-    const float half_dt = float(0.5 * dt);
-    f.drho[i] = f.drho[i] + drho_dt * half_dt;
+    f.drho[i] = f.drho[i] + drho_dt * float(0.5 * dt);
     float v2 = 0.f, a2 = 0.f;
 #pragma unroll
     for (int d = 0; d < D; ++d)
     {
         float F = pdis[d].value() * k.Vol + wdis[d].value() * k.Vol;
         f.force[d * n + i] = F;
-        f.off[d * n + i] = half_step(f.off[d * n + i], half_dt, vi[d]);
+        f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vi[d]));
         v2 += vi[d] * vi[d];
         float ft = F + k.mass * k.g[d];
         a2 += ft * ft;
@@ -910,14 +903,14 @@ __device__ __forceinline__ double first_particle_periodic(size_t i, size_t n, co
     f.drho_dt[i] = (rdis.value() * k.inv_z) * rho_i;
     float v2 = 0.f;
     float vn[3] = {di.x, di.y, di.z};
-    const float dt_f = float(dt), half_dt = float(0.5 * dt);
+    const float dt_f = float(dt);
 #pragma unroll
     for (int d = 0; d < D; ++d)
     {
         float F = f.force[d * n + i] + force[d].value() * k.Vol;
         f.force[d * n + i] = F;
         float vo = vn[d];
-        f.off[d * n + i] = half_step(f.off[d * n + i], half_dt, vo);
+        f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vo));
         vn[d] = vo + (f.fprior[d * n + i] + F) * k.inv_mass * dt_f;
         v2 += vn[d] * vn[d];
     }
@@ -978,15 +971,14 @@ __device__ __forceinline__ double second_particle_periodic(size_t i, size_t n, c
 
     float drho_dt = f.drho_dt[i] + rate.value() * rho_i;
     f.drho_dt[i] = drho_dt;
-    const float half_dt = float(0.5 * dt);
-    f.drho[i] = f.drho[i] + drho_dt * half_dt;
+    f.drho[i] = f.drho[i] + drho_dt * float(0.5 * dt);
     float v2 = 0.f, a2 = 0.f;
 #pragma unroll
     for (int d = 0; d < D; ++d)
     {
         float F = pdis[d].value() * k.Vol;
         f.force[d * n + i] = F;
-        f.off[d * n + i] = half_step(f.off[d * n + i], half_dt, vi[d]);
+        f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vi[d]));
         v2 += vi[d] * vi[d];
         float ft = F + f.fprior[d * n + i];
         a2 += ft * ft;
