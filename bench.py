@@ -3,8 +3,8 @@
 Headline workload: the 3D dam break of a 3.2 x 1.0 x 1.8 tank with a 1.2 x 1.0 x 0.6
 water block at dp = 0.006 (3,340,000 fluid particles, 2,456,600 wall particles), advanced
 by the mixed-precision solver (FP32 pair arithmetic with compensated sums on FP32
-positions relative to integer sub-cells; FP64 re-hash, dt reductions and conservation
-sums), timed beside the FP64 path on the same
+positions relative to integer sub-cells; FP64 position integration, re-hash, dt
+reductions and conservation sums), timed beside the FP64 path on the same
 case from the same initial state, with the field / probe / free-surface errors of mixed
 against FP64.  The FP64 drop-in is also measured on dp = 0.0075 (1,702,400 fluid
 particles) through the reference-shaped API (``fp64_drop_in``), a seeded batch of 64
@@ -38,7 +38,7 @@ import time
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
-DTYPE_MIXED = "f32 pairs and cell-relative positions / f64 re-hash, dt, sums"
+DTYPE_MIXED = "f32 pairs, cell-relative f32 positions / f64 position integration, re-hash, dt, sums"
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s (1 GB300): mixed-prec vs FP64 at <=1e-4 rel err; %HBM roofline"
