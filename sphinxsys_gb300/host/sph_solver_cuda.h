@@ -669,6 +669,46 @@ class ObservedQuantityRegressionCK : public RegressionSeriesDTW
     void writeToFile(size_t = 0) { record(observe_.exec()); }
 };
 
+// The regression recorders of the classic drivers (tests/3d_examples/test_3d_dambreak/
+// dambreak.cpp:86-87): RegressionTestDynamicTimeWarping<ReducedQuantityRecording<
+// TotalMechanicalEnergy>>(body, gravity) and RegressionTestDynamicTimeWarping<
+// ObservedQuantityRecording<Real>>(name, observer contact), with the state recorder's
+// classic name.
+template <class ReduceType>
+class ReducedQuantityRecording
+{
+};
+template <class DataType>
+class ObservedQuantityRecording
+{
+};
+template <>
+class RegressionTestDynamicTimeWarping<ReducedQuantityRecording<TotalMechanicalEnergy>> : public RegressionSeriesDTW
+{
+    TotalMechanicalEnergy energy_;
+
+  public:
+    RegressionTestDynamicTimeWarping(SPHBody &body, const Gravity &g)
+        : RegressionSeriesDTW(body.system_, body.name_, "TotalMechanicalEnergy"), energy_(body, g) {}
+    void writeToFile(size_t = 0) { record({energy_.exec()}); }
+};
+template <>
+class RegressionTestDynamicTimeWarping<ObservedQuantityRecording<Real>> : public RegressionSeriesDTW
+{
+    ObservedQuantity observe_;
+
+  public:
+    RegressionTestDynamicTimeWarping(const std::string &name, ContactRelation &contact)
+        : RegressionSeriesDTW(contact.getSPHBody().system_, contact.getSPHBody().name_, name),
+          observe_(name, contact) {}
+    void writeToFile(size_t = 0) { record(observe_.exec()); }
+};
+class BodyStatesRecordingToVtp : public BodyStatesRecordingToVtpCK<>
+{
+  public:
+    using BodyStatesRecordingToVtpCK<>::BodyStatesRecordingToVtpCK;
+};
+
 // ------------------------------------------------------------------ containers
 class BaseMethodContainer
 {

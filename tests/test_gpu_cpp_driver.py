@@ -25,7 +25,8 @@ def compile_example(tmp_path, name="dambreak_2d"):
     return exe
 
 
-@pytest.mark.parametrize("name", ["dambreak_2d", "taylor_green_2d", "dambreak_sycl_3d", "dambreak_sycl_2d"])
+@pytest.mark.parametrize("name", ["dambreak_2d", "dambreak_3d", "taylor_green_2d", "dambreak_sycl_3d",
+                                  "dambreak_sycl_2d"])
 def test_example_compiles(tmp_path, name):
     assert os.path.exists(compile_example(tmp_path, name))
 
@@ -187,3 +188,31 @@ def test_cpp_sycl_2d_driver_runs_reference_regression_and_restarts(tmp_path, gol
     assert int(restart[1]) == 4000 and float(restart[2]) == t4000
     final = [ln.split() for ln in res.stdout.split("\n") if ln.startswith("final")][0]
     assert float(final[2]) >= 20.0
+
+
+@pytest.mark.gpu
+def test_cpp_classic_3d_driver_matches_oracle_and_passes_reference_regression(tmp_path, golden):
+    """examples/dambreak_3d.cpp (the classic 3D driver's call sites and regression
+    recorders): 60 advection steps agree with the oracle (time within 1e-12, mechanical
+    energy within 1e-10); the whole run to t = 20 passes the reference's own DTW test
+    against the stored runs (exit status 0)."""
+    exe = compile_example(tmp_path, "dambreak_3d")
+    steps = 60
+    res = subprocess.run([exe, "20", str(steps), "--state_recording=0"], capture_output=True, text=True,
+                         cwd=tmp_path)
+    assert res.returncode == 0, res.stdout[-2000:] + res.stderr
+    final = [ln.split() for ln in res.stdout.split("\n") if ln.startswith("final")][0]
+    oc = O.OracleCase(cases.dambreak_3d_reference())
+    for _ in range(steps):
+        oc.advection_step()
+    assert int(final[1]) == steps
+    assert abs(float(final[2]) / oc.physical_time.value - 1) < 1e-12
+    assert abs(float(final[3]) / oc.total_mechanical_energy() - 1) < 1e-10
+    full = tmp_path / "full"
+    full.mkdir()
+    for group in ("WaterBody_TotalMechanicalEnergy", "FluidObserver_Pressure"):
+        RF.write_input_folder(str(full / "input"), golden, "dambreak3d", group)
+    res = subprocess.run([exe, "--state_recording=0"], capture_output=True, text=True, cwd=full)
+    print(res.stdout[-800:])
+    assert res.returncode == 0, res.stdout[-3000:] + res.stderr
+    assert res.stdout.count("correct based on the dynamic time warping regression test") == 2
