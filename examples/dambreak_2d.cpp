@@ -1,9 +1,11 @@
 /**
  * 2D dam break on the GB300 execution policy.  Same case, object names and main loop as
  * the reference example tests/2d_examples/test_2d_dambreak/Dambreak.cpp, compiled against
- * sphinxsys_gb300/host/sphinxsys_cuda.h and libsphx_cuda.so.  File output (VTP, restart,
- * regression databases) is replaced by printing the observed pressure and the
- * mechanical energy at the reference's observation interval.
+ * sphinxsys_gb300/host/sphinxsys_cuda.h and libsphx_cuda.so.  The regression recorders
+ * write the .dat series under ./output and, after a run to the end time, run the
+ * reference's dynamic-time-warping test against ./input (exit status 1 on failure); stdout
+ * carries "observe <step> <time> <p> <E>" at the reference's observation interval and
+ * "final <step> <time> <p> <E>".  VTP and restart output are left out.
  *
  * usage: dambreak_2d [end_time] [max_iterations]
  */
@@ -82,6 +84,10 @@ int main(int ac, char *av[])
         ParticleSorting particle_sorting(water_block);
         TotalMechanicalEnergy water_mechanical_energy(water_block, gravity);
         ObservedQuantity recorded_water_pressure("Pressure", fluid_observer_contact);
+        RegressionTestDynamicTimeWarping<ReducedQuantityRecording<TotalMechanicalEnergy>> write_water_mechanical_energy(
+            water_block, gravity);
+        RegressionTestDynamicTimeWarping<ObservedQuantityRecording<Real>> write_recorded_water_pressure(
+            "Pressure", fluid_observer_contact);
 
         sph_system.initializeSystemCellLinkedLists();
         sph_system.initializeSystemConfigurations();
@@ -93,8 +99,11 @@ int main(int ac, char *av[])
         int screen_output_interval = 100;
         int observation_sample_interval = screen_output_interval * 2;
         Real output_interval = 0.1;
+        write_water_mechanical_energy.writeToFile(number_of_iterations);
+        write_recorded_water_pressure.writeToFile(number_of_iterations);
         printf("observe %zu %.17g %.17g %.17g\n", number_of_iterations, physical_time,
                recorded_water_pressure.exec()[0], water_mechanical_energy.exec());
+        bool cut_short = false;
         while (physical_time < end_time)
         {
             Real integration_time = 0.0;
@@ -115,22 +124,37 @@ int main(int ac, char *av[])
                 }
                 if (number_of_iterations % screen_output_interval == 0 &&
                     number_of_iterations % observation_sample_interval == 0 && number_of_iterations != 0)
+                {
+                    write_water_mechanical_energy.writeToFile(number_of_iterations);
+                    write_recorded_water_pressure.writeToFile(number_of_iterations);
                     printf("observe %zu %.17g %.17g %.17g\n", number_of_iterations, physical_time,
                            recorded_water_pressure.exec()[0], water_mechanical_energy.exec());
+                }
                 number_of_iterations++;
                 if (number_of_iterations % 100 == 0 && number_of_iterations != 1)
                     particle_sorting.exec();
                 water_block.updateCellLinkedList();
                 water_wall_complex.updateConfiguration();
                 fluid_observer_contact.updateConfiguration();
-                if (max_iterations >= 0 && long(number_of_iterations) >= max_iterations)
+                cut_short = max_iterations >= 0 && long(number_of_iterations) >= max_iterations;
+                if (cut_short)
                     break;
             }
-            if (max_iterations >= 0 && long(number_of_iterations) >= max_iterations)
+            if (cut_short)
                 break;
         }
         printf("final %zu %.17g %.17g %.17g\n", number_of_iterations, physical_time,
                recorded_water_pressure.exec()[0], water_mechanical_energy.exec());
+        if (sph_system.GenerateRegressionData())
+        {
+            write_water_mechanical_energy.generateDataBase(1.0e-3);
+            write_recorded_water_pressure.generateDataBase(1.0e-3);
+        }
+        else if (!cut_short)
+        {
+            write_water_mechanical_energy.testResult();
+            write_recorded_water_pressure.testResult();
+        }
     }
     catch (const SphxException &e)
     {

@@ -216,3 +216,16 @@ def test_cpp_classic_3d_driver_matches_oracle_and_passes_reference_regression(tm
     print(res.stdout[-800:])
     assert res.returncode == 0, res.stdout[-3000:] + res.stderr
     assert res.stdout.count("correct based on the dynamic time warping regression test") == 2
+
+
+@pytest.mark.gpu
+def test_cpp_classic_2d_driver_passes_reference_regression(tmp_path, golden):
+    """examples/dambreak_2d.cpp to t = 20 with the stored runs of test_2d_dambreak as its
+    input folder: the reference's own DTW test passes for both recorded quantities."""
+    exe = compile_example(tmp_path)
+    for group in ("WaterBody_TotalMechanicalEnergy", "FluidObserver_Pressure"):
+        RF.write_input_folder(str(tmp_path / "input"), golden, "dambreak2d", group)
+    res = subprocess.run([exe], capture_output=True, text=True, cwd=tmp_path)
+    print(res.stdout[-600:])
+    assert res.returncode == 0, res.stdout[-3000:] + res.stderr
+    assert res.stdout.count("correct based on the dynamic time warping regression test") == 2
