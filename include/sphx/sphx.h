@@ -86,6 +86,12 @@ int sphx_body_upload_rows(sphx_body body, const char *name, const void *host, si
 int sphx_body_download_rows(sphx_body body, const char *name, void *host, size_t first, size_t count);
 /* DelegatedData(CudaDevicePolicy): device base pointer of a variable (SoA). */
 int sphx_body_device_ptr(sphx_body body, const char *name, void **dev, sphx_dtype *dtype, int *ncomp);
+/* Checked entry point: counts the particles of a floating-point variable with a
+ * non-finite component (NaN or infinity) into *non_finite (may be null) and returns
+ * SPHX_ERR_NUMERIC when there are any (synchronises).  The reference has no such check;
+ * its failures end the process (`exit(1)`, sphinxsys_variable.h:269-274,
+ * cell_linked_list.cpp:242-246), where this returns a status. */
+int sphx_body_check_finite(sphx_body body, const char *name, uint64_t *non_finite);
 
 /* ------------------------------------------------------------------ mesh + cell list */
 typedef struct
@@ -341,10 +347,24 @@ int sphx_mp_conservation(sphx_mp mp, double *out);
 /* UpperFrontInAxisDirection of the fluid inside an axis-aligned box region. */
 int sphx_mp_upper_front(sphx_mp mp, int axis, const double *region_lower, const double *region_upper,
                         double *front);
+/* Checked entry point on the solver state: particles with a non-finite value in any
+ * evolving field (position offset, velocity, pressure, density, density rate, force) and
+ * finite particles whose position lies outside the cell mesh (a particle that left the
+ * tank); outputs may be null.  Returns SPHX_ERR_NUMERIC when either count is non-zero
+ * (synchronises; reads the state only).  No counterpart in the reference, which clamps
+ * such particles into the boundary cells (base_mesh.hxx:9-15) or ends the process. */
+int sphx_mp_check_state(sphx_mp mp, uint64_t *non_finite, uint64_t *out_of_mesh);
 /* Kernel launch shape and neighbour strategy: block size (64..1024, multiple of 32) of
  * the sweep kernels, and 0 = stored neighbour index lists, 1 = cell sweep every
  * sub-step. */
 int sphx_mp_set_tuning(sphx_mp mp, int block, int strategy);
+/* Tile-grouped traversal of the sweeps and the neighbour build (dam-break solver): the
+ * particles of each box of tx x ty (x tz) sub-cells go to consecutive threads, so a thread
+ * block's neighbour records form a compact window; 0, 0, 0 turns it off.  Results do not
+ * change (same particle order, lists and arithmetic).  Replaces the index-range launch of
+ * particle_for (particle_iterators_sycl.h:229-241), whose work-groups follow the storage
+ * order. */
+int sphx_mp_set_tile(sphx_mp mp, int tx, int ty, int tz);
 /* Times one acoustic sub-step for every block size (64, 128, 256) and both neighbour
  * strategies, restores the state it advanced, and keeps the fastest setting; outputs
  * (any may be null) the chosen block, strategy and ms per sub-step. */
@@ -396,12 +416,18 @@ int sphx_batch_destroy(sphx_batch batch);
  * before each relaxation).  use_graph 1: the step runs as one CUDA graph launch whose
  * conditional WHILE node repeats the acoustic sub-step until no instance is active (the
  * graph is built on first use and rebuilt when list storage grows); 0: the same kernels,
- * with the host reading the loop flag after each sub-step.  An instance taking more than
- * 2^20 sub-steps ends the step with SPHX_ERR_TIMEOUT.  Outputs (may be null, else count
+ * with the host reading the loop flag after each sub-step.  An instance reaching the
+ * sub-step cap (sphx_batch_set_substep_cap) ends the step with SPHX_ERR_TIMEOUT.  Outputs (may be null, else count
  * entries): acoustic sub-steps of this step and physical time per instance. */
 int sphx_batch_advection_step(sphx_batch batch, int use_graph, int *substeps, double *physical_time);
 /* Block size (64..256, multiple of 32) of the two sweep kernels. */
 int sphx_batch_set_tuning(sphx_batch batch, int block);
+/* Cap of acoustic sub-steps per instance in one advection step (1..2^20, default 2^20):
+ * an instance that reaches it stops relaxing, the step completes its configuration update
+ * and returns SPHX_ERR_TIMEOUT.  The device-side loop of the graph therefore always ends.
+ * Replaces the reference's unbounded `while (relaxation_time < advection_dt)` of
+ * Dambreak.cpp:181-198, which has no failure path. */
+int sphx_batch_set_substep_cap(sphx_batch batch, int max_substeps);
 /* Graph launches made so far. */
 int sphx_batch_graph_launches(sphx_batch batch, uint64_t *out);
 /* Fluid state of one instance in its input particle order (any output may be null):

@@ -99,6 +99,11 @@ class BatchDamBreak:
     def set_tuning(self, block: int) -> None:
         N.call("sphx_batch_set_tuning", self.handle, int(block))
 
+    def set_substep_cap(self, max_substeps: int) -> None:
+        """Acoustic sub-steps an instance may take in one advection step before the step
+        ends with SPHX_ERR_TIMEOUT (sphx_batch_set_substep_cap)."""
+        N.call("sphx_batch_set_substep_cap", self.handle, int(max_substeps))
+
     def size(self):
         nf, nw = C.c_size_t(), C.c_size_t()
         N.call("sphx_batch_size", self.handle, C.byref(nf), C.byref(nw))

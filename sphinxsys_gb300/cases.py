@@ -104,7 +104,9 @@ def dambreak_3d_reference(dp: float = 0.05) -> DamBreakCase:
 def dambreak_3d(dp: float = 0.0075) -> DamBreakCase:
     """Benchmark tank 3.2 x 1.0 x 1.8 (z up), water 1.2 x 1.0 x 0.6 at x = 0, 4 wall layers.
 
-    The probe sits on the far wall at (DL, 0.5, 0.2).
+    Two wall-pressure probes at z = 0.2: on the far wall at (DL, 0.5, 0.2), where the water
+    arrives at impact (t ~ 1.3), and on the near wall at (0, 0.5, 0.2), inside the initial
+    column, wetted from t = 0.
     """
     DL, DW, DH = 3.2, 1.0, 1.8
     LL, LW, LH = 1.2, 1.0, 0.6
@@ -122,7 +124,7 @@ def dambreak_3d(dp: float = 0.0075) -> DamBreakCase:
         outer_center=inner_hs, outer_halfsize=outer_hs,
         inner_center=inner_hs, inner_halfsize=inner_hs,
         rho0=rho0, c0=c0, U_ref=U_ref, gravity=(0.0, 0.0, -g),
-        observers=[(DL, 0.5, 0.2)], loop_style=0, vertical_axis=2)
+        observers=[(DL, 0.5, 0.2), (0.0, 0.5, 0.2)], loop_style=0, vertical_axis=2)
 
 
 class MT19937_64:

@@ -28,7 +28,7 @@ using namespace sphx::mpc;
 
 namespace
 {
-constexpr int kMaxSubsteps = 1 << 20; // cap of acoustic sub-steps per advection step
+constexpr int kMaxSubsteps = 1 << 20; // default and largest cap of acoustic sub-steps per advection step
 
 struct BInst
 {
@@ -276,6 +276,7 @@ __global__ void k_b_begin(int count, const BInst *__restrict__ inst, BRun *run)
     r.active = 1;
     r.substeps = 0;
     r.iter = 0;
+    r.error = 0;
     r.ac = 0ull;
     r.adv = 0ull;
 }
@@ -335,8 +336,9 @@ __global__ void k_b_second(size_t n, const uint32_t *__restrict__ starts, int co
 // from the 1st-half maximum and decide whether another sub-step follows; sets the loop
 // condition (graph) or the flag the host reads.
 __global__ void k_b_control(int count, const BInst *__restrict__ inst, BRun *run, int *any_out,
-                            cudaGraphConditionalHandle handle, int use_graph)
+                            const int *__restrict__ cap, cudaGraphConditionalHandle handle, int use_graph)
 {
+    const int max_substeps = *cap;
     __shared__ int any;
     if (threadIdx.x == 0)
         any = 0;
@@ -352,7 +354,7 @@ __global__ void k_b_control(int count, const BInst *__restrict__ inst, BRun *run
         r.substeps += 1;
         r.iter += 1;
         bool more = r.relax < r.Dt;
-        if (r.iter >= kMaxSubsteps)
+        if (more && r.iter >= max_substeps) // needs another sub-step beyond the cap
         {
             more = false;
             r.error = 1;
@@ -447,6 +449,10 @@ struct sphx_batch_s
     MPNeighbors in{}, wl{};
     unsigned int *d_max = nullptr, *h_max = nullptr;
     int *d_any = nullptr, *h_any = nullptr;
+    // cap of acoustic sub-steps per instance and advection step (device copy read by the
+    // control kernel, so a captured graph sees a new value without being rebuilt)
+    int *d_cap = nullptr;
+    int max_substeps = kMaxSubsteps;
     int block = 128;
     // one executable graph per state parity: [density + step start] -> WHILE(sub-step) ->
     // [re-hash, sort, gather, neighbour lists, counter read-back]
@@ -611,7 +617,7 @@ int b_enqueue_substep(sphx_batch bt, cudaStream_t s, const MPState &cur, int use
     k_b_second<D><<<grid_for(n, blk), blk, 0, s>>>(n, bt->starts, bt->count, bt->inst, bt->run, cur, bt->w, bt->in,
                                                    bt->wl);
     SPHX_CUDA(cudaGetLastError());
-    k_b_control<<<1, 256, 0, s>>>(bt->count, bt->inst, bt->run, bt->d_any, handle, use_graph);
+    k_b_control<<<1, 256, 0, s>>>(bt->count, bt->inst, bt->run, bt->d_any, bt->d_cap, handle, use_graph);
     SPHX_CUDA(cudaGetLastError());
     return SPHX_OK;
 }
@@ -707,7 +713,7 @@ int b_advection_step(sphx_batch bt, int use_graph)
     else
     {
         SPHX_TRY(b_enqueue_begin<D>(bt, s, src));
-        for (int it = 0; it <= kMaxSubsteps; ++it)
+        for (int it = 0; it <= bt->max_substeps; ++it)
         {
             SPHX_TRY(b_enqueue_substep<D>(bt, s, src, 0, 0));
             ++loops;
@@ -724,8 +730,8 @@ int b_advection_step(sphx_batch bt, int use_graph)
     bt->parity ^= 1;
     for (int b = 0; b < bt->count; ++b)
         if (bt->h_run[b].error)
-            return fail(SPHX_ERR_TIMEOUT, "instance %d exceeded %d acoustic sub-steps in one advection step", b,
-                        kMaxSubsteps);
+            return fail(SPHX_ERR_TIMEOUT, "instance %d reached the cap of %d acoustic sub-steps in one advection step",
+                        b, bt->max_substeps);
     return b_check_lists<D>(bt);
 }
 
@@ -857,10 +863,11 @@ extern "C" int sphx_batch_create(sphx_ctx ctx, int dim, int count, const sphx_ba
     bt->wl.count = bt->alloc<uint32_t>(n);
     bt->d_max = bt->alloc<unsigned int>(2);
     bt->d_any = bt->alloc<int>(1);
+    bt->d_cap = bt->alloc<int>(1);
     int st;
     if (!bt->inst || !bt->run || !bt->starts || !bt->wstarts || !bt->f_offset || !bt->w_offset || !bt->cnt ||
         !bt->scan_tiles || !bt->key || !bt->rank || !bt->perm || !bt->ncell || !bt->noff || !bt->w.geo || !bt->w.n ||
-        !bt->in.count || !bt->wl.count || !bt->d_max || !bt->d_any)
+        !bt->in.count || !bt->wl.count || !bt->d_max || !bt->d_any || !bt->d_cap)
         return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "batch allocation failed"));
     if ((st = b_alloc_state(bt, bt->st[0])) != SPHX_OK || (st = b_alloc_state(bt, bt->st[1])) != SPHX_OK)
         return bail(st);
@@ -875,6 +882,8 @@ extern "C" int sphx_batch_create(sphx_ctx ctx, int dim, int count, const sphx_ba
         return bail(st);
     for (int q = 0; q < count; ++q)
         bt->h_run[q] = BRun{};
+    if (cudaMemcpy(bt->d_cap, &bt->max_substeps, sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(fail(SPHX_ERR_CUDA, "sub-step cap upload failed"));
     // host staging: FP64 SoA of fluid positions, wall positions and normals
     std::vector<double> fpos(size_t(D) * n), wpos(size_t(D) * nw), wnrm(size_t(D) * nw);
     std::vector<uint32_t> ids(n);
@@ -979,6 +988,17 @@ extern "C" int sphx_batch_set_tuning(sphx_batch bt, int block)
         return fail(SPHX_ERR_INVALID_ARG, "block must be 64..256 in steps of 32");
     bt->block = block;
     bt->invalidate_graphs();
+    return SPHX_OK;
+}
+
+extern "C" int sphx_batch_set_substep_cap(sphx_batch bt, int max_substeps)
+{
+    if (!bt || max_substeps < 1 || max_substeps > kMaxSubsteps)
+        return fail(SPHX_ERR_INVALID_ARG, "the sub-step cap must lie in 1..%d", kMaxSubsteps);
+    // ordered on the stream after every step already enqueued
+    SPHX_CUDA(cudaMemcpyAsync(bt->d_cap, &max_substeps, sizeof(int), cudaMemcpyHostToDevice, bt->ctx->stream));
+    SPHX_CUDA(cudaStreamSynchronize(bt->ctx->stream));
+    bt->max_substeps = max_substeps;
     return SPHX_OK;
 }
 

@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "mp_common.cuh"
+#include "mp_tiled.cuh"
 #include "sphx_device.cuh"
 #include "sphx_internal.cuh"
 
@@ -191,13 +192,37 @@ __global__ void k_mp_gather(size_t n, const uint32_t *__restrict__ perm, const u
 }
 
 // ---------------------------------------------------------------- configuration + density sums
-template <int D>
+// Particle handled by thread t: t itself, or the t-th particle of the tile-grouped order.
+template <bool ORDER>
+__device__ __forceinline__ size_t particle_of(size_t t, const uint32_t *__restrict__ order)
+{
+    return ORDER ? size_t(__ldg(&order[t])) : t;
+}
+
+template <int D, bool ORDER>
 __global__ void k_mp_build(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
-               const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, unsigned int *max_counts)
+               const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, unsigned int *max_counts,
+               const uint32_t *__restrict__ order)
+{
+    size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t < n)
+        build_particle<D>(particle_of<ORDER>(t, order), n, k.p, Visit{k.m, 0u, f_offset, w_offset}, f, w, in, wl,
+                          max_counts);
+}
+
+// Tile key of every particle (cell order) for the tile-grouped traversal order.
+template <int D>
+__global__ void k_mp_tile_key(size_t n, const float4 *__restrict__ geo0, TileShape ts, uint32_t *__restrict__ key,
+                              uint32_t *__restrict__ rank, uint32_t *__restrict__ count)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i < n)
-        build_particle<D>(i, n, k.p, Visit{k.m, 0u, f_offset, w_offset}, f, w, in, wl, max_counts);
+    if (i >= n)
+        return;
+    int c[3];
+    unpack_cell<D>(__float_as_uint(geo0[i].w), c);
+    const uint32_t t = tile_key<D>(ts, c);
+    key[i] = t;
+    rank[i] = atomicAdd(&count[t], 1u);
 }
 
 template <int D>
@@ -245,27 +270,223 @@ __global__ void k_mp_init1(size_t n, float *__restrict__ drho, const float *__re
 }
 
 // at most 64 registers: 4 blocks of 256 threads per SM
-template <int D, bool LISTS>
-__global__ void __launch_bounds__(256, 4) k_mp_first(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
-               const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, double dt,
-               unsigned long long *ac_slot)
+// ---------------------------------------------------------------- tiled strategy
+// Non-empty tiles of the tile-grouped order, compacted (tile_pos = exclusive scan of flags).
+__global__ void k_mp_tile_flags(size_t nt, const uint32_t *__restrict__ tile_offset, uint32_t *__restrict__ flags)
 {
-    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t < nt)
+        flags[t] = tile_offset[t + 1] > tile_offset[t] ? 1u : 0u;
+}
+
+__global__ void k_mp_tile_compact(size_t nt, const uint32_t *__restrict__ flags, const uint32_t *__restrict__ pos,
+                                  uint32_t *__restrict__ tiles, unsigned int *count)
+{
+    size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= nt)
+        return;
+    if (flags[t])
+        tiles[pos[t]] = uint32_t(t);
+    if (t == nt - 1)
+        *count = pos[t] + flags[t];
+}
+
+// Largest window population (fluid, wall) over the non-empty tiles: one warp per tile.
+template <int D>
+__global__ void k_mp_tile_population(const unsigned int *ntiles, MeshDev m, TileShape ts,
+                                     const uint32_t *__restrict__ tiles, const uint32_t *__restrict__ f_offset,
+                                     const uint32_t *__restrict__ w_offset, unsigned int *maxes)
+{
+    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (warp >= *ntiles)
+        return;
+    Window<D> w;
+    tile_window<D>(m, ts, tiles[warp], w);
+    unsigned nf = 0, nw = 0;
+    for (int col = int(lane); col < w.ncol; col += 32)
+    {
+        uint32_t a, b;
+        column_cells<D>(m, w, col, a, b);
+        nf += f_offset[b + 1] - f_offset[a];
+        nw += w_offset[b + 1] - w_offset[a];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        nf += __shfl_down_sync(0xffffffffu, nf, o);
+        nw += __shfl_down_sync(0xffffffffu, nw, o);
+    }
+    if (lane == 0)
+    {
+        atomicMax(&maxes[0], nf);
+        atomicMax(&maxes[1], nw);
+    }
+}
+
+// Shared-memory layout of a tiled kernel: run tables, then the record arrays (sizes from the
+// largest window: cap_f fluid and cap_w wall records).
+struct TiledSmem
+{
+    uint32_t fbeg[kTileMaxCols], fbase[kTileMaxCols + 1], wbeg[kTileMaxCols], wbase[kTileMaxCols + 1], total[2];
+};
+
+// Sets up the window of this block's tile and its run tables; false if the window exceeds
+// the staged capacity (never for capacities from k_mp_tile_population; the block then
+// records the overflow and skips its tile).
+template <int D>
+__device__ __forceinline__ bool tiled_setup(const MeshDev &m, const TileGrid &g, const uint32_t *f_offset,
+                                            const uint32_t *w_offset, unsigned cap_f, unsigned cap_w, TiledSmem &t,
+                                            Staged<D> &sw, unsigned int *overflow)
+{
+    tile_window<D>(m, g.ts, g.tiles[blockIdx.x], sw.w);
+    const uint32_t nf = window_table<D>(m, sw.w, f_offset, t.fbeg, t.fbase, &t.total[0]);
+    const uint32_t nw = window_table<D>(m, sw.w, w_offset, t.wbeg, t.wbase, &t.total[1]);
+    sw.fbeg = t.fbeg;
+    sw.fbase = t.fbase;
+    sw.wbeg = t.wbeg;
+    sw.wbase = t.wbase;
+    if (nf > cap_f || nw > cap_w)
+    {
+        if (threadIdx.x == 0)
+            atomicAdd(overflow, 1u);
+        return false;
+    }
+    return true;
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) k_mp_build_tiled(size_t n, MPConst k, MPFluid f,
+                                                        const uint32_t *__restrict__ f_offset, MPWall w,
+                                                        const uint32_t *__restrict__ w_offset, TileGrid g, MPLists in,
+                                                        MPLists wl, unsigned int *max_counts, unsigned cap_f,
+                                                        unsigned cap_w, unsigned int *overflow)
+{
+    extern __shared__ float4 dyn_smem[];
+    __shared__ TiledSmem t;
+    Staged<D> sw;
+    if (!tiled_setup<D>(k.m, g, f_offset, w_offset, cap_f, cap_w, t, sw, overflow))
+        return;
+    float4 *fa = dyn_smem, *wa = dyn_smem + cap_f;
+    for_each_staged<D>(sw.w, t.fbeg, t.fbase, [&](uint32_t j, uint32_t s) { fa[s] = f.geo0[j]; });
+    for_each_staged<D>(sw.w, t.wbeg, t.wbase, [&](uint32_t j, uint32_t s) { wa[s] = w.geo[j]; });
+    sw.fa = fa;
+    sw.wa = wa;
+    __syncthreads();
+    const uint32_t tile = g.tiles[blockIdx.x];
+    const uint32_t te = g.tile_offset[tile + 1];
+    for (uint32_t q = g.tile_offset[tile] + threadIdx.x; q < te; q += blockDim.x)
+        build_particle_tiled<D>(q, g.order[q], n, k.p, k.m, sw, f_offset, w_offset, f, in, wl, max_counts);
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) k_mp_first_tiled(size_t n, MPConst k, MPFluid f,
+                                                        const uint32_t *__restrict__ f_offset, MPWall w,
+                                                        const uint32_t *__restrict__ w_offset, TileGrid g, MPLists in,
+                                                        MPLists wl, double dt, unsigned long long *ac_slot,
+                                                        unsigned cap_f, unsigned cap_w, unsigned int *overflow)
+{
+    extern __shared__ float4 dyn_smem[];
+    __shared__ TiledSmem t;
+    Staged<D> sw;
     double vmax = -1.0e300;
-    if (i < n)
-        vmax = first_particle<D, LISTS>(i, n, k.p, Visit{k.m, 0u, f_offset, w_offset}, dt, f, w, in, wl);
+    if (tiled_setup<D>(k.m, g, f_offset, w_offset, cap_f, cap_w, t, sw, overflow))
+    {
+        float4 *fa = dyn_smem, *fb = fa + cap_f, *wa = fb + cap_f, *wb = wa + cap_w;
+        const Window<D> &win = sw.w;
+        for_each_staged<D>(win, t.fbeg, t.fbase, [&](uint32_t j, uint32_t s) {
+            const float4 gj = f.geo0[j];
+            fa[s] = make_float4(gj.x, gj.y, gj.z, __ldg(&f.dyn[j].w));
+            fb[s] = window_cell<D>(win, __float_as_uint(gj.w));
+        });
+        for_each_staged<D>(win, t.wbeg, t.wbase, [&](uint32_t j, uint32_t s) {
+            const float4 gj = w.geo[j];
+            wa[s] = gj;
+            wb[s] = window_cell<D>(win, __float_as_uint(gj.w));
+        });
+        sw.fa = fa;
+        sw.fb = fb;
+        sw.wa = wa;
+        sw.wb = wb;
+        __syncthreads();
+        const uint32_t tile = g.tiles[blockIdx.x];
+        const uint32_t te = g.tile_offset[tile + 1];
+        for (uint32_t q = g.tile_offset[tile] + threadIdx.x; q < te; q += blockDim.x)
+            vmax = fmax(vmax, first_particle_tiled<D>(q, g.order[q], n, k.p, sw, dt, f, in, wl));
+    }
     warp_max_to(ac_slot, vmax);
 }
 
-template <int D, bool LISTS>
+template <int D>
+__global__ void __launch_bounds__(256) k_mp_second_tiled(size_t n, MPConst k, MPFluid f,
+                                                         const uint32_t *__restrict__ f_offset, MPWall w,
+                                                         const uint32_t *__restrict__ w_offset, TileGrid g,
+                                                         MPLists in, MPLists wl, double dt,
+                                                         unsigned long long *adv_slot, unsigned cap_f, unsigned cap_w,
+                                                         unsigned int *overflow)
+{
+    extern __shared__ float4 dyn_smem[];
+    __shared__ TiledSmem t;
+    Staged<D> sw;
+    double amax = -1.0e300;
+    if (tiled_setup<D>(k.m, g, f_offset, w_offset, cap_f, cap_w, t, sw, overflow))
+    {
+        float4 *fa = dyn_smem, *fb = fa + cap_f, *wa = fb + cap_f, *wb = wa + cap_w;
+        float *fc = reinterpret_cast<float *>(wb + cap_w), *wc = fc + cap_f;
+        const Window<D> &win = sw.w;
+        for_each_staged<D>(win, t.fbeg, t.fbase, [&](uint32_t j, uint32_t s) {
+            const float4 gj = f.geo0[j], vj = f.dyn[j];
+            float4 c = window_cell<D>(win, __float_as_uint(gj.w));
+            c.w = vj.y;
+            fa[s] = make_float4(gj.x, gj.y, gj.z, vj.x);
+            fb[s] = c;
+            fc[s] = vj.z;
+        });
+        for_each_staged<D>(win, t.wbeg, t.wbase, [&](uint32_t j, uint32_t s) {
+            const float4 gj = w.geo[j], nj = w.n[j];
+            float4 c = window_cell<D>(win, __float_as_uint(gj.w));
+            c.w = nj.y;
+            wa[s] = make_float4(gj.x, gj.y, gj.z, nj.x);
+            wb[s] = c;
+            wc[s] = nj.z;
+        });
+        sw.fa = fa;
+        sw.fb = fb;
+        sw.fc = fc;
+        sw.wa = wa;
+        sw.wb = wb;
+        sw.wc = wc;
+        __syncthreads();
+        const uint32_t tile = g.tiles[blockIdx.x];
+        const uint32_t te = g.tile_offset[tile + 1];
+        for (uint32_t q = g.tile_offset[tile] + threadIdx.x; q < te; q += blockDim.x)
+            amax = fmax(amax, second_particle_tiled<D>(q, g.order[q], n, k.p, sw, dt, f, in, wl));
+    }
+    warp_max_to(adv_slot, amax);
+}
+
+template <int D, bool LISTS, bool ORDER>
+__global__ void __launch_bounds__(256, 4) k_mp_first(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
+               const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, double dt,
+               unsigned long long *ac_slot, const uint32_t *__restrict__ order)
+{
+    size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    double vmax = -1.0e300;
+    if (t < n)
+        vmax = first_particle<D, LISTS>(particle_of<ORDER>(t, order), n, k.p, Visit{k.m, 0u, f_offset, w_offset}, dt,
+                                        f, w, in, wl);
+    warp_max_to(ac_slot, vmax);
+}
+
+template <int D, bool LISTS, bool ORDER>
 __global__ void k_mp_second(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
                 const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, double dt,
-                unsigned long long *adv_slot)
+                unsigned long long *adv_slot, const uint32_t *__restrict__ order)
 {
-    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     double amax = -1.0e300;
-    if (i < n)
-        amax = second_particle<D, LISTS>(i, n, k.p, Visit{k.m, 0u, f_offset, w_offset}, dt, f, w, in, wl);
+    if (t < n)
+        amax = second_particle<D, LISTS>(particle_of<ORDER>(t, order), n, k.p, Visit{k.m, 0u, f_offset, w_offset},
+                                         dt, f, w, in, wl);
     warp_max_to(adv_slot, amax);
 }
 
@@ -472,6 +693,38 @@ __global__ void k_mp_conservation(size_t n, MPConst k, MPFluid f, double *__rest
             partials[blockIdx.x * 5 + q] = sm[q][0];
 }
 
+// State check (sphx_mp_check_state): counts particles with a non-finite value in any
+// evolving field (offset, velocity, pressure, density, density rate, force) and particles
+// whose reconstructed position lies outside the mesh [lower, lower + all_cells gs].  The
+// counts go to counts[0], counts[1] (one atomic per particle found).
+template <int D>
+__global__ void k_mp_check(size_t n, MPConst k, MPFluid f, unsigned long long *counts)
+{
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+    {
+        int c[3];
+        unpack_cell<D>(__float_as_uint(f.geo0[i].w), c);
+        const float4 di = f.dyn[i];
+        bool fin = isfinite(di.x) && isfinite(di.y) && isfinite(di.z) && isfinite(di.w) && isfinite(f.drho[i]) &&
+                   isfinite(f.drho_dt[i]);
+        bool in = true;
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+        {
+            const float o = f.off[d * n + i];
+            fin = fin && isfinite(o) && isfinite(f.force[d * n + i]);
+            const double x = position(k, f, n, i, d, c);
+            const double hi = k.m.lower[d] + double(k.m.all_cells[d]) * k.m.gs;
+            in = in && !(x < k.m.lower[d] || x > hi);
+        }
+        // a non-finite offset has no position; it counts once, as non-finite
+        if (!fin)
+            atomicAdd(&counts[0], 1ull);
+        else if (!in)
+            atomicAdd(&counts[1], 1ull);
+    }
+}
+
 template <int D>
 __global__ void k_mp_upper_front(size_t n, MPConst k, MPFluid f, int axis, double l0, double l1, double l2,
                                  double u0, double u1, double u2, unsigned long long *slot)
@@ -562,7 +815,10 @@ struct sphx_mp_s
     uint32_t *key = nullptr, *rank = nullptr, *perm = nullptr, *ncell = nullptr;
     float *noff = nullptr;
     MPLists in{}, wl{};
-    unsigned long long *slots = nullptr; // 0 acoustic, 1 advection, 2 misc, 3 build counts
+    // device scalars: 0 acoustic max, 1 advection max, 2 misc, 3 build counts, 4-5 state
+    // check, 6-7 tile preparation (window maxima, tile count, build overflow), 8 sweep
+    // overflow of the tiled strategy
+    unsigned long long *slots = nullptr;
     unsigned long long *h_slots = nullptr;
     double physical_time = 0, acoustic_dt = 0;
     // positions moved since the last configuration update: the re-hash, re-sort and list
@@ -575,6 +831,18 @@ struct sphx_mp_s
     cudaStream_t side = nullptr;
     cudaEvent_t ev_pos = nullptr, ev_rest = nullptr;
     int block = 128, strategy = 0;
+    // tile-grouped traversal (TileShape): tile[0] == 0 keeps the cell order; `order` holds
+    // the particles grouped by tile, recomputed at every configuration update
+    int tile[3] = {0, 0, 0};
+    uint32_t *order = nullptr, *tile_offset = nullptr;
+    bool order_active = false;
+    // tiled strategy (strategy 2): compacted non-empty tiles, scan scratch, the staged
+    // capacities of the current configuration and the strategy the lists were built for
+    uint32_t *tiles = nullptr, *tile_flags = nullptr, *tile_pos = nullptr;
+    unsigned ntiles_ne = 0, cap_f = 0, cap_w = 0;
+    bool lists_tiled = false;
+    int lists_strategy = -1;
+    size_t smem_set[3] = {0, 0, 0}; // dynamic shared memory granted to the three tiled kernels
     // optional CUDA-event timing of the two sweep kernels (sphx_mp_set_profiling)
     bool profiling = false;
     std::vector<cudaEvent_t> ev_first, ev_second; // start/stop pairs
@@ -662,23 +930,140 @@ int sort_keys(sphx_mp mp, size_t n, uint32_t *offset)
     return SPHX_OK;
 }
 
+TileShape tile_shape(sphx_mp mp, size_t *ntiles)
+{
+    TileShape ts{};
+    size_t nt = 1;
+    for (int d = 0; d < 3; ++d)
+    {
+        ts.t[d] = d < mp->dim ? std::max(mp->tile[d], 1) : 1;
+        ts.nt[d] = d < mp->dim ? (mp->k.m.all_cells[d] + ts.t[d] - 1) / ts.t[d] : 1;
+        nt *= size_t(ts.nt[d]);
+    }
+    *ntiles = nt;
+    return ts;
+}
+
+// The tile-grouped traversal order of the current cell order (a stable counting sort of the
+// particles by tile key), when a tile shape is set; dam-break (non-periodic) solver only.
+template <int D>
+int tile_order(sphx_mp mp)
+{
+    mp->order_active = false;
+    if (!mp->tile[0] || mp->k.periodic || mp->n == 0)
+        return SPHX_OK;
+    sphx_ctx ctx = mp->ctx;
+    cudaStream_t s = ctx->stream;
+    const size_t n = mp->n;
+    size_t nt = 0;
+    const TileShape ts = tile_shape(mp, &nt);
+    SPHX_CUDA(cudaMemsetAsync(mp->count, 0, nt * sizeof(uint32_t), s));
+    k_mp_tile_key<D><<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.geo0, ts, mp->key, mp->rank, mp->count);
+    SPHX_LAUNCHED(ctx);
+    SPHX_TRY(exclusive_scan(ctx, mp->count, mp->tile_offset, nt));
+    k_mp_set_total<<<1, 1, 0, s>>>(mp->tile_offset, nt, uint32_t(n));
+    SPHX_LAUNCHED(ctx);
+    k_mp_scatter<<<grid_for(n, 256), 256, 0, s>>>(n, mp->key, mp->rank, mp->tile_offset, mp->order);
+    SPHX_LAUNCHED(ctx);
+    k_mp_sort_segments<<<grid_for(nt, 256), 256, 0, s>>>(nt, mp->tile_offset, mp->order);
+    SPHX_LAUNCHED(ctx);
+    mp->order_active = true;
+    return SPHX_OK;
+}
+
+constexpr size_t kTiledSmemLimit = 200 * 1024; // dynamic shared memory a tiled block may take
+
+TileGrid tile_grid(sphx_mp mp)
+{
+    size_t nt = 0;
+    TileGrid g{};
+    g.ts = tile_shape(mp, &nt);
+    g.tiles = mp->tiles;
+    g.tile_offset = mp->tile_offset;
+    g.order = mp->order;
+    return g;
+}
+
+// Grants a tiled kernel `bytes` of dynamic shared memory (raised only when needed).
+template <class K>
+int grant_smem(sphx_mp mp, int which, K kernel, size_t bytes)
+{
+    if (bytes > mp->smem_set[which])
+    {
+        SPHX_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
+        mp->smem_set[which] = bytes;
+    }
+    return SPHX_OK;
+}
+
+// Non-empty tiles of the tile-grouped order and the largest window populations, read back
+// to size the staged windows (synchronises).  Sets mp->lists_tiled when the largest window
+// fits the shared-memory limit.
+template <int D>
+int tile_prepare(sphx_mp mp)
+{
+    sphx_ctx ctx = mp->ctx;
+    cudaStream_t s = ctx->stream;
+    size_t nt = 0;
+    const TileShape ts = tile_shape(mp, &nt);
+    unsigned int *res = reinterpret_cast<unsigned int *>(mp->slots + 6); // maxes, count, overflow
+    SPHX_CUDA(cudaMemsetAsync(res, 0, 4 * sizeof(unsigned int), s));
+    k_mp_tile_flags<<<grid_for(nt, 256), 256, 0, s>>>(nt, mp->tile_offset, mp->tile_flags);
+    SPHX_LAUNCHED(ctx);
+    SPHX_TRY(exclusive_scan(ctx, mp->tile_flags, mp->tile_pos, nt));
+    k_mp_tile_compact<<<grid_for(nt, 256), 256, 0, s>>>(nt, mp->tile_flags, mp->tile_pos, mp->tiles, res + 2);
+    SPHX_LAUNCHED(ctx);
+    const size_t warps = std::min(nt, mp->n);
+    k_mp_tile_population<D><<<grid_for(warps * 32, 256), 256, 0, s>>>(res + 2, mp->k.m, ts, mp->tiles, mp->f_offset,
+                                                                      mp->w_offset, res);
+    SPHX_LAUNCHED(ctx);
+    SPHX_CUDA(cudaMemcpyAsync(mp->h_slots + 6, res, 4 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+    SPHX_CUDA(cudaStreamSynchronize(s));
+    const unsigned int *h = reinterpret_cast<const unsigned int *>(mp->h_slots + 6);
+    mp->cap_f = std::max(h[0], 1u);
+    mp->cap_w = std::max(h[1], 1u);
+    mp->ntiles_ne = h[2];
+    mp->lists_tiled = 36 * size_t(mp->cap_f + mp->cap_w) + 64 <= kTiledSmemLimit && mp->ntiles_ne > 0;
+    return SPHX_OK;
+}
+
 template <int D>
 int launch_build(sphx_mp mp)
 {
     sphx_ctx ctx = mp->ctx;
     cudaStream_t s = ctx->stream;
     unsigned int *mc = reinterpret_cast<unsigned int *>(mp->slots + 3);
+    SPHX_TRY(tile_order<D>(mp));
+    mp->lists_tiled = false;
+    if (mp->strategy == 2 && mp->order_active)
+        SPHX_TRY(tile_prepare<D>(mp));
+    mp->lists_strategy = mp->strategy;
+    const unsigned tblk = unsigned(mp->block);
+    if (mp->lists_tiled)
+        SPHX_TRY(grant_smem(mp, 0, k_mp_build_tiled<D>, 16 * size_t(mp->cap_f + mp->cap_w)));
+    unsigned int *overflow = reinterpret_cast<unsigned int *>(mp->slots + 6) + 3;
     for (int attempt = 0; attempt < 2; ++attempt)
     {
         SPHX_CUDA(cudaMemsetAsync(mc, 0, 2 * sizeof(unsigned int), s));
         if (mp->k.periodic)
             k_mp_build_periodic<D><<<grid_for(mp->n, 256), 256, 0, s>>>(mp->n, mp->k, mp->a, mp->f_offset, mp->in, mc);
+        else if (mp->lists_tiled)
+            k_mp_build_tiled<D><<<mp->ntiles_ne, tblk, 16 * size_t(mp->cap_f + mp->cap_w), s>>>(
+                mp->n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset, tile_grid(mp), mp->in, mp->wl, mc,
+                mp->cap_f, mp->cap_w, overflow);
+        else if (mp->order_active)
+            k_mp_build<D, true><<<grid_for(mp->n, 256), 256, 0, s>>>(mp->n, mp->k, mp->a, mp->f_offset, mp->w,
+                                                                    mp->w_offset, mp->in, mp->wl, mc, mp->order);
         else
-            k_mp_build<D><<<grid_for(mp->n, 256), 256, 0, s>>>(mp->n, mp->k, mp->a, mp->f_offset, mp->w,
-                                                              mp->w_offset, mp->in, mp->wl, mc);
+            k_mp_build<D, false><<<grid_for(mp->n, 256), 256, 0, s>>>(mp->n, mp->k, mp->a, mp->f_offset, mp->w,
+                                                                     mp->w_offset, mp->in, mp->wl, mc, nullptr);
         SPHX_LAUNCHED(ctx);
         SPHX_CUDA(cudaMemcpyAsync(mp->h_slots + 3, mc, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+        SPHX_CUDA(cudaMemcpyAsync(mp->h_slots + 7, mp->slots + 7, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                  s));
         SPHX_CUDA(cudaStreamSynchronize(s));
+        if (mp->lists_tiled && reinterpret_cast<const unsigned int *>(mp->h_slots + 7)[1] != 0)
+            return fail(SPHX_ERR_CAPACITY, "a tile window exceeded its staged capacity");
         const unsigned int *h = reinterpret_cast<const unsigned int *>(mp->h_slots + 3);
         bool grow = false;
         if (h[0] > mp->in.cap)
@@ -728,7 +1113,12 @@ int read_slot(sphx_mp mp, int slot, double *out)
 {
     SPHX_CUDA(cudaMemcpyAsync(mp->h_slots + slot, mp->slots + slot, sizeof(unsigned long long),
                               cudaMemcpyDeviceToHost, mp->ctx->stream));
+    if (mp->lists_tiled)
+        SPHX_CUDA(cudaMemcpyAsync(mp->h_slots + 8, mp->slots + 8, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                  mp->ctx->stream));
     SPHX_CUDA(cudaStreamSynchronize(mp->ctx->stream));
+    if (mp->lists_tiled && mp->h_slots[8] != 0)
+        return fail(SPHX_ERR_CAPACITY, "a tile window exceeded its staged capacity in a sweep");
     *out = from_ordered_bits(mp->h_slots[slot]);
     return SPHX_OK;
 }
@@ -744,6 +1134,44 @@ int settle_configuration(sphx_mp mp)
     return SPHX_OK;
 }
 
+template <int D, bool LISTS, bool ORDER>
+void launch_first(sphx_mp mp, unsigned blk, double dt)
+{
+    const size_t n = mp->n;
+    k_mp_first<D, LISTS, ORDER><<<grid_for(n, blk), blk, 0, mp->ctx->stream>>>(
+        n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset, mp->in, mp->wl, dt, mp->slots, mp->order);
+}
+
+template <int D, bool LISTS, bool ORDER>
+void launch_second(sphx_mp mp, unsigned blk, double dt)
+{
+    const size_t n = mp->n;
+    k_mp_second<D, LISTS, ORDER><<<grid_for(n, blk), blk, 0, mp->ctx->stream>>>(
+        n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset, mp->in, mp->wl, dt, mp->slots + 1, mp->order);
+}
+
+template <int D>
+int launch_first_tiled(sphx_mp mp, unsigned blk, double dt)
+{
+    const size_t bytes = 32 * size_t(mp->cap_f + mp->cap_w);
+    SPHX_TRY(grant_smem(mp, 1, k_mp_first_tiled<D>, bytes));
+    k_mp_first_tiled<D><<<mp->ntiles_ne, blk, bytes, mp->ctx->stream>>>(
+        mp->n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset, tile_grid(mp), mp->in, mp->wl, dt, mp->slots,
+        mp->cap_f, mp->cap_w, reinterpret_cast<unsigned int *>(mp->slots + 8));
+    return SPHX_OK;
+}
+
+template <int D>
+int launch_second_tiled(sphx_mp mp, unsigned blk, double dt)
+{
+    const size_t bytes = 36 * size_t(mp->cap_f + mp->cap_w);
+    SPHX_TRY(grant_smem(mp, 2, k_mp_second_tiled<D>, bytes));
+    k_mp_second_tiled<D><<<mp->ntiles_ne, blk, bytes, mp->ctx->stream>>>(
+        mp->n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset, tile_grid(mp), mp->in, mp->wl, dt, mp->slots + 1,
+        mp->cap_f, mp->cap_w, reinterpret_cast<unsigned int *>(mp->slots + 8));
+    return SPHX_OK;
+}
+
 template <int D>
 int substep(sphx_mp mp, double dt)
 {
@@ -752,6 +1180,10 @@ int substep(sphx_mp mp, double dt)
     size_t n = mp->n;
     if (n == 0)
         return SPHX_OK;
+    // the lists follow the strategy they were built for; the build reads the geometry of
+    // the last configuration update only, so a rebuild here gives the same lists and sums
+    if (!mp->k.periodic && (mp->strategy == 2) != (mp->lists_strategy == 2))
+        SPHX_TRY(launch_build<D>(mp));
     unsigned blk = unsigned(mp->block);
     k_mp_init1<<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.drho, mp->a.drho_dt, mp->a.dyn, mp->k.p.p0_over_rho0,
                                                 float(0.5 * dt));
@@ -775,12 +1207,12 @@ int substep(sphx_mp mp, double dt)
             k_mp_first_periodic<D, false><<<grid_for(n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->f_offset, mp->in, dt,
                                                                           mp->slots);
     }
-    else if (mp->strategy == 0)
-        k_mp_first<D, true><<<grid_for(n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset,
-                                                            mp->in, mp->wl, dt, mp->slots);
+    else if (mp->lists_tiled)
+        SPHX_TRY(launch_first_tiled<D>(mp, blk, dt));
+    else if (mp->strategy != 1)
+        mp->order_active ? launch_first<D, true, true>(mp, blk, dt) : launch_first<D, true, false>(mp, blk, dt);
     else
-        k_mp_first<D, false><<<grid_for(n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset,
-                                                             mp->in, mp->wl, dt, mp->slots);
+        mp->order_active ? launch_first<D, false, true>(mp, blk, dt) : launch_first<D, false, false>(mp, blk, dt);
     SPHX_LAUNCHED(ctx);
     if (e[1])
         SPHX_CUDA(cudaEventRecord(e[1], s));
@@ -793,12 +1225,12 @@ int substep(sphx_mp mp, double dt)
         else
             launch_second_periodic<D, false>(mp, blk, dt);
     }
-    else if (mp->strategy == 0)
-        k_mp_second<D, true><<<grid_for(n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset,
-                                                             mp->in, mp->wl, dt, mp->slots + 1);
+    else if (mp->lists_tiled)
+        SPHX_TRY(launch_second_tiled<D>(mp, blk, dt));
+    else if (mp->strategy != 1)
+        mp->order_active ? launch_second<D, true, true>(mp, blk, dt) : launch_second<D, true, false>(mp, blk, dt);
     else
-        k_mp_second<D, false><<<grid_for(n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->f_offset, mp->w,
-                                                              mp->w_offset, mp->in, mp->wl, dt, mp->slots + 1);
+        mp->order_active ? launch_second<D, false, true>(mp, blk, dt) : launch_second<D, false, false>(mp, blk, dt);
     SPHX_LAUNCHED(ctx);
     if (e[3])
         SPHX_CUDA(cudaEventRecord(e[3], s));
@@ -1033,11 +1465,19 @@ extern "C" int sphx_mp_create(sphx_relation inner, sphx_relation wall, const sph
     mp->w.nw = nw;
     mp->in.count = mp->alloc<uint32_t>(n);
     mp->wl.count = mp->alloc<uint32_t>(n);
-    mp->slots = mp->alloc<unsigned long long>(8);
+    mp->slots = mp->alloc<unsigned long long>(10);
+    mp->order = mp->alloc<uint32_t>(n);
+    mp->tile_offset = mp->alloc<uint32_t>(nc + 1);
+    mp->tiles = mp->alloc<uint32_t>(nc);
+    mp->tile_flags = mp->alloc<uint32_t>(nc);
+    mp->tile_pos = mp->alloc<uint32_t>(nc);
     if (!mp->f_offset || !mp->w_offset || !mp->count || !mp->key || !mp->rank || !mp->perm || !mp->ncell ||
-        !mp->noff || !mp->w.geo || !mp->w.n || !mp->in.count || !mp->wl.count || !mp->slots)
+        !mp->noff || !mp->w.geo || !mp->w.n || !mp->in.count || !mp->wl.count || !mp->slots || !mp->order ||
+        !mp->tile_offset || !mp->tiles || !mp->tile_flags || !mp->tile_pos)
         return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "mixed-precision allocation failed"));
-    if (cudaMallocHost(&mp->h_slots, 8 * sizeof(unsigned long long)) != cudaSuccess)
+    if (cudaMemsetAsync(mp->slots, 0, 10 * sizeof(unsigned long long), ctx->stream) != cudaSuccess)
+        return bail(fail(SPHX_ERR_CUDA, "slot initialisation failed"));
+    if (cudaMallocHost(&mp->h_slots, 10 * sizeof(unsigned long long)) != cudaSuccess)
         return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "pinned allocation failed"));
     if ((st = alloc_lists(mp, mp->in, D == 2 ? 24 : 96)) != SPHX_OK ||
         (st = alloc_lists(mp, mp->wl, D == 2 ? 16 : 64)) != SPHX_OK)
@@ -1182,11 +1622,13 @@ extern "C" int sphx_mp_create_periodic(sphx_body fb, const sphx_fluid_params *p,
     mp->noff = mp->alloc<float>(3 * n);
     mp->in.count = mp->alloc<uint32_t>(n);
     mp->wl.count = mp->alloc<uint32_t>(n);
-    mp->slots = mp->alloc<unsigned long long>(8);
+    mp->slots = mp->alloc<unsigned long long>(10);
     if (!mp->f_offset || !mp->w_offset || !mp->count || !mp->key || !mp->rank || !mp->perm || !mp->ncell ||
         !mp->noff || !mp->in.count || !mp->wl.count || !mp->slots)
         return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "mixed-precision allocation failed"));
-    if (cudaMallocHost(&mp->h_slots, 8 * sizeof(unsigned long long)) != cudaSuccess)
+    if (cudaMemsetAsync(mp->slots, 0, 10 * sizeof(unsigned long long), ctx->stream) != cudaSuccess)
+        return bail(fail(SPHX_ERR_CUDA, "slot initialisation failed"));
+    if (cudaMallocHost(&mp->h_slots, 10 * sizeof(unsigned long long)) != cudaSuccess)
         return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "pinned allocation failed"));
     if ((st = alloc_lists(mp, mp->in, D == 2 ? 24 : 96)) != SPHX_OK || (st = alloc_lists(mp, mp->wl, 1)) != SPHX_OK)
         return bail(st);
@@ -1519,11 +1961,41 @@ extern "C" int sphx_mp_autotune(sphx_mp mp, int reps, int *best_block, int *best
 
 extern "C" int sphx_mp_set_tuning(sphx_mp mp, int block, int strategy)
 {
-    if (!mp || block < 64 || block > 256 || block % 32 != 0 || strategy < 0 || strategy > 1)
-        return fail(SPHX_ERR_INVALID_ARG, "block must be 64..256 in steps of 32, strategy 0 or 1");
+    if (!mp || block < 64 || block > 256 || block % 32 != 0 || strategy < 0 || strategy > 2)
+        return fail(SPHX_ERR_INVALID_ARG, "block must be 64..256 in steps of 32, strategy 0, 1 or 2");
+    if (strategy == 2 && mp->k.periodic)
+        return fail(SPHX_ERR_INVALID_ARG, "the tiled strategy serves the dam-break solver only");
+    if (strategy == 2 && (mp->tile[0] > kTileMaxExtent || mp->tile[1] > kTileMaxExtent || mp->tile[2] > kTileMaxExtent))
+        return fail(SPHX_ERR_INVALID_ARG, "the tiled strategy takes tiles of at most %d sub-cells per axis",
+                    kTileMaxExtent);
     mp->block = block;
     mp->strategy = strategy;
-    return SPHX_OK;
+    if (strategy == 2 && !mp->tile[0])
+    {
+        mp->tile[0] = mp->tile[1] = 4;
+        mp->tile[2] = mp->dim == 3 ? 4 : 0;
+    }
+    return SPHX_OK; // the lists follow at the next sub-step (substep rebuilds them)
+}
+
+extern "C" int sphx_mp_set_tile(sphx_mp mp, int tx, int ty, int tz)
+{
+    if (!mp || tx < 0 || ty < 0 || tz < 0 || tx > 64 || ty > 64 || tz > 64 || (tx == 0) != (ty == 0) ||
+        (mp->dim == 3 && (tx == 0) != (tz == 0)))
+        return fail(SPHX_ERR_INVALID_ARG, "tile extents must be 1..64 sub-cells per axis, or all 0 (off)");
+    if (tx && mp->k.periodic)
+        return fail(SPHX_ERR_INVALID_ARG, "the tile-grouped traversal serves the dam-break solver only");
+    if (mp->strategy == 2 && (!tx || tx > kTileMaxExtent || ty > kTileMaxExtent || tz > kTileMaxExtent))
+        return fail(SPHX_ERR_INVALID_ARG, "the tiled strategy takes tiles of 1..%d sub-cells per axis",
+                    kTileMaxExtent);
+    SPHX_TRY(settle_configuration(mp));
+    mp->tile[0] = tx;
+    mp->tile[1] = ty;
+    mp->tile[2] = mp->dim == 3 ? tz : 0;
+    if (mp->n == 0)
+        return SPHX_OK;
+    // the order (and, for the tiled strategy, the staged-index lists) of the new shape
+    return mp->dim == 2 ? launch_build<2>(mp) : launch_build<3>(mp);
 }
 
 extern "C" int sphx_mp_advection_step(sphx_mp mp, int loop_style, int *substeps, double *advection_dt,
@@ -1594,6 +2066,35 @@ extern "C" int sphx_mp_conservation(sphx_mp mp, double *out)
             s += h[b * 5 + q];
         out[q] = s;
     }
+    return SPHX_OK;
+}
+
+extern "C" int sphx_mp_check_state(sphx_mp mp, uint64_t *non_finite, uint64_t *out_of_mesh)
+{
+    if (!mp)
+        return fail(SPHX_ERR_INVALID_ARG, "null solver");
+    sphx_ctx ctx = mp->ctx;
+    SPHX_CUDA(cudaMemsetAsync(mp->slots + 4, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    if (mp->n > 0)
+    {
+        unsigned g = unsigned(std::max(1, std::min(ctx->num_sms * 4, int(grid_for(mp->n, 256)))));
+        if (mp->dim == 2)
+            k_mp_check<2><<<g, 256, 0, ctx->stream>>>(mp->n, mp->k, mp->a, mp->slots + 4);
+        else
+            k_mp_check<3><<<g, 256, 0, ctx->stream>>>(mp->n, mp->k, mp->a, mp->slots + 4);
+        SPHX_LAUNCHED(ctx);
+    }
+    SPHX_CUDA(cudaMemcpyAsync(mp->h_slots + 4, mp->slots + 4, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                              ctx->stream));
+    SPHX_CUDA(cudaStreamSynchronize(ctx->stream));
+    const uint64_t nf = mp->h_slots[4], om = mp->h_slots[5];
+    if (non_finite)
+        *non_finite = nf;
+    if (out_of_mesh)
+        *out_of_mesh = om;
+    if (nf || om)
+        return fail(SPHX_ERR_NUMERIC, "mixed-precision state: %llu particles with non-finite values, %llu outside the mesh",
+                    (unsigned long long)nf, (unsigned long long)om);
     return SPHX_OK;
 }
 

@@ -115,6 +115,27 @@ __host__ __device__ __forceinline__ void unpack_cell(uint32_t p, int *c)
         c[d] = int((p >> (d * CellLanes<D>::bits)) & CellLanes<D>::mask);
 }
 
+// Tile-grouped traversal of the sweeps: the sub-cells are grouped in boxes of t[0] x t[1]
+// (x t[2]) sub-cells and the particles of one box are handed to consecutive threads, so a
+// block's neighbour records span a compact window that stays in L1 instead of the long
+// column a run of consecutive particles spans in the linear cell order.  The particle
+// order, the neighbour lists and the arithmetic are unchanged: only which thread handles
+// which particle.  nt[d] = boxes along axis d; t[0] == 0 turns the grouping off.
+struct TileShape
+{
+    int t[3], nt[3];
+};
+
+template <int D>
+__device__ __forceinline__ uint32_t tile_key(const TileShape &ts, const int *c)
+{
+    uint32_t k = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        k = k * uint32_t(ts.nt[d]) + uint32_t(c[d] / ts.t[d]);
+    return k;
+}
+
 struct MPParams
 {
     float gs_f, rc_sqr, inv_h, fW;
@@ -131,7 +152,39 @@ struct MPParams
     float mu2, eps_h, tvc_scale, tvc_lim;
 };
 
+// The reference's lattice number density (computeLatticeNumberDensity, adaptation.cpp:25-58:
+// W summed over the lattice points i dp closer than the cut-off) evaluated with this
+// solver's FP32 kernel, i.e. the arithmetic of wc2_W on the rounded constants fW and 1 / h
+// and the squared distance as the sweeps form it, accumulated in FP64.  The density
+// summation divides FP32 kernel sums by it, so the rounding of fW and 1 / h (up to 3 x 2^-24
+// relative in the sum, 4e-5 of pressure at c0^2 = 240) cancels as it does in the
+// reference's FP32 build, where sigma0 and the sums share one precision.
+inline double lattice_sigma_fp32(int dim, float fW, float inv_h, double cutoff, double dp)
+{
+    const int depth = int(cutoff / dp) + 1;
+    double sigma = 0.0;
+    const int kd = dim == 3 ? depth : 0;
+    for (int k = -kd; k <= kd; ++k)
+        for (int j = -depth; j <= depth; ++j)
+            for (int i = -depth; i <= depth; ++i)
+            {
+                const double x = i * dp, y = j * dp, z = k * dp;
+                if (!(std::sqrt(x * x + y * y + z * z) < cutoff))
+                    continue;
+                const float xf = float(x), yf = float(y), zf = float(z);
+                const float r2 = std::fma(zf, zf, std::fma(yf, yf, xf * xf));
+                const float q = std::sqrt(r2) * inv_h;
+                const float t = 1.0f - 0.5f * q;
+                const float t2 = t * t;
+                const float w = t2 * t2;
+                const float poly = w * (1.0f + 2.0f * q);
+                sigma += double(fW * poly);
+            }
+    return sigma;
+}
+
 // Constants of one fluid body against one static wall (same rounding for every solver).
+// sigma0 is replaced by lattice_sigma_fp32 of the same lattice (spacing vol^(1/dim)).
 inline MPParams make_params(int dim, double grid_spacing, double h, double rho0, double c0, double vol, double mass,
                             double sigma0, double wall_mass_over_rho0, double wall_vol, double limiter_slope,
                             const double *gravity)
@@ -150,6 +203,9 @@ inline MPParams make_params(int dim, double grid_spacing, double h, double rho0,
     k.Vol = float(vol);
     k.mass = float(mass);
     k.inv_mass = float(1.0 / mass);
+    const double dp = dim == 3 ? std::cbrt(vol) : std::sqrt(vol);
+    (void)sigma0; // the FP64 lattice sum of the drop-in; see lattice_sigma_fp32
+    sigma0 = lattice_sigma_fp32(dim, k.fW, k.inv_h, wk.rc, dp);
     k.sigma0 = sigma0;
     k.rho0_over_sigma0 = float(rho0 / sigma0);
     k.wall_factor = float(wall_mass_over_rho0 * rho0 * rho0 / (sigma0 * mass));
@@ -315,12 +371,13 @@ __device__ __forceinline__ void axis_reach(float o, float inv_gs, float r, int &
     lo = max(0, min(kReach, int(ceilf((r - o) * inv_gs))));
 }
 
-// Candidates of the pruned (2 kReach + 1)^D window around sub-cell c; the cells of one
-// instance start at cell_base (columns along the last axis are contiguous in the linear
-// cell order).
-template <int D, bool PRUNE, class F>
-__device__ __forceinline__ void for_each_candidate(const MeshDev &m, uint32_t cell_base, const uint32_t *offset,
-                                                   const int *c, const Reach &q, F &&f)
+// Candidate runs of the pruned (2 kReach + 1)^D window around sub-cell c: run(x, y, b, e)
+// for every column (x, y) of the window (x alone in 2D) with the candidate particles
+// [b, e) of its cells along the last axis; the cells of one instance start at cell_base
+// (columns along the last axis are contiguous in the linear cell order).
+template <int D, bool PRUNE, class R>
+__device__ __forceinline__ void for_each_candidate_run(const MeshDev &m, uint32_t cell_base, const uint32_t *offset,
+                                                       const int *c, const Reach &q, R &&run)
 {
     if (!PRUNE)
     {
@@ -331,9 +388,7 @@ __device__ __forceinline__ void for_each_candidate(const MeshDev &m, uint32_t ce
             for (int x = lo0; x <= hi0; ++x)
             {
                 uint32_t a = cell_base + uint32_t(x) * uint32_t(m.all_cells[1]);
-                uint32_t b = offset[a + uint32_t(lo1)], e = offset[a + uint32_t(hi1) + 1];
-                for (uint32_t j = b; j < e; ++j)
-                    f(j);
+                run(x, 0, offset[a + uint32_t(lo1)], offset[a + uint32_t(hi1) + 1]);
             }
         }
         else
@@ -344,9 +399,7 @@ __device__ __forceinline__ void for_each_candidate(const MeshDev &m, uint32_t ce
                 {
                     uint32_t a = cell_base +
                                  (uint32_t(x) * uint32_t(m.all_cells[1]) + uint32_t(y)) * uint32_t(m.all_cells[2]);
-                    uint32_t b = offset[a + uint32_t(lo2)], e = offset[a + uint32_t(hi2) + 1];
-                    for (uint32_t j = b; j < e; ++j)
-                        f(j);
+                    run(x, y, offset[a + uint32_t(lo2)], offset[a + uint32_t(hi2) + 1]);
                 }
         }
         return;
@@ -364,9 +417,7 @@ __device__ __forceinline__ void for_each_candidate(const MeshDev &m, uint32_t ce
             axis_reach(q.o[1], q.inv_gs, sqrtf(fmaxf(r2 - gx * gx, 0.0f)), l1, h1);
             const int lo1 = max(c[1] - l1, 0), hi1 = min(c[1] + h1, m.all_cells[1] - 1);
             uint32_t a = cell_base + uint32_t(x) * uint32_t(m.all_cells[1]);
-            uint32_t b = offset[a + uint32_t(lo1)], e = offset[a + uint32_t(hi1) + 1];
-            for (uint32_t j = b; j < e; ++j)
-                f(j);
+            run(x, 0, offset[a + uint32_t(lo1)], offset[a + uint32_t(hi1) + 1]);
         }
     }
     else
@@ -388,12 +439,21 @@ __device__ __forceinline__ void for_each_candidate(const MeshDev &m, uint32_t ce
                 const int lo2 = max(c[2] - l2, 0), hi2 = min(c[2] + h2, m.all_cells[2] - 1);
                 uint32_t a = cell_base +
                              (uint32_t(x) * uint32_t(m.all_cells[1]) + uint32_t(y)) * uint32_t(m.all_cells[2]);
-                uint32_t b = offset[a + uint32_t(lo2)], e = offset[a + uint32_t(hi2) + 1];
-                for (uint32_t j = b; j < e; ++j)
-                    f(j);
+                run(x, y, offset[a + uint32_t(lo2)], offset[a + uint32_t(hi2) + 1]);
             }
         }
     }
+}
+
+// Candidates of the pruned window one by one: f(j) in run order.
+template <int D, bool PRUNE, class F>
+__device__ __forceinline__ void for_each_candidate(const MeshDev &m, uint32_t cell_base, const uint32_t *offset,
+                                                   const int *c, const Reach &q, F &&f)
+{
+    for_each_candidate_run<D, PRUNE>(m, cell_base, offset, c, q, [&](int, int, uint32_t b, uint32_t e) {
+        for (uint32_t j = b; j < e; ++j)
+            f(j);
+    });
 }
 
 // Neighbour visits of one particle: stored lists (LISTS) or a sweep of the sub-cells with

@@ -388,6 +388,56 @@ extern "C" int sphx_body_device_ptr(sphx_body b, const char *name, void **dev, s
     return SPHX_OK;
 }
 
+namespace
+{
+// Particles of an SoA variable (component c of particle i at v[c * n + i]) with a
+// non-finite component; one atomic per particle found.
+template <typename T>
+__global__ void k_count_non_finite(size_t n, int ncomp, const T *__restrict__ v, unsigned long long *count)
+{
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+    {
+        bool fin = true;
+        for (int c = 0; c < ncomp; ++c)
+            fin = fin && isfinite(v[size_t(c) * n + i]);
+        if (!fin)
+            atomicAdd(count, 1ull);
+    }
+}
+} // namespace
+
+extern "C" int sphx_body_check_finite(sphx_body b, const char *name, uint64_t *non_finite)
+{
+    if (!b || !name)
+        return fail(SPHX_ERR_INVALID_ARG, "invalid check arguments");
+    Field *f = b->find(name);
+    if (!f)
+        return fail(SPHX_ERR_NOT_FOUND, "variable %s is not registered", name);
+    if (f->dtype != SPHX_F64 && f->dtype != SPHX_F32)
+        return fail(SPHX_ERR_INVALID_ARG, "variable %s is not a floating-point variable", name);
+    sphx_ctx ctx = b->ctx;
+    SPHX_TRY(ctx->ensure_scratch(sizeof(unsigned long long)));
+    unsigned long long *d = static_cast<unsigned long long *>(ctx->d_scratch);
+    SPHX_CUDA(cudaMemsetAsync(d, 0, sizeof(unsigned long long), ctx->stream));
+    if (b->n > 0)
+    {
+        unsigned g = unsigned(std::max(1, std::min(ctx->num_sms * 4, int(grid_for(b->n, 256)))));
+        if (f->dtype == SPHX_F64)
+            k_count_non_finite<<<g, 256, 0, ctx->stream>>>(b->n, f->ncomp, static_cast<const double *>(f->dev), d);
+        else
+            k_count_non_finite<<<g, 256, 0, ctx->stream>>>(b->n, f->ncomp, static_cast<const float *>(f->dev), d);
+        SPHX_LAUNCHED(ctx);
+    }
+    unsigned long long h = 0;
+    SPHX_CUDA(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    SPHX_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (non_finite)
+        *non_finite = h;
+    if (h)
+        return fail(SPHX_ERR_NUMERIC, "variable %s: %llu particles with non-finite values", name, h);
+    return SPHX_OK;
+}
+
 extern "C" int sphx_mesh_from_bounds(int dim, const double *lower, const double *upper, double gs, int buffer_width,
                                      sphx_mesh_desc *out)
 {

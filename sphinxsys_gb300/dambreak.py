@@ -156,6 +156,10 @@ class MixedPrecisionDamBreak:
     def set_tuning(self, block: int, strategy: int) -> None:
         self._N.call("sphx_mp_set_tuning", self.handle, int(block), int(strategy))
 
+    def set_tile(self, tx: int, ty: int, tz: int = 0) -> None:
+        """Tile-grouped traversal (sphx_mp_set_tile); 0, 0, 0 keeps the cell order."""
+        self._N.call("sphx_mp_set_tile", self.handle, int(tx), int(ty), int(tz))
+
     def advection_step(self):
         C, N = self._C, self._N
         sub = C.c_int()
@@ -262,6 +266,16 @@ class MixedPrecisionDamBreak:
         out = np.zeros(5)
         self._N.call("sphx_mp_conservation", self.handle, out.ctypes.data_as(C.POINTER(C.c_double)))
         return out
+
+    def check_state(self):
+        """(particles with a non-finite value, finite particles outside the mesh) of the
+        solver state (sphx_mp_check_state)."""
+        C = self._C
+        nf, om = C.c_uint64(), C.c_uint64()
+        st = self._N.load().sphx_mp_check_state(self.handle, C.byref(nf), C.byref(om))
+        if st not in (self._N.SPHX_OK, 7):  # 7: SPHX_ERR_NUMERIC, reported through the counts
+            self._N.check(st)
+        return int(nf.value), int(om.value)
 
     def upper_front(self, axis: int, lower, upper) -> float:
         C = self._C

@@ -55,6 +55,7 @@ SIGNATURES = {
     "sphx_body_upload_rows": (_i, [_vp, C.c_char_p, _vp, _sz, _sz]),
     "sphx_body_download_rows": (_i, [_vp, C.c_char_p, _vp, _sz, _sz]),
     "sphx_body_device_ptr": (_i, [_vp, C.c_char_p, _pvp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "sphx_body_check_finite": (_i, [_vp, C.c_char_p, _pu64]),
     "sphx_mesh_from_bounds": (_i, [_i, _pd, _pd, _d, _i, C.POINTER(MeshDesc)]),
     "sphx_cell_list_create": (_i, [_vp, C.POINTER(MeshDesc), _sz, _pvp]),
     "sphx_cell_list_destroy": (_i, [_vp]),
@@ -109,7 +110,9 @@ SIGNATURES = {
     "sphx_mp_download_host": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "sphx_mp_conservation": (_i, [_vp, _pd]),
     "sphx_mp_upper_front": (_i, [_vp, _i, _pd, _pd, _pd]),
+    "sphx_mp_check_state": (_i, [_vp, _pu64, _pu64]),
     "sphx_mp_set_tuning": (_i, [_vp, _i, _i]),
+    "sphx_mp_set_tile": (_i, [_vp, _i, _i, _i]),
     "sphx_mp_set_profiling": (_i, [_vp, _i]),
     "sphx_mp_autotune": (_i, [_vp, _i, C.POINTER(C.c_int), C.POINTER(C.c_int), _pd]),
     "sphx_mp_kernel_times": (_i, [_vp, _pd]),
@@ -118,6 +121,7 @@ SIGNATURES = {
     "sphx_batch_destroy": (_i, [_vp]),
     "sphx_batch_advection_step": (_i, [_vp, _i, C.POINTER(C.c_int), _pd]),
     "sphx_batch_set_tuning": (_i, [_vp, _i]),
+    "sphx_batch_set_substep_cap": (_i, [_vp, _i]),
     "sphx_batch_graph_launches": (_i, [_vp, _pu64]),
     "sphx_batch_download": (_i, [_vp, _i, _pd, _pd, _pd, _pd]),
     "sphx_batch_size": (_i, [_vp, _psz, _psz]),

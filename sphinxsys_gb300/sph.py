@@ -303,6 +303,15 @@ class SPHBody:
         N.call("sphx_body_download", self.handle, name.encode(), res.ctypes.data_as(C.c_void_p), self.n)
         return res[:, 0].copy() if nc.value == 1 else res
 
+    def count_non_finite(self, name: str) -> int:
+        """Particles of a floating-point variable with a NaN or infinite component
+        (sphx_body_check_finite; 0 when the variable is finite)."""
+        out = C.c_uint64()
+        st = N.load().sphx_body_check_finite(self.handle, name.encode(), C.byref(out))
+        if st not in (N.SPHX_OK, 7):  # 7: SPHX_ERR_NUMERIC, reported through the count
+            N.check(st)
+        return int(out.value)
+
     def upload_rows(self, name: str, values: np.ndarray, first: int) -> None:
         """Writes rows [first, first + len(values)) of a registered variable."""
         a = np.ascontiguousarray(values)

@@ -84,4 +84,7 @@ def main(root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SPHINXSYS_REFERENCE")
+    if not src:
+        sys.exit("usage: python make_golden.py <SPHinXsys source tree> (or set SPHINXSYS_REFERENCE)")
+    main(src)

@@ -100,3 +100,28 @@ def test_batch_rejects_mixed_dimensions():
     insts = [small_instances(2, 1, seed=5)[0], small_instances(3, 1, seed=5)[0]]
     with pytest.raises(ValueError):
         BatchDamBreak(insts)
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_substep_cap_ends_the_step_with_timeout(use_graph):
+    """An instance that needs more acoustic sub-steps than the cap allows stops relaxing; the
+    step finishes its configuration update and reports SPHX_ERR_TIMEOUT (the graph's WHILE
+    loop ends on the cap, so nothing waits).  Lifting the cap, the batch steps on."""
+    from sphinxsys_gb300.native import SphxError
+    insts = small_instances(2, 2, seed=6)
+    b = BatchDamBreak(insts, use_graph=use_graph)
+    first = b.advection_step()
+    assert int(first.min()) >= 3, first  # dam breaks take ~5 sub-steps per advection step
+    b.set_substep_cap(2)
+    with pytest.raises(SphxError) as e:
+        b.advection_step()
+    assert e.value.code == 6, e.value  # SPHX_ERR_TIMEOUT
+    b.set_substep_cap(int(first.max()) + 50)
+    again = b.advection_step()
+    assert int(again.min()) >= 1
+    for q in range(len(insts)):
+        for x in b.download(q):
+            assert np.all(np.isfinite(x))
+    for bad in (0, -1, (1 << 20) + 1):
+        with pytest.raises(SphxError):
+            b.set_substep_cap(bad)

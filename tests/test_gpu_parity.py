@@ -180,9 +180,59 @@ def test_fields_3d(case):
     compare_neighbors(sim.water_block_inner.neighbors(), oc.neighbors(O.INNER), 3)
     compare_neighbors(sim.water_wall_contact.neighbors(), oc.neighbors(O.CONTACT), 3, contact=True)
     subs = run_both(sim, oc, 10)
-    assert sum(subs) >= 40
+    while sum(subs) < 100:  # at least 100 acoustic steps
+        subs += run_both(sim, oc, 1)
     errs = compare_fields(sim, oc)
     assert max(errs.values()) < FIELD_RTOL, errs
+    assert rel_err(sim.recorded_pressure.exec(), oc.observe_pressure()) < 1e-9
+
+
+def pair_lists(counts_len, gpu_relation=None, oracle=None, which=None):
+    """Neighbour counts and indices only (the per-pair kernel values of a 1.7M-particle
+    relation would take several GB)."""
+    counts = np.zeros(counts_len, dtype=np.uint32)
+    u32 = C.POINTER(C.c_uint32)
+    if gpu_relation is not None:
+        total = C.c_size_t()
+        native.call("sphx_relation_download", gpu_relation.handle, counts.ctypes.data_as(u32), None, None, None,
+                    None, None, C.byref(total))
+        j = np.zeros(int(counts.sum()), dtype=np.uint32)
+        native.call("sphx_relation_download", gpu_relation.handle, counts.ctypes.data_as(u32), j.ctypes.data_as(u32),
+                    None, None, None, None, C.byref(total))
+    else:
+        O.lib().orc_get_neighbors(oracle.h, which, O._p(counts), None, None, None, None, None)
+        j = np.zeros(int(counts.sum()), dtype=np.uint32)
+        O.lib().orc_get_neighbors(oracle.h, which, O._p(counts), O._p(j), None, None, None, None)
+    return counts, j
+
+
+def test_fields_at_fp64_config_size():
+    """The FP64 drop-in against the oracle on the 3D dam break at dp = 0.0075 (tank
+    3.2 x 1.0 x 1.8, 1,702,400 fluid particles): cell lists, inner and wall pair lists equal
+    at the start and after 20 advection steps (100+ acoustic steps), fields within 1e-10."""
+    import os
+    O.set_num_threads(os.cpu_count() or 1)
+    case = cases.dambreak_3d(0.0075)
+    sim, oc = DamBreak(case), O.OracleCase(case)
+    n = sim.water_block.n
+    assert n == oc.n(O.FLUID) == 1_702_400
+
+    def same_pairs():
+        for rel, which in ((sim.water_block_inner, O.INNER), (sim.water_wall_contact, O.CONTACT)):
+            cg, jg = pair_lists(n, gpu_relation=rel)
+            co, jo = pair_lists(n, oracle=oc, which=which)
+            assert np.array_equal(cg, co) and np.array_equal(jg, jo), which
+        off, idx = sim.water_block.cell_list_arrays()
+        ooff, oidx = oc.cell_list(O.FLUID)
+        assert np.array_equal(off, ooff) and np.array_equal(idx, oidx)
+
+    same_pairs()
+    subs = run_both(sim, oc, 20)
+    assert sum(subs) >= 100, subs
+    errs = compare_fields(sim, oc)
+    print(case.name, sum(subs), errs)
+    assert max(errs.values()) < FIELD_RTOL, errs
+    same_pairs()
     assert rel_err(sim.recorded_pressure.exec(), oc.observe_pressure()) < 1e-9
 
 
