@@ -354,9 +354,12 @@ int sphx_mp_upper_front(sphx_mp mp, int axis, const double *region_lower, const 
  * (synchronises; reads the state only).  No counterpart in the reference, which clamps
  * such particles into the boundary cells (base_mesh.hxx:9-15) or ends the process. */
 int sphx_mp_check_state(sphx_mp mp, uint64_t *non_finite, uint64_t *out_of_mesh);
-/* Kernel launch shape and neighbour strategy: block size (64..1024, multiple of 32) of
+/* Kernel launch shape and neighbour strategy: block size (64..256, multiple of 32) of
  * the sweep kernels, and 0 = stored neighbour index lists, 1 = cell sweep every
- * sub-step. */
+ * sub-step, 2 = tiled (dam-break solver): one block per tile of sub-cells with the tile's
+ * neighbour window staged in shared memory and lists of indices into it (tile shape from
+ * sphx_mp_set_tile, 4 x 4 (x 4) by default, at most 8 per axis).  All three give the same
+ * results bit for bit. */
 int sphx_mp_set_tuning(sphx_mp mp, int block, int strategy);
 /* Tile-grouped traversal of the sweeps and the neighbour build (dam-break solver): the
  * particles of each box of tx x ty (x tz) sub-cells go to consecutive threads, so a thread
@@ -365,9 +368,12 @@ int sphx_mp_set_tuning(sphx_mp mp, int block, int strategy);
  * particle_for (particle_iterators_sycl.h:229-241), whose work-groups follow the storage
  * order. */
 int sphx_mp_set_tile(sphx_mp mp, int tx, int ty, int tz);
-/* Times one acoustic sub-step for every block size (64, 128, 256) and both neighbour
- * strategies, restores the state it advanced, and keeps the fastest setting; outputs
- * (any may be null) the chosen block, strategy and ms per sub-step. */
+/* Current launch block, neighbour strategy and tile shape (tile: 3 ints; any may be null). */
+int sphx_mp_get_tuning(sphx_mp mp, int *block, int *strategy, int *tile);
+/* Times one acoustic sub-step for every block size (64, 128, 256) with each neighbour
+ * strategy (the tiled one with several tile shapes), restores the state it advanced,
+ * and keeps the fastest setting; outputs (any may be null) the chosen block, strategy and
+ * ms per sub-step (sphx_mp_get_tuning gives the tile shape). */
 int sphx_mp_autotune(sphx_mp mp, int reps, int *best_block, int *best_strategy, double *best_ms);
 /* CUDA-event timing of the two sweep kernels of every sub-step (on the context's
  * stream); switching it resets the totals. */

@@ -96,7 +96,7 @@ __device__ __forceinline__ void hash_position(const BInst &k, const double *x, u
     sub_cell_index<D>(k.m, k.inv_gs, x, c);
 #pragma unroll
     for (int d = 0; d < D; ++d)
-        noff[d * n + i] = float(x[d] - cell_corner(k.m, d, c[d]));
+        stage_offset(noff, n, i, d, x[d] - cell_corner(k.m, d, c[d]));
     store_hash<D>(k, c, ncell, i, key, rank, cnt);
 }
 
@@ -118,26 +118,25 @@ __global__ void k_b_from_fp64(size_t n, const double *__restrict__ pos, const ui
 }
 
 template <int D>
-__global__ void k_b_rehash(size_t n, const float4 *__restrict__ geo0, const float *__restrict__ off,
-                           const uint32_t *__restrict__ starts, int count, const BInst *__restrict__ inst,
-                           uint32_t *__restrict__ ncell, float *__restrict__ noff, uint32_t *__restrict__ key,
-                           uint32_t *__restrict__ rank, uint32_t *__restrict__ cnt)
+__global__ void k_b_rehash(size_t n, MPState f, const uint32_t *__restrict__ starts, int count,
+                           const BInst *__restrict__ inst, uint32_t *__restrict__ ncell, float *__restrict__ noff,
+                           uint32_t *__restrict__ key, uint32_t *__restrict__ rank, uint32_t *__restrict__ cnt)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
     const BInst &k = inst[find_instance(starts, count, uint32_t(i))];
     int c0[3];
-    unpack_cell<D>(__float_as_uint(geo0[i].w), c0);
-    float o[3] = {0.f, 0.f, 0.f}, no[3];
+    unpack_cell<D>(__float_as_uint(f.geo0[i].w), c0);
+    double o[3] = {0.0, 0.0, 0.0}, no[3];
 #pragma unroll
     for (int d = 0; d < D; ++d)
-        o[d] = off[d * n + i];
+        o[d] = offset_of(f, n, i, d);
     int c[3] = {0, 0, 0};
     rehash_relative<D>(k.m, k.inv_gs, false, c0, o, c, no);
 #pragma unroll
     for (int d = 0; d < D; ++d)
-        noff[d * n + i] = no[d];
+        stage_offset(noff, n, i, d, no[d]);
     store_hash<D>(k, c, ncell, i, key, rank, cnt);
 }
 
@@ -184,6 +183,7 @@ __global__ void k_b_gather(size_t n, const uint32_t *__restrict__ perm, const ui
     {
         o[d] = noff[d * n + i];
         dst.off[d * n + k] = o[d];
+        dst.off_lo[d * n + k] = noff[(3 + d) * n + i];
         dst.force[d * n + k] = src.force[d * n + i];
     }
     dst.geo0[k] = make_float4(o[0], o[1], o[2], __uint_as_float(ncell[i]));
@@ -412,7 +412,7 @@ __global__ void k_b_download(size_t n, const uint32_t *__restrict__ starts, int 
 #pragma unroll
     for (int d = 0; d < D; ++d)
     {
-        out[d * stride + o] = cell_corner(k.m, d, c[d]) + double(f.off[d * n + i]);
+        out[d * stride + o] = cell_corner(k.m, d, c[d]) + offset_of(f, n, i, d);
         out[(D + d) * stride + o] = v[d];
     }
     out[(2 * D) * stride + o] = double(k.p.rho0) + double(f.drho[i]);
@@ -492,12 +492,13 @@ int b_alloc_state(sphx_batch bt, MPState &s)
     s.geo0 = bt->alloc<float4>(n);
     s.dyn = bt->alloc<float4>(n);
     s.off = bt->alloc<float>(D * n);
+    s.off_lo = bt->alloc<float>(D * n);
     s.force = bt->alloc<float>(D * n);
     s.drho = bt->alloc<float>(n);
     s.drho_dt = bt->alloc<float>(n);
     s.drho_sum = bt->alloc<float>(n);
     s.id = bt->alloc<uint32_t>(n);
-    if (!s.geo0 || !s.dyn || !s.off || !s.force || !s.drho || !s.drho_dt || !s.drho_sum || !s.id)
+    if (!s.geo0 || !s.dyn || !s.off || !s.off_lo || !s.force || !s.drho || !s.drho_dt || !s.drho_sum || !s.id)
         return fail(SPHX_ERR_OUT_OF_MEMORY, "batch state allocation failed");
     return SPHX_OK;
 }
@@ -553,7 +554,7 @@ int b_enqueue_configuration(sphx_batch bt, cudaStream_t s, const MPState &src, c
     if (rehash)
     {
         SPHX_CUDA(cudaMemsetAsync(bt->cnt, 0, bt->ncells * sizeof(uint32_t), s));
-        k_b_rehash<D><<<grid_for(n, 256), 256, 0, s>>>(n, src.geo0, src.off, bt->starts, bt->count, bt->inst,
+        k_b_rehash<D><<<grid_for(n, 256), 256, 0, s>>>(n, src, bt->starts, bt->count, bt->inst,
                                                        bt->ncell, bt->noff, bt->key, bt->rank, bt->cnt);
         SPHX_CUDA(cudaGetLastError());
     }
@@ -856,7 +857,7 @@ extern "C" int sphx_batch_create(sphx_ctx ctx, int dim, int count, const sphx_ba
     bt->rank = bt->alloc<uint32_t>(big);
     bt->perm = bt->alloc<uint32_t>(big);
     bt->ncell = bt->alloc<uint32_t>(n);
-    bt->noff = bt->alloc<float>(3 * n);
+    bt->noff = bt->alloc<float>(6 * n);
     bt->w.geo = bt->alloc<float4>(nw);
     bt->w.n = bt->alloc<float4>(nw);
     bt->in.count = bt->alloc<uint32_t>(n);

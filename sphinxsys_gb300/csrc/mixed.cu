@@ -83,7 +83,7 @@ __global__ void k_mp_from_fp64(size_t n, const double *__restrict__ pos, size_t 
     sub_cell_index<D>(m, k.inv_gs, x, c);
 #pragma unroll
     for (int d = 0; d < D; ++d)
-        noff[d * n + i] = float(x[d] - cell_corner(m, d, c[d]));
+        stage_offset(noff, n, i, d, x[d] - cell_corner(m, d, c[d]));
     ncell[i] = pack_cell<D>(c);
     uint32_t lc = linear_cell<D>(m, c);
     key[i] = lc;
@@ -94,9 +94,9 @@ __global__ void k_mp_from_fp64(size_t n, const double *__restrict__ pos, size_t 
 // it into its box, as PeriodicBounding does at the end of the advection step
 // (domain_bounding.h:103-113); between the position update and the next re-hash the
 // offset may still point outside the box.
-__device__ __forceinline__ double reconstruct(const MPConst &k, int d, int cell, float offset)
+__device__ __forceinline__ double reconstruct(const MPConst &k, int d, int cell, double offset)
 {
-    double x = cell_corner(k.m, d, cell) + double(offset);
+    double x = cell_corner(k.m, d, cell) + offset;
     if (k.periodic)
     {
         const double L = k.up[d] - k.lo[d];
@@ -109,25 +109,24 @@ __device__ __forceinline__ double reconstruct(const MPConst &k, int d, int cell,
 }
 
 template <int D>
-__global__ void k_mp_rehash(size_t n, const float4 *__restrict__ geo0, const float *__restrict__ off, MPConst k,
-                            uint32_t *__restrict__ ncell, float *__restrict__ noff, uint32_t *__restrict__ key,
-                            uint32_t *__restrict__ rank, uint32_t *__restrict__ count)
+__global__ void k_mp_rehash(size_t n, MPFluid f, MPConst k, uint32_t *__restrict__ ncell, float *__restrict__ noff,
+                            uint32_t *__restrict__ key, uint32_t *__restrict__ rank, uint32_t *__restrict__ count)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
     const MeshDev &m = k.m;
     int c0[3];
-    unpack_cell<D>(__float_as_uint(geo0[i].w), c0);
-    float o[3] = {0.f, 0.f, 0.f}, no[3];
+    unpack_cell<D>(__float_as_uint(f.geo0[i].w), c0);
+    double o[3] = {0.0, 0.0, 0.0}, no[3];
 #pragma unroll
     for (int d = 0; d < D; ++d)
-        o[d] = off[d * n + i];
+        o[d] = offset_of(f, n, i, d);
     int c[3] = {0, 0, 0};
     rehash_relative<D>(m, k.inv_gs, k.periodic != 0, c0, o, c, no);
 #pragma unroll
     for (int d = 0; d < D; ++d)
-        noff[d * n + i] = no[d];
+        stage_offset(noff, n, i, d, no[d]);
     ncell[i] = pack_cell<D>(c);
     uint32_t lc = linear_cell<D>(m, c);
     key[i] = lc;
@@ -178,6 +177,7 @@ __global__ void k_mp_gather(size_t n, const uint32_t *__restrict__ perm, const u
     {
         o[d] = noff[d * n + i];
         dst.off[d * n + k] = o[d];
+        dst.off_lo[d * n + k] = noff[(3 + d) * n + i];
         dst.force[d * n + k] = src.force[d * n + i];
     }
     dst.geo0[k] = make_float4(o[0], o[1], o[2], __uint_as_float(ncell[i]));
@@ -245,7 +245,7 @@ __global__ void k_mp_density_periodic(size_t n, MPFluid f)
     f.drho[i] = f.drho_sum[i];
 #pragma unroll
     for (int d = 0; d < D; ++d)
-        f.off[d * n + i] = f.off[d * n + i] + f.shift[d * n + i];
+        store_offset(f, n, i, d, offset_of(f, n, i, d) + double(f.shift[d * n + i]));
 }
 
 // DensitySummation update with the FreeSurface rule rho = max(rho_sum, rho0), at the
@@ -464,6 +464,59 @@ __global__ void __launch_bounds__(256) k_mp_second_tiled(size_t n, MPConst k, MP
     warp_max_to(adv_slot, amax);
 }
 
+// ---------------------------------------------------------------- asynchronous gathers (strategy 3)
+// The stored lists of strategy 0 with the neighbour records copied by cp.async into a
+// per-thread ring in dynamic shared memory (DEPTH slots): same lists, order and arithmetic,
+// so the results are those of strategy 0 bit for bit.
+constexpr int kAsyncDepthFirst = 8, kAsyncDepthSecond = 8;
+
+template <int DEPTH>
+__device__ __forceinline__ AsyncRing<DEPTH> async_ring(void *smem, bool two_parts)
+{
+    AsyncRing<DEPTH> r;
+    r.tid = threadIdx.x;
+    r.bd = blockDim.x;
+    const size_t slots = size_t(DEPTH) * blockDim.x;
+    r.a = static_cast<float4 *>(smem);
+    r.b = two_parts ? r.a + slots : nullptr;
+    r.c = reinterpret_cast<float *>(two_parts ? r.b + slots : r.a + slots);
+    r.idx = reinterpret_cast<uint32_t *>(r.c + slots);
+    return r;
+}
+
+template <int D, int DEPTH>
+__global__ void __launch_bounds__(256) k_mp_first_async(size_t n, MPConst k, MPFluid f, MPWall w, MPLists in,
+                                                        MPLists wl, double dt, unsigned long long *ac_slot)
+{
+    extern __shared__ float4 ring_smem[];
+    const AsyncRing<DEPTH> ring = async_ring<DEPTH>(ring_smem, false);
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    double vmax = -1.0e300;
+    if (i < n)
+        vmax = first_particle<D, true, DEPTH>(i, n, k.p, Visit{k.m, 0u, nullptr, nullptr}, dt, f, w, in, wl, &ring);
+    warp_max_to(ac_slot, vmax);
+}
+
+template <int D, int DEPTH>
+__global__ void __launch_bounds__(256) k_mp_second_async(size_t n, MPConst k, MPFluid f, MPWall w, MPLists in,
+                                                         MPLists wl, double dt, unsigned long long *adv_slot)
+{
+    extern __shared__ float4 ring_smem[];
+    const AsyncRing<DEPTH> ring = async_ring<DEPTH>(ring_smem, true);
+    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    double amax = -1.0e300;
+    if (i < n)
+        amax = second_particle<D, true, DEPTH>(i, n, k.p, Visit{k.m, 0u, nullptr, nullptr}, dt, f, w, in, wl, &ring);
+    warp_max_to(adv_slot, amax);
+}
+
+// Ring bytes per block: 1st half 16 (geo0) + 4 (pressure) + 4 (entry), 2nd half 16 + 16 + 4
+// per slot.
+inline size_t async_ring_bytes(bool second, unsigned blk)
+{
+    return second ? size_t(kAsyncDepthSecond) * blk * 36 : size_t(kAsyncDepthFirst) * blk * 24;
+}
+
 template <int D, bool LISTS, bool ORDER>
 __global__ void __launch_bounds__(256, 4) k_mp_first(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
                const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, double dt,
@@ -571,6 +624,7 @@ __global__ void k_mp_place_geometry(size_t n, const uint32_t *__restrict__ perm,
     {
         o[d] = noff[d * n + i];
         dst.off[d * n + k] = o[d];
+        dst.off_lo[d * n + k] = noff[(3 + d) * n + i];
     }
     dst.geo0[k] = make_float4(o[0], o[1], o[2], __uint_as_float(ncell[i]));
 }
@@ -601,7 +655,7 @@ __global__ void k_mp_place_state(size_t n, const uint32_t *__restrict__ perm, co
 // ---------------------------------------------------------------- outputs
 __device__ __forceinline__ double position(const MPConst &k, const MPFluid &f, size_t n, size_t i, int d, const int *c)
 {
-    return reconstruct(k, d, c[d], f.off[d * n + i]);
+    return reconstruct(k, d, c[d], offset_of(f, n, i, d));
 }
 
 template <int D>
@@ -711,8 +765,7 @@ __global__ void k_mp_check(size_t n, MPConst k, MPFluid f, unsigned long long *c
 #pragma unroll
         for (int d = 0; d < D; ++d)
         {
-            const float o = f.off[d * n + i];
-            fin = fin && isfinite(o) && isfinite(f.force[d * n + i]);
+            fin = fin && isfinite(f.off[d * n + i]) && isfinite(f.off_lo[d * n + i]) && isfinite(f.force[d * n + i]);
             const double x = position(k, f, n, i, d, c);
             const double hi = k.m.lower[d] + double(k.m.all_cells[d]) * k.m.gs;
             in = in && !(x < k.m.lower[d] || x > hi);
@@ -842,7 +895,7 @@ struct sphx_mp_s
     unsigned ntiles_ne = 0, cap_f = 0, cap_w = 0;
     bool lists_tiled = false;
     int lists_strategy = -1;
-    size_t smem_set[3] = {0, 0, 0}; // dynamic shared memory granted to the three tiled kernels
+    size_t smem_set[5] = {0, 0, 0, 0, 0}; // dynamic shared memory granted to the tiled and ring kernels
     // optional CUDA-event timing of the two sweep kernels (sphx_mp_set_profiling)
     bool profiling = false;
     std::vector<cudaEvent_t> ev_first, ev_second; // start/stop pairs
@@ -882,12 +935,13 @@ int alloc_state(sphx_mp mp, MPFluid &s)
     s.geo0 = mp->alloc<float4>(n);
     s.dyn = mp->alloc<float4>(n);
     s.off = mp->alloc<float>(D * n);
+    s.off_lo = mp->alloc<float>(D * n);
     s.force = mp->alloc<float>(D * n);
     s.drho = mp->alloc<float>(n);
     s.drho_dt = mp->alloc<float>(n);
     s.drho_sum = mp->alloc<float>(n);
     s.id = mp->alloc<uint32_t>(n);
-    if (!s.geo0 || !s.dyn || !s.off || !s.force || !s.drho || !s.drho_dt || !s.drho_sum || !s.id)
+    if (!s.geo0 || !s.dyn || !s.off || !s.off_lo || !s.force || !s.drho || !s.drho_dt || !s.drho_sum || !s.id)
         return fail(SPHX_ERR_OUT_OF_MEMORY, "mixed-precision state allocation failed");
     if (mp->k.periodic)
     {
@@ -1093,7 +1147,7 @@ int configuration_update(sphx_mp mp, bool from_state)
         SPHX_CUDA(cudaMemsetAsync(mp->count, 0, mp->ncells * sizeof(uint32_t), s));
         if (n > 0)
         {
-            k_mp_rehash<D><<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.geo0, mp->a.off, mp->k, mp->ncell, mp->noff,
+            k_mp_rehash<D><<<grid_for(n, 256), 256, 0, s>>>(n, mp->a, mp->k, mp->ncell, mp->noff,
                                                             mp->key, mp->rank, mp->count);
             SPHX_LAUNCHED(ctx);
         }
@@ -1148,6 +1202,26 @@ void launch_second(sphx_mp mp, unsigned blk, double dt)
     const size_t n = mp->n;
     k_mp_second<D, LISTS, ORDER><<<grid_for(n, blk), blk, 0, mp->ctx->stream>>>(
         n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset, mp->in, mp->wl, dt, mp->slots + 1, mp->order);
+}
+
+template <int D>
+int launch_first_async(sphx_mp mp, unsigned blk, double dt)
+{
+    const size_t bytes = async_ring_bytes(false, blk);
+    SPHX_TRY(grant_smem(mp, 3, k_mp_first_async<D, kAsyncDepthFirst>, bytes));
+    k_mp_first_async<D, kAsyncDepthFirst><<<grid_for(mp->n, blk), blk, bytes, mp->ctx->stream>>>(
+        mp->n, mp->k, mp->a, mp->w, mp->in, mp->wl, dt, mp->slots);
+    return SPHX_OK;
+}
+
+template <int D>
+int launch_second_async(sphx_mp mp, unsigned blk, double dt)
+{
+    const size_t bytes = async_ring_bytes(true, blk);
+    SPHX_TRY(grant_smem(mp, 4, k_mp_second_async<D, kAsyncDepthSecond>, bytes));
+    k_mp_second_async<D, kAsyncDepthSecond><<<grid_for(mp->n, blk), blk, bytes, mp->ctx->stream>>>(
+        mp->n, mp->k, mp->a, mp->w, mp->in, mp->wl, dt, mp->slots + 1);
+    return SPHX_OK;
 }
 
 template <int D>
@@ -1209,6 +1283,8 @@ int substep(sphx_mp mp, double dt)
     }
     else if (mp->lists_tiled)
         SPHX_TRY(launch_first_tiled<D>(mp, blk, dt));
+    else if (mp->strategy == 3)
+        SPHX_TRY(launch_first_async<D>(mp, blk, dt));
     else if (mp->strategy != 1)
         mp->order_active ? launch_first<D, true, true>(mp, blk, dt) : launch_first<D, true, false>(mp, blk, dt);
     else
@@ -1227,6 +1303,8 @@ int substep(sphx_mp mp, double dt)
     }
     else if (mp->lists_tiled)
         SPHX_TRY(launch_second_tiled<D>(mp, blk, dt));
+    else if (mp->strategy == 3)
+        SPHX_TRY(launch_second_async<D>(mp, blk, dt));
     else if (mp->strategy != 1)
         mp->order_active ? launch_second<D, true, true>(mp, blk, dt) : launch_second<D, true, false>(mp, blk, dt);
     else
@@ -1459,7 +1537,7 @@ extern "C" int sphx_mp_create(sphx_relation inner, sphx_relation wall, const sph
     mp->rank = mp->alloc<uint32_t>(big);
     mp->perm = mp->alloc<uint32_t>(big);
     mp->ncell = mp->alloc<uint32_t>(n);
-    mp->noff = mp->alloc<float>(3 * n);
+    mp->noff = mp->alloc<float>(6 * n);
     mp->w.geo = mp->alloc<float4>(nw);
     mp->w.n = mp->alloc<float4>(nw);
     mp->w.nw = nw;
@@ -1619,7 +1697,7 @@ extern "C" int sphx_mp_create_periodic(sphx_body fb, const sphx_fluid_params *p,
     mp->rank = mp->alloc<uint32_t>(n);
     mp->perm = mp->alloc<uint32_t>(n);
     mp->ncell = mp->alloc<uint32_t>(n);
-    mp->noff = mp->alloc<float>(3 * n);
+    mp->noff = mp->alloc<float>(6 * n);
     mp->in.count = mp->alloc<uint32_t>(n);
     mp->wl.count = mp->alloc<uint32_t>(n);
     mp->slots = mp->alloc<unsigned long long>(10);
@@ -1864,15 +1942,16 @@ struct Snapshot
     int take(sphx_mp mp, bool restore)
     {
         size_t n = mp->n, D = size_t(mp->dim);
-        void *src[6] = {mp->a.dyn, mp->a.off, mp->a.force, mp->a.drho, mp->a.drho_dt, mp->slots};
-        size_t bytes[6] = {n * sizeof(float4), D * n * 4, D * n * 4, n * 4, n * 4, 2 * sizeof(unsigned long long)};
+        void *src[7] = {mp->a.dyn, mp->a.off, mp->a.off_lo, mp->a.force, mp->a.drho, mp->a.drho_dt, mp->slots};
+        size_t bytes[7] = {n * sizeof(float4), D * n * 4, D * n * 4, D * n * 4, n * 4, n * 4,
+                           2 * sizeof(unsigned long long)};
         if (!restore)
         {
-            bufs.assign(6, nullptr);
-            for (int q = 0; q < 6; ++q)
+            bufs.assign(7, nullptr);
+            for (int q = 0; q < 7; ++q)
                 SPHX_CUDA(cudaMallocAsync(&bufs[q], std::max<size_t>(bytes[q], 1), mp->ctx->stream));
         }
-        for (int q = 0; q < 6; ++q)
+        for (int q = 0; q < 7; ++q)
         {
             void *dst = restore ? src[q] : bufs[q];
             const void *from = restore ? bufs[q] : src[q];
@@ -1903,21 +1982,46 @@ extern "C" int sphx_mp_autotune(sphx_mp mp, int reps, int *best_block, int *best
     Snapshot snap;
     SPHX_TRY(snap.take(mp, false));
     const int blocks[3] = {64, 128, 256};
+    // candidate settings: strategies 0 and 1 in cell order, the tiled strategy 2 with
+    // several tile shapes (sub-cells per axis), each with every block size
+    struct Setting
+    {
+        int strategy, tile[3];
+    };
+    std::vector<Setting> settings = {{0, {0, 0, 0}}, {1, {0, 0, 0}}};
+    if (!mp->k.periodic)
+    {
+        settings.push_back(Setting{3, {0, 0, 0}});
+        if (mp->dim == 3)
+            for (const Setting &t : {Setting{2, {4, 4, 4}}, Setting{2, {4, 4, 8}}})
+                settings.push_back(t);
+        else
+            for (const Setting &t : {Setting{2, {8, 8, 0}}, Setting{2, {4, 8, 0}}})
+                settings.push_back(t);
+    }
     int keep_block = mp->block, keep_strategy = mp->strategy;
+    int keep_tile[3] = {mp->tile[0], mp->tile[1], mp->tile[2]};
     bool keep_prof = mp->profiling;
     double best = 1e300;
     int bb = keep_block, bs = keep_strategy;
+    int bt[3] = {keep_tile[0], keep_tile[1], keep_tile[2]};
     cudaEvent_t e0, e1;
     SPHX_CUDA(cudaEventCreate(&e0));
     SPHX_CUDA(cudaEventCreate(&e1));
     int st = SPHX_OK;
     mp->profiling = false;
-    for (int strategy = 0; strategy < 2 && st == SPHX_OK; ++strategy)
+    for (size_t si = 0; si < settings.size() && st == SPHX_OK; ++si)
         for (int bi = 0; bi < 3 && st == SPHX_OK; ++bi)
         {
+            const Setting &set = settings[si];
+            const bool retile = set.tile[0] != mp->tile[0] || set.tile[1] != mp->tile[1] || set.tile[2] != mp->tile[2];
             mp->block = blocks[bi];
-            mp->strategy = strategy;
-            if ((st = snap.take(mp, true)) != SPHX_OK)
+            mp->strategy = set.strategy;
+            for (int d = 0; d < 3; ++d)
+                mp->tile[d] = set.tile[d];
+            if (retile) // the order, and for strategy 2 the lists, of the new shape
+                st = mp->dim == 2 ? launch_build<2>(mp) : launch_build<3>(mp);
+            if (st != SPHX_OK || (st = snap.take(mp, true)) != SPHX_OK)
                 break;
             if ((st = (mp->dim == 2 ? substep<2>(mp, dt) : substep<3>(mp, dt))) != SPHX_OK) // warm-up
                 break;
@@ -1933,7 +2037,9 @@ extern "C" int sphx_mp_autotune(sphx_mp mp, int reps, int *best_block, int *best
             {
                 best = ms / reps;
                 bb = blocks[bi];
-                bs = strategy;
+                bs = set.strategy;
+                for (int d = 0; d < 3; ++d)
+                    bt[d] = set.tile[d];
             }
         }
     int st2 = snap.take(mp, true);
@@ -1946,10 +2052,17 @@ extern "C" int sphx_mp_autotune(sphx_mp mp, int reps, int *best_block, int *best
     {
         mp->block = keep_block;
         mp->strategy = keep_strategy;
-        return st != SPHX_OK ? st : st2;
+        for (int d = 0; d < 3; ++d)
+            mp->tile[d] = keep_tile[d];
+        int st3 = mp->dim == 2 ? launch_build<2>(mp) : launch_build<3>(mp);
+        return st != SPHX_OK ? st : (st2 != SPHX_OK ? st2 : st3);
     }
     mp->block = bb;
     mp->strategy = bs;
+    for (int d = 0; d < 3; ++d)
+        mp->tile[d] = bt[d];
+    // lists and order of the chosen setting (the build reads the configuration geometry only)
+    SPHX_TRY(mp->dim == 2 ? launch_build<2>(mp) : launch_build<3>(mp));
     if (best_block)
         *best_block = bb;
     if (best_strategy)
@@ -1961,8 +2074,10 @@ extern "C" int sphx_mp_autotune(sphx_mp mp, int reps, int *best_block, int *best
 
 extern "C" int sphx_mp_set_tuning(sphx_mp mp, int block, int strategy)
 {
-    if (!mp || block < 64 || block > 256 || block % 32 != 0 || strategy < 0 || strategy > 2)
-        return fail(SPHX_ERR_INVALID_ARG, "block must be 64..256 in steps of 32, strategy 0, 1 or 2");
+    if (!mp || block < 64 || block > 256 || block % 32 != 0 || strategy < 0 || strategy > 3)
+        return fail(SPHX_ERR_INVALID_ARG, "block must be 64..256 in steps of 32, strategy 0, 1, 2 or 3");
+    if (strategy == 3 && mp->k.periodic)
+        return fail(SPHX_ERR_INVALID_ARG, "the asynchronous-gather strategy serves the dam-break solver only");
     if (strategy == 2 && mp->k.periodic)
         return fail(SPHX_ERR_INVALID_ARG, "the tiled strategy serves the dam-break solver only");
     if (strategy == 2 && (mp->tile[0] > kTileMaxExtent || mp->tile[1] > kTileMaxExtent || mp->tile[2] > kTileMaxExtent))
@@ -1976,6 +2091,20 @@ extern "C" int sphx_mp_set_tuning(sphx_mp mp, int block, int strategy)
         mp->tile[2] = mp->dim == 3 ? 4 : 0;
     }
     return SPHX_OK; // the lists follow at the next sub-step (substep rebuilds them)
+}
+
+extern "C" int sphx_mp_get_tuning(sphx_mp mp, int *block, int *strategy, int *tile)
+{
+    if (!mp)
+        return fail(SPHX_ERR_INVALID_ARG, "null solver");
+    if (block)
+        *block = mp->block;
+    if (strategy)
+        *strategy = mp->strategy;
+    if (tile)
+        for (int d = 0; d < 3; ++d)
+            tile[d] = mp->tile[d];
+    return SPHX_OK;
 }
 
 extern "C" int sphx_mp_set_tile(sphx_mp mp, int tx, int ty, int tz)

@@ -69,21 +69,21 @@ __device__ __forceinline__ void sub_cell_index(const MeshDev &m, double inv_gs, 
     }
 }
 
-// New (cell, offset) of a particle that moved by its FP32 offset from the corner of cell c0
+// New (cell, offset) of a particle that moved by its FP64 offset from the corner of cell c0
 // (the offset may lie outside that cell): k = floor(offset / gs) cells along each axis,
-// then the offset re-based to the new cell in FP64 and rounded once to FP32.  A periodic
+// then the offset re-based to the new cell in FP64.  A periodic
 // box wraps the cell over its all_cells cells (the position moves by one period, the offset
 // stays); otherwise the cell is clamped to the mesh as sub_cell_index does.  In exact
 // arithmetic this equals the re-hash of the absolute position (corner + offset) with half
 // its FP64 operations, which run at 1/64 of the FP32 rate on GB300.
 template <int D>
 __device__ __forceinline__ void rehash_relative(const MeshDev &m, double inv_gs, bool periodic, const int *c0,
-                                                const float *offset, int *c, float *noff)
+                                                const double *offset, int *c, double *noff)
 {
 #pragma unroll
     for (int a = 0; a < D; ++a)
     {
-        const double o = double(offset[a]);
+        const double o = offset[a];
         const int k = int(floor(o * inv_gs));
         const int ncell = m.all_cells[a];
         int ca = c0[a] + k, shift = k;
@@ -95,7 +95,7 @@ __device__ __forceinline__ void rehash_relative(const MeshDev &m, double inv_gs,
             shift = ca - c0[a];
         }
         c[a] = ca;
-        noff[a] = float(o - double(shift) * m.gs);
+        noff[a] = o - double(shift) * m.gs;
     }
 }
 
@@ -224,10 +224,39 @@ inline MPParams make_params(int dim, double grid_spacing, double h, double rho0,
 struct MPState
 {
     float4 *geo0, *dyn; // {offset at the last configuration update, packed cell}; {velocity, pressure}
-    float *off, *force, *drho, *drho_dt, *drho_sum;
+    // current offset from the cell corner as an FP32 pair: off = the FP64 offset rounded to
+    // FP32 (what the pair arithmetic reads), off_lo = the FP32 rounding of its residual, so
+    // the position integration carries the FP64 offset from step to step
+    float *off, *off_lo, *force, *drho, *drho_dt, *drho_sum;
     uint32_t *id;
     float *fprior, *shift; // periodic flow only: prior (viscous) force, transport-velocity shift
 };
+
+// FP64 offset of particle i along axis d, and its storage as the (off, off_lo) pair.
+__device__ __forceinline__ double offset_of(const MPState &f, size_t n, size_t i, int d)
+{
+    return double(f.off[d * n + i]) + double(f.off_lo[d * n + i]);
+}
+__device__ __forceinline__ void store_offset(const MPState &f, size_t n, size_t i, int d, double x)
+{
+    const float hi = float(x);
+    f.off[d * n + i] = hi;
+    f.off_lo[d * n + i] = float(x - double(hi));
+}
+// Staging of new offsets between a re-hash and the gather into cell order: the FP32 pair
+// of the FP64 offset, component d of particle i at noff[d * n + i] and noff[(3 + d) * n + i].
+__device__ __forceinline__ void stage_offset(float *noff, size_t n, size_t i, int d, double x)
+{
+    const float hi = float(x);
+    noff[d * n + i] = hi;
+    noff[(3 + d) * n + i] = float(x - double(hi));
+}
+
+// Position half-step x += dt / 2 v in FP64 on the stored pair.
+__device__ __forceinline__ void half_step(const MPState &f, size_t n, size_t i, int d, double dt, float v)
+{
+    store_offset(f, n, i, d, offset_of(f, n, i, d) + 0.5 * dt * double(v));
+}
 
 struct MPWallData
 {
@@ -525,6 +554,86 @@ __device__ __forceinline__ void list_sweep(size_t i, size_t n, const MPNeighbors
     flush();
 }
 
+// ---------------------------------------------------------------- asynchronous gathers
+// cp.async copies of neighbour records from global into shared memory: the copy is in
+// flight without holding registers, so a thread keeps DEPTH neighbours' records (and the
+// list entries DEPTH further on) in flight while it computes, instead of the U records an
+// unrolled register gather holds.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned a = unsigned(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+    const unsigned a = unsigned(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Per-thread ring of DEPTH slots in shared memory, slot-major (slot s of thread t at
+// [s * blockDim + t], so a warp's lanes touch consecutive words: no bank conflicts).
+template <int DEPTH>
+struct AsyncRing
+{
+    float4 *a, *b;  // two 16-byte parts of a record (b may be unused)
+    float *c;       // a 4-byte part (may be unused)
+    uint32_t *idx;  // list entries DEPTH neighbours ahead
+    unsigned tid, bd;
+    __device__ __forceinline__ unsigned at(unsigned slot) const { return slot * bd + tid; }
+};
+
+// list_sweep with the records fetched through the ring: issue(j, slot) starts the copies of
+// neighbour j into a slot, read(slot) returns the record, pair/flush as list_sweep.  The
+// neighbours, their order and the kGroup flushes are those of list_sweep, so the sums are
+// the same bit for bit.  Each iteration commits one copy group (possibly empty), so waiting
+// for all but the DEPTH - 1 newest groups completes exactly the oldest neighbour's copies.
+template <int DEPTH, class Issue, class Read, class Pair, class Flush>
+__device__ __forceinline__ void list_sweep_async(size_t i, size_t n, const MPNeighbors &l,
+                                                 const AsyncRing<DEPTH> &ring, Issue &&issue, Read &&read,
+                                                 Pair &&pair, Flush &&flush)
+{
+    const unsigned c = min(l.count[i], l.cap);
+    const uint32_t *J = l.J + i;
+#pragma unroll
+    for (int u = 0; u < DEPTH; ++u)
+    {
+        if (unsigned(u) < c)
+            issue(__ldg(&J[size_t(u) * n]), unsigned(u));
+        if (unsigned(u + DEPTH) < c)
+            cp_async4(&ring.idx[ring.at(u)], &J[size_t(u + DEPTH) * n]);
+        cp_async_commit();
+    }
+    unsigned g = 0, slot = 0;
+    for (unsigned s = 0; s < c; ++s)
+    {
+        cp_async_wait<DEPTH - 1>();
+        const auto r = read(slot);
+        pair(r); // consumes the slot before it is refilled
+        const unsigned nx = s + DEPTH;
+        if (nx < c)
+        {
+            issue(ring.idx[ring.at(slot)], slot);
+            if (nx + DEPTH < c)
+                cp_async4(&ring.idx[ring.at(slot)], &J[size_t(nx + DEPTH) * n]);
+        }
+        cp_async_commit();
+        if (++g == kGroup)
+        {
+            flush();
+            g = 0;
+        }
+        slot = slot + 1 == DEPTH ? 0 : slot + 1;
+    }
+    flush();
+    cp_async_wait<0>();
+}
+
 // Same visits by cell sweep: accepts the candidates the build accepted.
 template <int D, bool PRUNE, class Load, class Pair, class Flush>
 __device__ __forceinline__ void cell_sweep(const Visit &v, const uint32_t *offset, const int *ci, float gs, uint32_t pib,
@@ -562,10 +671,12 @@ struct SecondRec
 // 1st half of one particle: pressure force and density-rate dissipation against fluid and
 // wall neighbours, velocity update and the first position half-step.  Returns the
 // acoustic-time-step candidate c0 + |v|.
-template <int D, bool LISTS>
+// DEPTH > 0: the stored lists with the neighbour records gathered through an AsyncRing of
+// that depth (ring: slots for geo0 in a, the pressure in c).
+template <int D, bool LISTS, int DEPTH = 0>
 __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPParams &k, const Visit &v, double dt,
                                                  const MPState &f, const MPWallData &w, const MPNeighbors &in,
-                                                 const MPNeighbors &wl)
+                                                 const MPNeighbors &wl, const AsyncRing<DEPTH> *ring = nullptr)
 {
     const float4 gi = f.geo0[i];
     const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
@@ -596,7 +707,17 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
         rdis.flush();
     };
     auto load = [&](uint32_t j) { return FirstRec{__ldg(&f.geo0[j]), __ldg(&f.dyn[j].w)}; };
-    if (LISTS)
+    if constexpr (DEPTH > 0)
+    {
+        const AsyncRing<DEPTH> &rg = *ring;
+        auto issue = [&](uint32_t j, unsigned slot) {
+            cp_async16(&rg.a[rg.at(slot)], &f.geo0[j]);
+            cp_async4(&rg.c[rg.at(slot)], &f.dyn[j].w);
+        };
+        auto read = [&](unsigned slot) { return FirstRec{rg.a[rg.at(slot)], rg.c[rg.at(slot)]}; };
+        list_sweep_async<DEPTH>(i, n, in, rg, issue, read, pair, flush);
+    }
+    else if (LISTS)
         list_sweep<true, kUnrollFirst>(i, n, in, load, pair, flush);
     else
         cell_sweep<D, true>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, i, f.geo0, load, pair, flush);
@@ -623,7 +744,7 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
         wrdis.flush();
     };
     auto wload = [&](uint32_t j) { return __ldg(&w.geo[j]); };
-    if (LISTS)
+    if (LISTS || DEPTH > 0)
         list_sweep<true, kUnrollFirst>(i, n, wl, wload, wpair, wflush);
     else
         cell_sweep<D, false>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, ~size_t(0), w.geo, wload,
@@ -640,7 +761,7 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
         f.force[d * n + i] = F;
         float vo = vn[d];
         // position half-step in FP64 (initialisation of the 1st half, old velocity)
-        f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vo));
+        half_step(f, n, i, d, dt, vo);
         vn[d] = vo + (k.g[d] + F * k.inv_mass) * dt_f;
         v2 += vn[d] * vn[d];
     }
@@ -652,10 +773,12 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
 // 2nd half of one particle: the second position half-step, density rate and pressure
 // dissipation against fluid and wall neighbours, density update.  Returns the
 // advection-time-step candidate max(|v|^2, 4 h |F + F_prior| / m).
-template <int D, bool LISTS>
+// DEPTH > 0: the stored lists with the neighbour records gathered through an AsyncRing of
+// that depth (ring: slots for geo0 in a, dyn in b).
+template <int D, bool LISTS, int DEPTH = 0>
 __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPParams &k, const Visit &v, double dt,
                                                   const MPState &f, const MPWallData &w, const MPNeighbors &in,
-                                                  const MPNeighbors &wl)
+                                                  const MPNeighbors &wl, const AsyncRing<DEPTH> *ring = nullptr)
 {
     const float4 gi = f.geo0[i];
     const uint32_t pib = __float_as_uint(gi.w) + CellLanes<D>::bias;
@@ -688,7 +811,17 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
             pdis[d].flush();
     };
     auto load = [&](uint32_t j) { return SecondRec{__ldg(&f.geo0[j]), __ldg(&f.dyn[j])}; };
-    if (LISTS)
+    if constexpr (DEPTH > 0)
+    {
+        const AsyncRing<DEPTH> &rg = *ring;
+        auto issue = [&](uint32_t j, unsigned slot) {
+            cp_async16(&rg.a[rg.at(slot)], &f.geo0[j]);
+            cp_async16(&rg.b[rg.at(slot)], &f.dyn[j]);
+        };
+        auto read = [&](unsigned slot) { return SecondRec{rg.a[rg.at(slot)], rg.b[rg.at(slot)]}; };
+        list_sweep_async<DEPTH>(i, n, in, rg, issue, read, pair, flush);
+    }
+    else if (LISTS)
         list_sweep<false, kUnrollSecond>(i, n, in, load, pair, flush);
     else
         cell_sweep<D, true>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, i, f.geo0, load, pair, flush);
@@ -717,7 +850,7 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
             wdis[d].flush();
     };
     auto wload = [&](uint32_t j) { return SecondRec{__ldg(&w.geo[j]), __ldg(&w.n[j])}; };
-    if (LISTS)
+    if (LISTS || DEPTH > 0)
         list_sweep<false, kUnrollSecond>(i, n, wl, wload, wpair, wflush);
     else
         cell_sweep<D, false>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, ~size_t(0), w.geo, wload,
@@ -732,7 +865,7 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
     {
         float F = pdis[d].value() * k.Vol + wdis[d].value() * k.Vol;
         f.force[d * n + i] = F;
-        f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vi[d]));
+        half_step(f, n, i, d, dt, vi[d]);
         v2 += vi[d] * vi[d];
         float ft = F + k.mass * k.g[d];
         a2 += ft * ft;
@@ -970,7 +1103,7 @@ __device__ __forceinline__ double first_particle_periodic(size_t i, size_t n, co
         float F = f.force[d * n + i] + force[d].value() * k.Vol;
         f.force[d * n + i] = F;
         float vo = vn[d];
-        f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vo));
+        half_step(f, n, i, d, dt, vo);
         vn[d] = vo + (f.fprior[d * n + i] + F) * k.inv_mass * dt_f;
         v2 += vn[d] * vn[d];
     }
@@ -1038,7 +1171,7 @@ __device__ __forceinline__ double second_particle_periodic(size_t i, size_t n, c
     {
         float F = pdis[d].value() * k.Vol;
         f.force[d * n + i] = F;
-        f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vi[d]));
+        half_step(f, n, i, d, dt, vi[d]);
         v2 += vi[d] * vi[d];
         float ft = F + f.fprior[d * n + i];
         a2 += ft * ft;

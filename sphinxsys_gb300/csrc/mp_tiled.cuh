@@ -340,7 +340,7 @@ __device__ __forceinline__ double first_particle_tiled(size_t t, size_t i, size_
         float F = f.force[d * n + i] + force[d].value() * k.Vol + wforce[d].value() * k.Vol;
         f.force[d * n + i] = F;
         float vo = vn[d];
-        f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vo));
+        half_step(f, n, i, d, dt, vo);
         vn[d] = vo + (k.g[d] + F * k.inv_mass) * dt_f;
         v2 += vn[d] * vn[d];
     }
@@ -426,7 +426,7 @@ __device__ __forceinline__ double second_particle_tiled(size_t t, size_t i, size
     {
         float F = pdis[d].value() * k.Vol + wdis[d].value() * k.Vol;
         f.force[d * n + i] = F;
-        f.off[d * n + i] = float(double(f.off[d * n + i]) + 0.5 * dt * double(vi[d]));
+        half_step(f, n, i, d, dt, vi[d]);
         v2 += vi[d] * vi[d];
         float ft = F + k.mass * k.g[d];
         a2 += ft * ft;

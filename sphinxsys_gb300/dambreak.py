@@ -172,11 +172,20 @@ class MixedPrecisionDamBreak:
         return sub.value, Dt.value
 
     def autotune(self, reps: int = 3):
-        """Picks the fastest block size and neighbour strategy on the current state."""
+        """Picks the fastest block size, neighbour strategy and tile shape on the current
+        state; returns (block, strategy, ms per sub-step)."""
         C = self._C
         b, st, ms = C.c_int(), C.c_int(), C.c_double()
         self._N.call("sphx_mp_autotune", self.handle, int(reps), C.byref(b), C.byref(st), C.byref(ms))
         return b.value, st.value, ms.value
+
+    def tuning(self) -> dict:
+        """Current block size, strategy and tile shape (sphx_mp_get_tuning)."""
+        C = self._C
+        b, st = C.c_int(), C.c_int()
+        t = (C.c_int * 3)()
+        self._N.call("sphx_mp_get_tuning", self.handle, C.byref(b), C.byref(st), t)
+        return {"block": b.value, "strategy": st.value, "tile": list(t)}
 
     def set_profiling(self, on: bool) -> None:
         self._N.call("sphx_mp_set_profiling", self.handle, int(on))

@@ -113,6 +113,7 @@ SIGNATURES = {
     "sphx_mp_check_state": (_i, [_vp, _pu64, _pu64]),
     "sphx_mp_set_tuning": (_i, [_vp, _i, _i]),
     "sphx_mp_set_tile": (_i, [_vp, _i, _i, _i]),
+    "sphx_mp_get_tuning": (_i, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "sphx_mp_set_profiling": (_i, [_vp, _i]),
     "sphx_mp_autotune": (_i, [_vp, _i, C.POINTER(C.c_int), C.POINTER(C.c_int), _pd]),
     "sphx_mp_kernel_times": (_i, [_vp, _pd]),

@@ -68,6 +68,42 @@ def test_strategies_and_block_sizes_bitwise_equal():
             assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("case, tiles", [
+    (cases.dambreak_2d(), [(4, 4, 0), (8, 8, 0), (2, 8, 0)]),
+    (cases.dambreak_3d(0.04), [(4, 4, 4), (2, 2, 8), (8, 8, 2), (1, 3, 5)]),
+], ids=["2d", "3d"])
+def test_tiled_and_async_strategies_bitwise_equal(case, tiles):
+    """Strategy 2 (tile windows staged in shared memory, lists of staged indices) and
+    strategy 3 (the stored lists with records gathered by cp.async into a shared-memory
+    ring) visit the same neighbours in the same order with the same arithmetic as the
+    stored lists of strategy 0: equal bit for bit, for every tile shape and block size; so
+    does the tile-grouped traversal of strategy 0."""
+    def run(block, strategy, tile):
+        mp = MixedPrecisionDamBreak(case, block=block, strategy=strategy)
+        if tile is not None:
+            mp.set_tile(*tile)
+        subs = [mp.advection_step()[0] for _ in range(5)]
+        mp.sync_fp64()
+        return subs, [mp.fp64.water_block.download(n) for n in ("Position", "Velocity", "Density", "Pressure")]
+
+    ref_subs, ref = run(128, 0, None)
+    runs = [(128, 0, tiles[0])] + [(b, 2, t) for t in tiles for b in (64, 256)] + [(b, 3, None) for b in (64, 256)]
+    for block, strategy, tile in runs:
+        subs, out = run(block, strategy, tile)
+        assert subs == ref_subs, (block, strategy, tile)
+        for a, b in zip(ref, out):
+            assert np.array_equal(a, b), (block, strategy, tile)
+
+
+def test_tiled_strategy_rejects_large_tiles():
+    from sphinxsys_gb300.native import SphxError
+    mp = MixedPrecisionDamBreak(cases.dambreak_2d(), strategy=2)
+    with pytest.raises(SphxError):
+        mp.set_tile(16, 16, 0)
+    mp.set_tile(8, 8, 0)
+    mp.advection_step()
+
+
 def test_mixed_precision_upper_front_and_probe():
     case = cases.dambreak_2d()
     ref, mp, _ = run_pair(case, 10)
