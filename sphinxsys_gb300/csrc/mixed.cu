@@ -470,6 +470,9 @@ __global__ void __launch_bounds__(256) k_mp_second_tiled(size_t n, MPConst k, MP
 // so the results are those of strategy 0 bit for bit.
 constexpr int kAsyncDepthFirst = 8, kAsyncDepthSecond = 8;
 
+// Ring layout in the dynamic shared memory, DEPTH x blockDim slots per part:
+// two parts (2nd half): a (16 B), b (16 B), idx (4 B) = 36 B per slot;
+// one part (1st half): a (16 B), c (4 B), idx (4 B) = 24 B per slot (async_ring_bytes).
 template <int DEPTH>
 __device__ __forceinline__ AsyncRing<DEPTH> async_ring(void *smem, bool two_parts)
 {
@@ -478,9 +481,18 @@ __device__ __forceinline__ AsyncRing<DEPTH> async_ring(void *smem, bool two_part
     r.bd = blockDim.x;
     const size_t slots = size_t(DEPTH) * blockDim.x;
     r.a = static_cast<float4 *>(smem);
-    r.b = two_parts ? r.a + slots : nullptr;
-    r.c = reinterpret_cast<float *>(two_parts ? r.b + slots : r.a + slots);
-    r.idx = reinterpret_cast<uint32_t *>(r.c + slots);
+    if (two_parts)
+    {
+        r.b = r.a + slots;
+        r.c = nullptr;
+        r.idx = reinterpret_cast<uint32_t *>(r.b + slots);
+    }
+    else
+    {
+        r.b = nullptr;
+        r.c = reinterpret_cast<float *>(r.a + slots);
+        r.idx = reinterpret_cast<uint32_t *>(r.c + slots);
+    }
     return r;
 }
 
@@ -510,11 +522,11 @@ __global__ void __launch_bounds__(256) k_mp_second_async(size_t n, MPConst k, MP
     warp_max_to(adv_slot, amax);
 }
 
-// Ring bytes per block: 1st half 16 (geo0) + 4 (pressure) + 4 (entry), 2nd half 16 + 16 + 4
-// per slot.
+// Ring bytes per block (the layout of async_ring): 1st half 16 (geo0) + 4 (pressure) + 4
+// (list entry), 2nd half 16 (geo0) + 16 (dyn) + 4 (list entry) per slot.
 inline size_t async_ring_bytes(bool second, unsigned blk)
 {
-    return second ? size_t(kAsyncDepthSecond) * blk * 36 : size_t(kAsyncDepthFirst) * blk * 24;
+    return second ? size_t(kAsyncDepthSecond) * blk * (16 + 16 + 4) : size_t(kAsyncDepthFirst) * blk * (16 + 4 + 4);
 }
 
 template <int D, bool LISTS, bool ORDER>
