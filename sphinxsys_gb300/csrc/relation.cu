@@ -48,6 +48,13 @@ struct BuildArgs
     unsigned int *max_count;
 };
 
+// Two passes per source particle.  Pass 1 walks the candidate cells with the FP32
+// pre-filter only and writes the cell-list entry index of every candidate that passes
+// into the particle's list slots.  Pass 2 walks that short list: the exact FP64 membership
+// test, then W, dW, e (and r) in FP64 for the accepted pairs, compacted in place.  The FP64
+// work of pass 2 runs with nearly all lanes of a warp busy; in one pass it ran for the
+// whole warp whenever any lane accepted a candidate.  Entries, order and values are those
+// of the one-pass form.  The capacity check uses the pass-1 count (a superset).
 template <int D, bool INNER>
 __global__ void __launch_bounds__(kBlock) k_build(BuildArgs a)
 {
@@ -67,8 +74,8 @@ __global__ void __launch_bounds__(kBlock) k_build(BuildArgs a)
         hi[d] = min(a.m.all_cells[d], c[d] + a.depth + 1);
     }
     const size_t stride = size_t(a.cap) * a.n_src;
-    unsigned cnt = 0;
-    double ws = INNER ? a.k.factor_W : 0.0;
+    // pass 1: FP32 pre-filter, candidate entries into the list slots
+    unsigned cand = 0;
     int cc[3] = {0, 0, 0};
     for (cc[0] = lo[0]; cc[0] < hi[0]; ++cc[0])
     {
@@ -92,57 +99,65 @@ __global__ void __launch_bounds__(kBlock) k_build(BuildArgs a)
                     }
                     if (d2f > a.k.prefilter_sqr)
                         continue;
-                    uint32_t j = a.pidx[kk];
-                    if (INNER && j == uint32_t(i))
+                    if (INNER && a.pidx[kk] == uint32_t(i))
                         continue;
-                    double dx[3] = {0, 0, 0};
-#pragma unroll
-                    for (int d = 0; d < D; ++d)
-                        dx[d] = __dsub_rn(xi[d], a.spos[d * a.n_tgt + kk]);
-                    double r2 = __dadd_rn(__dmul_rn(dx[0], dx[0]), __dmul_rn(dx[1], dx[1]));
-                    if (D == 3)
-                        r2 = __dadd_rn(r2, __dmul_rn(dx[2], dx[2]));
-                    if (!(r2 < a.k.rc_sqr))
-                        continue;
-                    // one reciprocal square root gives r and 1/r; e = dx / (r + TinyReal) of
-                    // the reference differs from dx / r by TinyReal / r relative, far below
-                    // one rounding, except for coincident particles where e is zero
-                    double ri = rsqrt(r2);
-                    double r = r2 > 0.0 ? r2 * ri : 0.0;
-                    double inv = r2 > 0.0 ? ri : 1.0 / kTinyReal;
-                    double q = r * a.k.inv_h;
-                    // Wendland C2 with t = 1 - q/2: W ~ t^4 (1 + 2q), dW ~ 0.625 (q - 2)^3 q = -5 t^3 q
-                    double t = 1.0 - 0.5 * q;
-                    double t2 = t * t, t3 = t2 * t;
-                    double W = a.k.factor_W * (t2 * t2 * (1.0 + 2.0 * q));
-                    double dW = a.k.factor_dW * (-5.0 * t3 * q);
-                    if (cnt < unsigned(a.cap))
-                    {
-                        size_t slot = size_t(cnt) * a.n_src + i;
-                        a.J[slot] = j;
-                        a.DW[slot] = dW;
-#pragma unroll
-                        for (int d = 0; d < D; ++d)
-                            a.E[d * stride + slot] = dx[d] * inv;
-                        if (a.R)
-                            a.R[slot] = r;
-                        if (a.W)
-                            a.W[slot] = W;
-                    }
-                    if (INNER)
-                        ws += W;
-                    else
-                        ws += (W * a.tgt_inv_rho0) * a.tgt_mass[j];
-                    ++cnt;
+                    if (cand < unsigned(a.cap))
+                        a.J[size_t(cand) * a.n_src + i] = kk;
+                    ++cand;
                 }
                 if (D == 2)
                     break;
             }
         }
     }
+    // pass 2: exact test and kernel values over the candidates, in place
+    const unsigned stored = min(cand, unsigned(a.cap));
+    unsigned cnt = 0;
+    double ws = INNER ? a.k.factor_W : 0.0;
+    for (unsigned s = 0; s < stored; ++s)
+    {
+        const uint32_t kk = a.J[size_t(s) * a.n_src + i];
+        double dx[3] = {0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            dx[d] = __dsub_rn(xi[d], a.spos[d * a.n_tgt + kk]);
+        double r2 = __dadd_rn(__dmul_rn(dx[0], dx[0]), __dmul_rn(dx[1], dx[1]));
+        if (D == 3)
+            r2 = __dadd_rn(r2, __dmul_rn(dx[2], dx[2]));
+        if (!(r2 < a.k.rc_sqr))
+            continue;
+        const uint32_t j = a.pidx[kk];
+        // one reciprocal square root gives r and 1/r; e = dx / (r + TinyReal) of the
+        // reference differs from dx / r by TinyReal / r relative, far below one rounding,
+        // except for coincident particles where e is zero
+        double ri = rsqrt(r2);
+        double r = r2 > 0.0 ? r2 * ri : 0.0;
+        double inv = r2 > 0.0 ? ri : 1.0 / kTinyReal;
+        double q = r * a.k.inv_h;
+        // Wendland C2 with t = 1 - q/2: W ~ t^4 (1 + 2q), dW ~ 0.625 (q - 2)^3 q = -5 t^3 q
+        double t = 1.0 - 0.5 * q;
+        double t2 = t * t, t3 = t2 * t;
+        double W = a.k.factor_W * (t2 * t2 * (1.0 + 2.0 * q));
+        double dW = a.k.factor_dW * (-5.0 * t3 * q);
+        size_t slot = size_t(cnt) * a.n_src + i;
+        a.J[slot] = j;
+        a.DW[slot] = dW;
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            a.E[d * stride + slot] = dx[d] * inv;
+        if (a.R)
+            a.R[slot] = r;
+        if (a.W)
+            a.W[slot] = W;
+        if (INNER)
+            ws += W;
+        else
+            ws += (W * a.tgt_inv_rho0) * a.tgt_mass[j];
+        ++cnt;
+    }
     a.count[i] = cnt;
     a.wsum[i] = ws;
-    atomicMax(a.max_count, cnt);
+    atomicMax(a.max_count, cand);
 }
 } // namespace
 
