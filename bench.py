@@ -10,7 +10,10 @@ against FP64.  The FP64 drop-in is also measured on dp = 0.0075 (1,702,400 fluid
 particles) through the reference-shaped API (``fp64_drop_in``), a seeded batch of 64
 independent dam breaks against the same instances run one by one in FP64 (``batch``), and
 the 3D periodic Taylor-Green vortex at 256^3 in mixed precision with its kinetic-energy
-decay and a few FP64 steps of the same case (``taylor_green``).
+decay and a few FP64 steps of the same case (``taylor_green``).  ``accuracy_vs_fp64``
+runs the headline geometry at dp = 0.02 in both precisions to t = 0.75 and reports the
+wall-probe and free-surface errors the 1e-4 bound refers to (the probe on the near wall,
+wetted from t = 0).
 
 One bench step is one advection step of the Dambreak.cpp loop: advection dt, density
 summation, the acoustic sub-steps (1st + 2nd half each) and the cell-list / configuration
@@ -166,7 +169,10 @@ def mixed_leg(args, torch, local, world):
     mp = MixedPrecisionDamBreak(case, device=local)
     ref = mp.fp64  # the FP64 set-up is also the FP64 reference run (same initial state)
     n = ref.water_block.n
-    tuned = mp.autotune(reps=2) if args.autotune else None
+    tuned = None
+    if args.autotune:
+        b, st, ms = mp.autotune(reps=2)
+        tuned = dict(mp.tuning(), ms_per_substep=ms)
     mp.set_profiling(True)
     el, subs, launches, clocks = timed_steps(torch, mp.ctx, mp.advection_step, args.steps, args.warmup,
                                              ClockSampler(local))
@@ -246,6 +252,44 @@ def mixed_leg(args, torch, local, world):
     }
     del mp, ref
     return out
+
+
+def accuracy_leg(args):
+    """Mixed precision against FP64 where the headline's 1e-4 bound applies: the same
+    geometry at dp = args.acc_dp, both solvers from one initial state to t = args.acc_t,
+    recorded every 5 advection steps; the near-wall probe at (0, 0.5, 0.2) (wetted from
+    t = 0) relative to max(|p_fp64|, 0.1 rho0 g (H - z)), and the free-surface height over
+    the initial column (the criteria of tests/test_gpu_accuracy.py)."""
+    from sphinxsys_gb300 import cases
+    from sphinxsys_gb300 import sph as S
+    from sphinxsys_gb300.dambreak import DamBreak, MixedPrecisionDamBreak
+    case = cases.dambreak_3d(args.acc_dp)
+    k = case.observers.index((0.0, 0.5, 0.2))
+    lo, up = list(case.sys_lower), list(case.sys_upper)
+    lo[0] = case.water_center[0] - case.water_halfsize[0]
+    up[0] = case.water_center[0] + case.water_halfsize[0]
+    mp = MixedPrecisionDamBreak(case)
+    rows_m, steps = [], 0
+    while mp.physical_time < args.acc_t:
+        mp.advection_step()
+        steps += 1
+        if steps % 5 == 0:
+            rows_m.append((float(mp.observe_pressure_view()[k]), mp.upper_front(case.vertical_axis, lo, up)))
+    del mp
+    sim = DamBreak(case)
+    rows_f = []
+    for s_ in range(1, steps + 1):
+        sim.advection_step()
+        if s_ % 5 == 0:
+            rows_f.append((float(sim.recorded_pressure.exec()[k]),
+                           S.UpperFrontInAxisDirection(sim.water_block, lo, up, case.vertical_axis).exec()))
+    floor = 0.1 * case.rho0 * case.gravity_g * (2.0 * case.water_halfsize[2] - case.observers[k][2])
+    p_rel = [abs(a[0] - b[0]) / max(abs(b[0]), floor) for a, b in zip(rows_m, rows_f)]
+    fs_rel = [abs(a[1] / b[1] - 1.0) for a, b in zip(rows_m, rows_f)]
+    return {"workload": case.name, "t_end": sim.physical_time, "advection_steps": steps, "records": len(p_rel),
+            "probe": list(case.observers[k]), "probe_max_rel_err": max(p_rel), "probe_max_abs_err":
+            max(abs(a[0] - b[0]) for a, b in zip(rows_m, rows_f)), "free_surface_max_rel_err": max(fs_rel),
+            "bound": 1e-4, "within_bound": max(p_rel) <= 1e-4 and max(fs_rel) <= 1e-4}
 
 
 def fp64_leg(args, torch, local):
@@ -504,11 +548,13 @@ def main():
     ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--batch-count", type=int, default=64, help="instances of the batched leg (0 = skip)")
     ap.add_argument("--batch-steps", type=int, default=5)
-    ap.add_argument("--batch-fp64-steps", type=int, default=1)
+    ap.add_argument("--batch-fp64-steps", type=int, default=3)
     ap.add_argument("--batch-fp64-warmup", type=int, default=1)
     ap.add_argument("--tg-resolution", type=int, default=256, help="Taylor-Green particles per side (0 = skip)")
     ap.add_argument("--tg-steps", type=int, default=10)
     ap.add_argument("--tg-fp64-steps", type=int, default=3)
+    ap.add_argument("--acc-dp", type=float, default=0.02, help="accuracy leg spacing (0 = skip)")
+    ap.add_argument("--acc-t", type=float, default=0.75, help="accuracy leg end time")
     args = ap.parse_args()
     rank, world, local = dist_info()
 
@@ -536,6 +582,7 @@ def main():
     fp64 = None if args.no_fp64 else fp64_leg(args, torch, local)
     batch = batch_leg(args, torch, local) if args.batch_count > 0 else None
     taylor_green = taylor_green_leg(args, torch, local) if args.tg_resolution > 0 else None
+    accuracy = accuracy_leg(args) if args.acc_dp > 0 and rank == 0 else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -559,7 +606,8 @@ def main():
             "gpu_launches": int(mixed["launches"]), "clocks": mixed["clocks"],
             "mixed_precision": {"speedup_vs_fp64_same_case": mixed["speedup_vs_fp64"],
                                 "fp64_same_case": mixed["fp64_same_case"],
-                                "errors_vs_fp64": mixed["errors_vs_fp64"], "lists": mixed["lists"]},
+                                "errors_vs_fp64": mixed["errors_vs_fp64"], "lists": mixed["lists"],
+                                "accuracy_vs_fp64": accuracy},
             "fp64_drop_in": fp64,
             "batch": batch,
             "taylor_green": taylor_green,

@@ -185,7 +185,6 @@ __global__ void k_b_gather(size_t n, const uint32_t *__restrict__ perm, const ui
         dst.off[d * n + k] = o[d];
         dst.off_lo[d * n + k] = noff[(3 + d) * n + i];
         dst.force[d * n + k] = src.force[d * n + i];
-        dst.v_lo[d * n + k] = src.v_lo[d * n + i];
     }
     dst.geo0[k] = make_float4(o[0], o[1], o[2], __uint_as_float(ncell[i]));
     dst.dyn[k] = src.dyn[i];
@@ -414,7 +413,7 @@ __global__ void k_b_download(size_t n, const uint32_t *__restrict__ starts, int 
     for (int d = 0; d < D; ++d)
     {
         out[d * stride + o] = cell_corner(k.m, d, c[d]) + offset_of(f, n, i, d);
-        out[(D + d) * stride + o] = double(v[d]) + double(f.v_lo[d * n + i]);
+        out[(D + d) * stride + o] = v[d];
     }
     out[(2 * D) * stride + o] = double(k.p.rho0) + double(f.drho[i]);
     out[(2 * D + 1) * stride + o] = di.w;
@@ -494,14 +493,12 @@ int b_alloc_state(sphx_batch bt, MPState &s)
     s.dyn = bt->alloc<float4>(n);
     s.off = bt->alloc<float>(D * n);
     s.off_lo = bt->alloc<float>(D * n);
-    s.v_lo = bt->alloc<float>(D * n);
     s.force = bt->alloc<float>(D * n);
     s.drho = bt->alloc<float>(n);
     s.drho_dt = bt->alloc<float>(n);
     s.drho_sum = bt->alloc<float>(n);
     s.id = bt->alloc<uint32_t>(n);
-    if (!s.geo0 || !s.dyn || !s.off || !s.off_lo || !s.v_lo || !s.force || !s.drho || !s.drho_dt || !s.drho_sum ||
-        !s.id)
+    if (!s.geo0 || !s.dyn || !s.off || !s.off_lo || !s.force || !s.drho || !s.drho_dt || !s.drho_sum || !s.id)
         return fail(SPHX_ERR_OUT_OF_MEMORY, "batch state allocation failed");
     return SPHX_OK;
 }
@@ -933,7 +930,6 @@ extern "C" int sphx_batch_create(sphx_ctx ctx, int dim, int count, const sphx_ba
         cudaMemcpy(a0.id, ids.data(), n * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
         // fluid at rest with rho = rho0 and no pressure force yet
         cudaMemset(a0.dyn, 0, n * sizeof(float4)) == cudaSuccess &&
-        cudaMemset(a0.v_lo, 0, size_t(D) * n * 4) == cudaSuccess &&
         cudaMemset(a0.force, 0, size_t(D) * n * 4) == cudaSuccess &&
         cudaMemset(a0.drho, 0, n * 4) == cudaSuccess && cudaMemset(a0.drho_dt, 0, n * 4) == cudaSuccess;
     if (!ok)

@@ -179,7 +179,6 @@ __global__ void k_mp_gather(size_t n, const uint32_t *__restrict__ perm, const u
         dst.off[d * n + k] = o[d];
         dst.off_lo[d * n + k] = noff[(3 + d) * n + i];
         dst.force[d * n + k] = src.force[d * n + i];
-        dst.v_lo[d * n + k] = src.v_lo[d * n + i];
     }
     dst.geo0[k] = make_float4(o[0], o[1], o[2], __uint_as_float(ncell[i]));
     dst.dyn[k] = src.dyn[i];
@@ -608,9 +607,7 @@ __global__ void k_mp_import(size_t n, ImportArgs a, MPFluid f)
 #pragma unroll
     for (int d = 0; d < D; ++d)
     {
-        const double vd = a.vel ? a.vel[d * n + i] : 0.0;
-        v[d] = float(vd);
-        f.v_lo[d * n + i] = float(vd - double(v[d]));
+        v[d] = a.vel ? float(a.vel[d * n + i]) : 0.f;
         f.force[d * n + i] = a.force ? float(a.force[d * n + i]) : 0.f;
         if (f.fprior)
             f.fprior[d * n + i] = a.fprior ? float(a.fprior[d * n + i]) : 0.f;
@@ -657,9 +654,7 @@ __global__ void k_mp_place_state(size_t n, const uint32_t *__restrict__ perm, co
 #pragma unroll
     for (int d = 0; d < D; ++d)
     {
-        const double vd = vel[size_t(i) * D + d];
-        v[d] = float(vd);
-        dst.v_lo[d * n + k] = float(vd - double(v[d]));
+        v[d] = float(vel[size_t(i) * D + d]);
         dst.force[d * n + k] = float(force[size_t(i) * D + d]);
     }
     float dr = float(rho[i] - rho0);
@@ -692,7 +687,7 @@ __global__ void k_mp_download(size_t n, MPConst k, MPFluid f, double *__restrict
     for (int d = 0; d < D; ++d)
     {
         pos[d * n + o] = position(k, f, n, i, d, c);
-        vel[d * n + o] = double(v[d]) + double(f.v_lo[d * n + i]);
+        vel[d * n + o] = v[d];
         force[d * n + o] = f.force[d * n + i];
         if (fprior && f.fprior)
             fprior[d * n + o] = f.fprior[d * n + i];
@@ -720,7 +715,7 @@ __global__ void k_mp_export_rows(size_t n, MPConst k, MPFluid f, double *__restr
     for (int d = 0; d < D; ++d)
     {
         pos[size_t(o) * D + d] = position(k, f, n, i, d, c);
-        vel[size_t(o) * D + d] = double(v[d]) + double(f.v_lo[d * n + i]);
+        vel[size_t(o) * D + d] = v[d];
     }
     rho[o] = double(k.p.rho0) + double(f.drho[i]);
     p[o] = di.w;
@@ -741,7 +736,7 @@ __global__ void k_mp_conservation(size_t n, MPConst k, MPFluid f, double *__rest
 #pragma unroll
         for (int d = 0; d < D; ++d)
         {
-            double v = double(vv[d]) + double(f.v_lo[d * n + i]);
+            double v = vv[d];
             s[1 + d] += m * v;
             v2 += v * v;
             gx += k.gd[d] * (-position(k, f, n, i, d, c));
@@ -782,8 +777,7 @@ __global__ void k_mp_check(size_t n, MPConst k, MPFluid f, unsigned long long *c
 #pragma unroll
         for (int d = 0; d < D; ++d)
         {
-            fin = fin && isfinite(f.off[d * n + i]) && isfinite(f.off_lo[d * n + i]) && isfinite(f.force[d * n + i]) &&
-                  isfinite(f.v_lo[d * n + i]);
+            fin = fin && isfinite(f.off[d * n + i]) && isfinite(f.off_lo[d * n + i]) && isfinite(f.force[d * n + i]);
             const double x = position(k, f, n, i, d, c);
             const double hi = k.m.lower[d] + double(k.m.all_cells[d]) * k.m.gs;
             in = in && !(x < k.m.lower[d] || x > hi);
@@ -954,14 +948,12 @@ int alloc_state(sphx_mp mp, MPFluid &s)
     s.dyn = mp->alloc<float4>(n);
     s.off = mp->alloc<float>(D * n);
     s.off_lo = mp->alloc<float>(D * n);
-    s.v_lo = mp->alloc<float>(D * n);
     s.force = mp->alloc<float>(D * n);
     s.drho = mp->alloc<float>(n);
     s.drho_dt = mp->alloc<float>(n);
     s.drho_sum = mp->alloc<float>(n);
     s.id = mp->alloc<uint32_t>(n);
-    if (!s.geo0 || !s.dyn || !s.off || !s.off_lo || !s.v_lo || !s.force || !s.drho || !s.drho_dt || !s.drho_sum ||
-        !s.id)
+    if (!s.geo0 || !s.dyn || !s.off || !s.off_lo || !s.force || !s.drho || !s.drho_dt || !s.drho_sum || !s.id)
         return fail(SPHX_ERR_OUT_OF_MEMORY, "mixed-precision state allocation failed");
     if (mp->k.periodic)
     {
@@ -1962,17 +1954,16 @@ struct Snapshot
     int take(sphx_mp mp, bool restore)
     {
         size_t n = mp->n, D = size_t(mp->dim);
-        void *src[8] = {mp->a.dyn,  mp->a.off,  mp->a.off_lo,  mp->a.v_lo,
-                        mp->a.force, mp->a.drho, mp->a.drho_dt, mp->slots};
-        size_t bytes[8] = {n * sizeof(float4), D * n * 4, D * n * 4, D * n * 4, D * n * 4, n * 4, n * 4,
+        void *src[7] = {mp->a.dyn, mp->a.off, mp->a.off_lo, mp->a.force, mp->a.drho, mp->a.drho_dt, mp->slots};
+        size_t bytes[7] = {n * sizeof(float4), D * n * 4, D * n * 4, D * n * 4, n * 4, n * 4,
                            2 * sizeof(unsigned long long)};
         if (!restore)
         {
-            bufs.assign(8, nullptr);
-            for (int q = 0; q < 8; ++q)
+            bufs.assign(7, nullptr);
+            for (int q = 0; q < 7; ++q)
                 SPHX_CUDA(cudaMallocAsync(&bufs[q], std::max<size_t>(bytes[q], 1), mp->ctx->stream));
         }
-        for (int q = 0; q < 8; ++q)
+        for (int q = 0; q < 7; ++q)
         {
             void *dst = restore ? src[q] : bufs[q];
             const void *from = restore ? bufs[q] : src[q];

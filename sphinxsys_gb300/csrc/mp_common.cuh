@@ -228,10 +228,6 @@ struct MPState
     // FP32 (what the pair arithmetic reads), off_lo = the FP32 rounding of its residual, so
     // the position integration carries the FP64 offset from step to step
     float *off, *off_lo, *force, *drho, *drho_dt, *drho_sum;
-    // FP32 residual of the velocity (component d of particle i at v_lo[d * n + i]): the
-    // velocity update is a compensated (Kahan) FP32 sum, v + v_lo is the running velocity
-    // and dyn holds v, what the neighbours read
-    float *v_lo;
     uint32_t *id;
     float *fprior, *shift; // periodic flow only: prior (viscous) force, transport-velocity shift
 };
@@ -254,17 +250,6 @@ __device__ __forceinline__ void stage_offset(float *noff, size_t n, size_t i, in
     const float hi = float(x);
     noff[d * n + i] = hi;
     noff[(3 + d) * n + i] = float(x - double(hi));
-}
-
-// Velocity update v += a dt as a compensated FP32 sum on (v, v_lo) (Kahan, 1965): the
-// rounding of each addition is carried in v_lo instead of accumulating over the sub-steps.
-__device__ __forceinline__ float kick(const MPState &f, size_t n, size_t i, int d, float v, float inc)
-{
-    float &lo = f.v_lo[d * n + i];
-    const float y = inc + lo;
-    const float t = v + y;
-    lo = y - (t - v);
-    return t;
 }
 
 // Position half-step x += dt / 2 v in FP64 on the stored pair.
@@ -777,7 +762,7 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
         float vo = vn[d];
         // position half-step in FP64 (initialisation of the 1st half, old velocity)
         half_step(f, n, i, d, dt, vo);
-        vn[d] = kick(f, n, i, d, vo, (k.g[d] + F * k.inv_mass) * dt_f);
+        vn[d] = vo + (k.g[d] + F * k.inv_mass) * dt_f;
         v2 += vn[d] * vn[d];
     }
     // the pressure stays the one the neighbours of this sweep read
@@ -1119,7 +1104,7 @@ __device__ __forceinline__ double first_particle_periodic(size_t i, size_t n, co
         f.force[d * n + i] = F;
         float vo = vn[d];
         half_step(f, n, i, d, dt, vo);
-        vn[d] = kick(f, n, i, d, vo, (f.fprior[d * n + i] + F) * k.inv_mass * dt_f);
+        vn[d] = vo + (f.fprior[d * n + i] + F) * k.inv_mass * dt_f;
         v2 += vn[d] * vn[d];
     }
     f.dyn[i] = make_float4(vn[0], vn[1], D == 3 ? vn[2] : 0.f, p_i);

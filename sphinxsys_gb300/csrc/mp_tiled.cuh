@@ -341,7 +341,7 @@ __device__ __forceinline__ double first_particle_tiled(size_t t, size_t i, size_
         f.force[d * n + i] = F;
         float vo = vn[d];
         half_step(f, n, i, d, dt, vo);
-        vn[d] = kick(f, n, i, d, vo, (k.g[d] + F * k.inv_mass) * dt_f);
+        vn[d] = vo + (k.g[d] + F * k.inv_mass) * dt_f;
         v2 += vn[d] * vn[d];
     }
     f.dyn[i] = make_float4(vn[0], vn[1], D == 3 ? vn[2] : 0.f, p_i);
