@@ -145,9 +145,10 @@ int sphx_exclusive_scan_u32(sphx_ctx ctx, const uint32_t *d_in, uint32_t *d_out,
  * fixed 128 KiB device array of the library that every GPU loading the library holds until
  * the process exits.  At most SPHX_SCAN_NOALLOC_MAX_N entries (larger n returns
  * SPHX_ERR_INVALID_ARG).  The first call on a device looks up the array's address and
- * should come before any stream capture.  Calls share the array: calls that overlap on the
- * GPU race, so serialise them on one stream.  With `total` non-null the call synchronises
- * `stream` to return the sum of all n inputs. */
+ * should come before any stream capture.  The looked-up address is kept for the life of
+ * the process, so calls after a cudaDeviceReset of that device are not supported.  Calls
+ * share the array: calls that overlap on the GPU race, so serialise them on one stream.
+ * With `total` non-null the call synchronises `stream` to return the sum of all n inputs. */
 #define SPHX_SCAN_NOALLOC_MAX_N 67108864u
 int sphx_exclusive_scan_u32_noalloc(void *stream, const uint32_t *d_in, uint32_t *d_out, size_t n, uint32_t *total);
 
