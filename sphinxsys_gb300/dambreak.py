@@ -534,11 +534,19 @@ if __name__ == "__main__":
     ap.add_argument("--run", default=None, choices=["fp64", "mixed"],
                     help="only advance one solver to t_end and report its throughput")
     ap.add_argument("--out", default=None)
+    ap.add_argument("--block", type=int, default=128, help="mixed solver: sweep block size")
+    ap.add_argument("--strategy", type=int, default=0, help="mixed solver: neighbour strategy 0-3")
+    ap.add_argument("--tile", type=int, nargs=3, default=None, help="mixed solver: tile shape (sub-cells)")
     a = ap.parse_args()
     c = dambreak_3d(a.dp) if a.dim == 3 else dambreak_2d(a.dp)
     if a.run:
         import time
-        sim = MixedPrecisionDamBreak(c) if a.run == "mixed" else DamBreak(c)
+        if a.run == "mixed":
+            sim = MixedPrecisionDamBreak(c, block=a.block, strategy=a.strategy)
+            if a.tile:
+                sim.set_tile(*a.tile)
+        else:
+            sim = DamBreak(c)
         n = sim.n_fluid if a.run == "mixed" else sim.water_block.n
         t0, steps, subs = time.perf_counter(), 0, 0
         while sim.physical_time < a.t_end:
