@@ -48,6 +48,11 @@ METRIC = "particle-steps/s (1 GB300): mixed-prec vs FP64 at <=1e-4 rel err; %HBM
 UNIT = "particle-steps/s"
 
 
+def to_json(obj) -> str:
+    """One JSON line; numpy scalars (and anything else with .item()) become Python values."""
+    return json.dumps(obj, default=lambda o: o.item() if hasattr(o, "item") else str(o))
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -191,7 +196,7 @@ def mixed_leg(args, torch, local, world):
     # a probe the water has not reached reads 0 in both runs: no relative error there
     probes = []
     for pos, a, b in zip(case.observers, p_mp, p_fp):
-        wetted = abs(b) > 0.0
+        wetted = bool(abs(b) > 0.0)
         probes.append({"position": list(pos), "mixed": float(a), "fp64": float(b), "wetted": wetted,
                        "abs_err": abs(float(a) - float(b)),
                        "rel_err": abs(float(a) - float(b)) / abs(float(b)) if wetted else None})
@@ -529,7 +534,7 @@ def reference_arm(args, rank, world):
                          "sample": f"{args.steps} advection steps ({subs} acoustic sub-steps) of {case.name}"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    print(json.dumps(line), flush=True)
+    print(to_json(line), flush=True)
 
 
 def main():
@@ -612,7 +617,7 @@ def main():
             "batch": batch,
             "taylor_green": taylor_green,
         }
-        print(json.dumps(line), flush=True)
+        print(to_json(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
