@@ -130,16 +130,18 @@ def traffic_of(key):
 
 def bytes_fp64_second(n_fluid: int, n_wall_active: int, nnz: int) -> int:
     """Integration2ndHalf, FP64 3D: 136 B per fluid particle (read x, v, rho, drho, Vol;
-    write x, rho, drho, F), 80 B per active wall particle (x, V, v_ave, n), 4 B per stored
-    neighbour index."""
-    return 136 * n_fluid + 80 * n_wall_active + 4 * nnz
+    write x, rho, drho, F), 80 B per active wall particle (x, V, v_ave, n), 36 B per stored
+    pair: the neighbour index and the configuration-time dW (8 B) and e (24 B) the classic
+    neighbourhood keeps for the whole advection step."""
+    return 136 * n_fluid + 80 * n_wall_active + 36 * nnz
 
 
 def bytes_mp_second(n_fluid: int, n_wall_active: int, nnz: int) -> int:
-    """Mixed 2nd half, 3D: per fluid particle read geo0 (16), dyn (16), off (12), drho (4),
-    drho_dt (4), write off (12), drho (4), drho_dt (4), force (12) = 84 B; per active wall
-    particle geo (16) and normal (16) = 32 B; 4 B per stored neighbour index."""
-    return 84 * n_fluid + 32 * n_wall_active + 4 * nnz
+    """Mixed 2nd half, 3D: per fluid particle read geo0 (16), dyn (16), the offset pair
+    off + off_lo (24), drho (4), drho_dt (4), write the offset pair (24), drho (4),
+    drho_dt (4), force (12) = 108 B; per active wall particle geo (16) and normal (16) =
+    32 B; 4 B per stored neighbour index."""
+    return 108 * n_fluid + 32 * n_wall_active + 4 * nnz
 
 
 def timed_steps(torch, ctx, step_fn, steps, warmup, sampler=None):
@@ -421,10 +423,10 @@ def batch_leg(args, torch, local):
 
 
 def bytes_mp_second_periodic(n_fluid: int, nnz: int) -> int:
-    """Mixed 2nd half of the periodic flow, 3D: per particle read geo0 (16), dyn (16),
-    off (12), drho (4), drho_dt (4), prior force (12), write off (12), drho (4), drho_dt (4),
-    force (12) = 96 B; 4 B per stored neighbour entry."""
-    return 96 * n_fluid + 4 * nnz
+    """Mixed 2nd half of the periodic flow, 3D: per particle read geo0 (16), dyn (16), the
+    offset pair (24), drho (4), drho_dt (4), prior force (12), write the offset pair (24),
+    drho (4), drho_dt (4), force (12) = 120 B; 4 B per stored neighbour entry."""
+    return 120 * n_fluid + 4 * nnz
 
 
 def taylor_green_leg(args, torch, local):
