@@ -127,6 +127,32 @@ def test_ck_correction_matrix_is_identity_on_a_full_lattice():
     assert np.all(c >= 1.0)
 
 
+def wendland_lattice_sum(dim: int, h_ratio: float = 1.3) -> float:
+    """sum_j W(|x_j|) dp^dim over the lattice points within the cut-off (Wendland C2)."""
+    h, r = h_ratio, np.arange(-4, 5)
+    grids = np.meshgrid(*([r] * dim), indexing="ij")
+    q = np.sqrt(sum(g.astype(float) ** 2 for g in grids)) / h
+    alpha = 21.0 / (16.0 * np.pi * h ** 3) if dim == 3 else 7.0 / (4.0 * np.pi * h ** 2)
+    return float(np.sum(np.where(q < 2.0, alpha * (1 - q / 2) ** 4 * (1 + 2 * q), 0.0)))
+
+
+def test_ck_initial_interior_compression_is_the_lattice_sum():
+    """CompressionSummation with Vol_ref = dp^3 (density_regularization.hpp:40-60, the
+    lattice generator's volume) starts the interior of the 3D SYCL dam break at the
+    kernel's lattice sum, 1.0095 for h = 1.3 dp, not at 1: the initial over-pressure whose
+    release puts the CK mechanical energy above the reference's stored runs."""
+    oc = O.OracleCase(cases.dambreak_3d_reference(0.05))
+    oc.ck_initialize()
+    c = oc.ck_get("Compression")
+    x = oc.get("Position")
+    interior = (x[:, 0] > 0.3) & (x[:, 0] < 1.7) & (x[:, 1] > 0.3) & (x[:, 1] < 0.7) & \
+               (x[:, 2] > 0.15) & (x[:, 2] < 0.35)
+    assert interior.sum() > 100
+    expect = wendland_lattice_sum(3)
+    assert abs(expect - 1.0095) < 1e-4
+    assert np.max(np.abs(c[interior] - expect)) < 2e-3  # tabulated kernel, exact lattice
+
+
 @pytest.mark.slow
 def test_ck_oracle_2d_dambreak_passes_reference_dtw_regression(golden):
     """The CK numerics (tests_sycl/2d_examples/test_2d_dambreak_sycl/dambreak_sycl.cpp loop:
