@@ -529,6 +529,56 @@ inline size_t async_ring_bytes(bool second, unsigned blk)
     return second ? size_t(kAsyncDepthSecond) * blk * (16 + 16 + 4) : size_t(kAsyncDepthFirst) * blk * (16 + 4 + 4);
 }
 
+// ---------------------------------------------------------------- persistent warps (strategy 4)
+// The stored lists of strategy 0 with a grid of the resident capacity: each warp takes the
+// next chunk of 32 consecutive particles from a counter until all are done, so no warp slot
+// idles while a block waits for its slowest warp or while the last wave drains.  The same
+// per-particle work: results equal strategy 0 bit for bit (the time-step maxima are exact
+// maxima, independent of the order).
+__device__ __forceinline__ size_t next_chunk(unsigned int *counter)
+{
+    unsigned c = 0;
+    if ((threadIdx.x & 31u) == 0)
+        c = atomicAdd(counter, 1u);
+    return size_t(__shfl_sync(0xffffffffu, c, 0)) * 32u;
+}
+
+// Blocks of 256 the persistent 1st half is compiled to fit per SM (4: 64 registers with some
+// spills; 3: ~80 registers without): a build-time tuning parameter.
+#ifndef SPHX_PERSISTENT_FIRST_MINB
+#define SPHX_PERSISTENT_FIRST_MINB 4
+#endif
+
+template <int D>
+__global__ void __launch_bounds__(256, SPHX_PERSISTENT_FIRST_MINB) k_mp_first_persistent(size_t n, MPConst k, MPFluid f, MPWall w, MPLists in,
+                                                             MPLists wl, double dt, unsigned long long *ac_slot,
+                                                             unsigned int *counter)
+{
+    double vmax = -1.0e300;
+    for (size_t base = next_chunk(counter); base < n; base = next_chunk(counter))
+    {
+        const size_t i = base + (threadIdx.x & 31u);
+        if (i < n)
+            vmax = fmax(vmax, first_particle<D, true>(i, n, k.p, Visit{k.m, 0u, nullptr, nullptr}, dt, f, w, in, wl));
+    }
+    warp_max_to(ac_slot, vmax);
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) k_mp_second_persistent(size_t n, MPConst k, MPFluid f, MPWall w, MPLists in,
+                                                              MPLists wl, double dt, unsigned long long *adv_slot,
+                                                              unsigned int *counter)
+{
+    double amax = -1.0e300;
+    for (size_t base = next_chunk(counter); base < n; base = next_chunk(counter))
+    {
+        const size_t i = base + (threadIdx.x & 31u);
+        if (i < n)
+            amax = fmax(amax, second_particle<D, true>(i, n, k.p, Visit{k.m, 0u, nullptr, nullptr}, dt, f, w, in, wl));
+    }
+    warp_max_to(adv_slot, amax);
+}
+
 template <int D, bool LISTS, bool ORDER>
 __global__ void __launch_bounds__(256, 4) k_mp_first(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
                const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, double dt,
@@ -882,7 +932,7 @@ struct sphx_mp_s
     MPLists in{}, wl{};
     // device scalars: 0 acoustic max, 1 advection max, 2 misc, 3 build counts, 4-5 state
     // check, 6-7 tile preparation (window maxima, tile count, build overflow), 8 sweep
-    // overflow of the tiled strategy
+    // overflow of the tiled strategy, 10-11 chunk counters of the persistent sweeps
     unsigned long long *slots = nullptr;
     unsigned long long *h_slots = nullptr;
     double physical_time = 0, acoustic_dt = 0;
@@ -1216,6 +1266,41 @@ void launch_second(sphx_mp mp, unsigned blk, double dt)
         n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset, mp->in, mp->wl, dt, mp->slots + 1, mp->order);
 }
 
+// Grid of the resident capacity for a persistent kernel (blocks per SM from the occupancy
+// calculator, times the SMs), the chunk counters cleared before each launch.
+template <class K>
+int persistent_grid(sphx_mp mp, K kernel, unsigned blk, unsigned *grid)
+{
+    int per_sm = 0;
+    SPHX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, int(blk), 0));
+    *grid = unsigned(std::max(1, per_sm) * std::max(1, mp->ctx->num_sms));
+    return SPHX_OK;
+}
+
+template <int D>
+int launch_first_persistent(sphx_mp mp, unsigned blk, double dt)
+{
+    unsigned grid = 0;
+    SPHX_TRY(persistent_grid(mp, k_mp_first_persistent<D>, blk, &grid));
+    unsigned int *counter = reinterpret_cast<unsigned int *>(mp->slots + 10);
+    SPHX_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int), mp->ctx->stream));
+    k_mp_first_persistent<D><<<grid, blk, 0, mp->ctx->stream>>>(mp->n, mp->k, mp->a, mp->w, mp->in, mp->wl, dt,
+                                                                 mp->slots, counter);
+    return SPHX_OK;
+}
+
+template <int D>
+int launch_second_persistent(sphx_mp mp, unsigned blk, double dt)
+{
+    unsigned grid = 0;
+    SPHX_TRY(persistent_grid(mp, k_mp_second_persistent<D>, blk, &grid));
+    unsigned int *counter = reinterpret_cast<unsigned int *>(mp->slots + 11);
+    SPHX_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int), mp->ctx->stream));
+    k_mp_second_persistent<D><<<grid, blk, 0, mp->ctx->stream>>>(mp->n, mp->k, mp->a, mp->w, mp->in, mp->wl, dt,
+                                                                  mp->slots + 1, counter);
+    return SPHX_OK;
+}
+
 template <int D>
 int launch_first_async(sphx_mp mp, unsigned blk, double dt)
 {
@@ -1297,6 +1382,8 @@ int substep(sphx_mp mp, double dt)
         SPHX_TRY(launch_first_tiled<D>(mp, blk, dt));
     else if (mp->strategy == 3)
         SPHX_TRY(launch_first_async<D>(mp, blk, dt));
+    else if (mp->strategy == 4)
+        SPHX_TRY(launch_first_persistent<D>(mp, blk, dt));
     else if (mp->strategy != 1)
         mp->order_active ? launch_first<D, true, true>(mp, blk, dt) : launch_first<D, true, false>(mp, blk, dt);
     else
@@ -1317,6 +1404,8 @@ int substep(sphx_mp mp, double dt)
         SPHX_TRY(launch_second_tiled<D>(mp, blk, dt));
     else if (mp->strategy == 3)
         SPHX_TRY(launch_second_async<D>(mp, blk, dt));
+    else if (mp->strategy == 4)
+        SPHX_TRY(launch_second_persistent<D>(mp, blk, dt));
     else if (mp->strategy != 1)
         mp->order_active ? launch_second<D, true, true>(mp, blk, dt) : launch_second<D, true, false>(mp, blk, dt);
     else
@@ -1555,7 +1644,7 @@ extern "C" int sphx_mp_create(sphx_relation inner, sphx_relation wall, const sph
     mp->w.nw = nw;
     mp->in.count = mp->alloc<uint32_t>(n);
     mp->wl.count = mp->alloc<uint32_t>(n);
-    mp->slots = mp->alloc<unsigned long long>(10);
+    mp->slots = mp->alloc<unsigned long long>(12);
     mp->order = mp->alloc<uint32_t>(n);
     mp->tile_offset = mp->alloc<uint32_t>(nc + 1);
     mp->tiles = mp->alloc<uint32_t>(nc);
@@ -1565,9 +1654,9 @@ extern "C" int sphx_mp_create(sphx_relation inner, sphx_relation wall, const sph
         !mp->noff || !mp->w.geo || !mp->w.n || !mp->in.count || !mp->wl.count || !mp->slots || !mp->order ||
         !mp->tile_offset || !mp->tiles || !mp->tile_flags || !mp->tile_pos)
         return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "mixed-precision allocation failed"));
-    if (cudaMemsetAsync(mp->slots, 0, 10 * sizeof(unsigned long long), ctx->stream) != cudaSuccess)
+    if (cudaMemsetAsync(mp->slots, 0, 12 * sizeof(unsigned long long), ctx->stream) != cudaSuccess)
         return bail(fail(SPHX_ERR_CUDA, "slot initialisation failed"));
-    if (cudaMallocHost(&mp->h_slots, 10 * sizeof(unsigned long long)) != cudaSuccess)
+    if (cudaMallocHost(&mp->h_slots, 12 * sizeof(unsigned long long)) != cudaSuccess)
         return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "pinned allocation failed"));
     if ((st = alloc_lists(mp, mp->in, D == 2 ? 24 : 96)) != SPHX_OK ||
         (st = alloc_lists(mp, mp->wl, D == 2 ? 16 : 64)) != SPHX_OK)
@@ -1712,13 +1801,13 @@ extern "C" int sphx_mp_create_periodic(sphx_body fb, const sphx_fluid_params *p,
     mp->noff = mp->alloc<float>(6 * n);
     mp->in.count = mp->alloc<uint32_t>(n);
     mp->wl.count = mp->alloc<uint32_t>(n);
-    mp->slots = mp->alloc<unsigned long long>(10);
+    mp->slots = mp->alloc<unsigned long long>(12);
     if (!mp->f_offset || !mp->w_offset || !mp->count || !mp->key || !mp->rank || !mp->perm || !mp->ncell ||
         !mp->noff || !mp->in.count || !mp->wl.count || !mp->slots)
         return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "mixed-precision allocation failed"));
-    if (cudaMemsetAsync(mp->slots, 0, 10 * sizeof(unsigned long long), ctx->stream) != cudaSuccess)
+    if (cudaMemsetAsync(mp->slots, 0, 12 * sizeof(unsigned long long), ctx->stream) != cudaSuccess)
         return bail(fail(SPHX_ERR_CUDA, "slot initialisation failed"));
-    if (cudaMallocHost(&mp->h_slots, 10 * sizeof(unsigned long long)) != cudaSuccess)
+    if (cudaMallocHost(&mp->h_slots, 12 * sizeof(unsigned long long)) != cudaSuccess)
         return bail(fail(SPHX_ERR_OUT_OF_MEMORY, "pinned allocation failed"));
     if ((st = alloc_lists(mp, mp->in, D == 2 ? 24 : 96)) != SPHX_OK || (st = alloc_lists(mp, mp->wl, 1)) != SPHX_OK)
         return bail(st);
@@ -2004,6 +2093,7 @@ extern "C" int sphx_mp_autotune(sphx_mp mp, int reps, int *best_block, int *best
     if (!mp->k.periodic)
     {
         settings.push_back(Setting{3, {0, 0, 0}});
+        settings.push_back(Setting{4, {0, 0, 0}});
         if (mp->dim == 3)
             for (const Setting &t : {Setting{2, {4, 4, 4}}, Setting{2, {4, 4, 8}}})
                 settings.push_back(t);
@@ -2086,10 +2176,10 @@ extern "C" int sphx_mp_autotune(sphx_mp mp, int reps, int *best_block, int *best
 
 extern "C" int sphx_mp_set_tuning(sphx_mp mp, int block, int strategy)
 {
-    if (!mp || block < 64 || block > 256 || block % 32 != 0 || strategy < 0 || strategy > 3)
-        return fail(SPHX_ERR_INVALID_ARG, "block must be 64..256 in steps of 32, strategy 0, 1, 2 or 3");
-    if (strategy == 3 && mp->k.periodic)
-        return fail(SPHX_ERR_INVALID_ARG, "the asynchronous-gather strategy serves the dam-break solver only");
+    if (!mp || block < 64 || block > 256 || block % 32 != 0 || strategy < 0 || strategy > 4)
+        return fail(SPHX_ERR_INVALID_ARG, "block must be 64..256 in steps of 32, strategy 0 to 4");
+    if (strategy >= 3 && mp->k.periodic)
+        return fail(SPHX_ERR_INVALID_ARG, "strategies 3 and 4 serve the dam-break solver only");
     if (strategy == 2 && mp->k.periodic)
         return fail(SPHX_ERR_INVALID_ARG, "the tiled strategy serves the dam-break solver only");
     if (strategy == 2 && (mp->tile[0] > kTileMaxExtent || mp->tile[1] > kTileMaxExtent || mp->tile[2] > kTileMaxExtent))

@@ -75,7 +75,8 @@ def test_strategies_and_block_sizes_bitwise_equal():
 def test_tiled_and_async_strategies_bitwise_equal(case, tiles):
     """Strategy 2 (tile windows staged in shared memory, lists of staged indices) and
     strategy 3 (the stored lists with records gathered by cp.async into a shared-memory
-    ring) visit the same neighbours in the same order with the same arithmetic as the
+    ring) and strategy 4 (the stored lists on persistent warps taking chunks of particles)
+    visit the same neighbours in the same order with the same arithmetic as the
     stored lists of strategy 0: equal bit for bit, for every tile shape and block size; so
     does the tile-grouped traversal of strategy 0."""
     def run(block, strategy, tile):
@@ -87,7 +88,7 @@ def test_tiled_and_async_strategies_bitwise_equal(case, tiles):
         return subs, [mp.fp64.water_block.download(n) for n in ("Position", "Velocity", "Density", "Pressure")]
 
     ref_subs, ref = run(128, 0, None)
-    runs = [(128, 0, tiles[0])] + [(b, 2, t) for t in tiles for b in (64, 256)] + [(b, 3, None) for b in (64, 256)]
+    runs = [(128, 0, tiles[0])] + [(b, 2, t) for t in tiles for b in (64, 256)] + [(b, s_, None) for b in (64, 256) for s_ in (3, 4)]
     for block, strategy, tile in runs:
         subs, out = run(block, strategy, tile)
         assert subs == ref_subs, (block, strategy, tile)
