@@ -359,8 +359,10 @@ int sphx_mp_check_state(sphx_mp mp, uint64_t *non_finite, uint64_t *out_of_mesh)
  * the sweep kernels, and 0 = stored neighbour index lists, 1 = cell sweep every
  * sub-step, 2 = tiled (dam-break solver): one block per tile of sub-cells with the tile's
  * neighbour window staged in shared memory and lists of indices into it (tile shape from
- * sphx_mp_set_tile, 4 x 4 (x 4) by default, at most 8 per axis).  All three give the same
- * results bit for bit. */
+ * sphx_mp_set_tile, 4 x 4 (x 4) by default, at most 8 per axis), 3 = the stored lists with
+ * the neighbour records gathered by cp.async into a per-thread ring in shared memory,
+ * 4 = the stored lists on persistent warps that take chunks of 32 particles (3 and 4
+ * dam-break solver only).  All give the same results bit for bit. */
 int sphx_mp_set_tuning(sphx_mp mp, int block, int strategy);
 /* Tile-grouped traversal of the sweeps and the neighbour build (dam-break solver): the
  * particles of each box of tx x ty (x tz) sub-cells go to consecutive threads, so a thread
