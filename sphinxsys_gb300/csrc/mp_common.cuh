@@ -494,23 +494,6 @@ struct Visit
     const uint32_t *f_offset, *w_offset;
 };
 
-// A stored list entry.  The lists stream from DRAM once per sweep (about 4 B x 78 per
-// particle, several times the particle records), so they are loaded with the streaming
-// (evict-first) cache policy: they should not push the particle records, which every
-// neighbour gathers again, out of L2.  SPHX_LIST_LOAD_STREAMING=0 at build time loads
-// them as read-only data instead.
-#ifndef SPHX_LIST_LOAD_STREAMING
-#define SPHX_LIST_LOAD_STREAMING 1
-#endif
-__device__ __forceinline__ uint32_t list_entry(const uint32_t *p)
-{
-#if SPHX_LIST_LOAD_STREAMING
-    return __ldcs(p);
-#else
-    return __ldg(p);
-#endif
-}
-
 // Calls pair(x) for every stored neighbour of i, with U neighbour records loaded
 // before the arithmetic, and flush() after every kGroup neighbours; load(j) fetches what
 // pair() consumes.  PREFETCH also loads the next U list entries before the current
@@ -529,7 +512,7 @@ __device__ __forceinline__ void list_sweep(size_t i, size_t n, const MPNeighbors
     {
 #pragma unroll
         for (int u = 0; u < U; ++u)
-            jn[u] = list_entry(&J[size_t(u) * n]);
+            jn[u] = __ldg(&J[size_t(u) * n]);
     }
     for (; s + kGroup <= c; s += kGroup)
     {
@@ -547,14 +530,14 @@ __device__ __forceinline__ void list_sweep(size_t i, size_t n, const MPNeighbors
                 {
 #pragma unroll
                     for (int u = 0; u < U; ++u)
-                        jn[u] = list_entry(&J[size_t(nx + u) * n]);
+                        jn[u] = __ldg(&J[size_t(nx + u) * n]);
                 }
             }
             else
             {
 #pragma unroll
                 for (int u = 0; u < U; ++u)
-                    jj[u] = list_entry(&J[size_t(s + h + u) * n]);
+                    jj[u] = __ldg(&J[size_t(s + h + u) * n]);
             }
             decltype(load(0u)) rec[U];
 #pragma unroll
@@ -567,7 +550,7 @@ __device__ __forceinline__ void list_sweep(size_t i, size_t n, const MPNeighbors
         flush();
     }
     for (; s < c; ++s)
-        pair(load(list_entry(&J[size_t(s) * n])));
+        pair(load(__ldg(&J[size_t(s) * n])));
     flush();
 }
 
