@@ -361,8 +361,11 @@ int sphx_mp_check_state(sphx_mp mp, uint64_t *non_finite, uint64_t *out_of_mesh)
  * neighbour window staged in shared memory and lists of indices into it (tile shape from
  * sphx_mp_set_tile, 4 x 4 (x 4) by default, at most 8 per axis), 3 = the stored lists with
  * the neighbour records gathered by cp.async into a per-thread ring in shared memory,
- * 4 = the stored lists on persistent warps that take chunks of 32 particles (3 and 4
- * dam-break solver only).  All give the same results bit for bit. */
+ * 4 = the stored lists on persistent warps that take chunks of 32 particles, 5 and 6 =
+ * the stored lists with 2 and 4 lanes per particle (16 and 8 particles per warp; each
+ * lane takes every 2nd / 4th list slot, sums combined by warp shuffles) (3 to 6 dam-break
+ * solver only).  Strategies 0 to 4 give the same results bit for bit; 5 and 6 sum each
+ * particle's neighbours in another order and agree with them to FP32 rounding. */
 int sphx_mp_set_tuning(sphx_mp mp, int block, int strategy);
 /* Tile-grouped traversal of the sweeps and the neighbour build (dam-break solver): the
  * particles of each box of tx x ty (x tz) sub-cells go to consecutive threads, so a thread
@@ -374,7 +377,8 @@ int sphx_mp_set_tile(sphx_mp mp, int tx, int ty, int tz);
 /* Current launch block, neighbour strategy and tile shape (tile: 3 ints; any may be null). */
 int sphx_mp_get_tuning(sphx_mp mp, int *block, int *strategy, int *tile);
 /* Times one acoustic sub-step for every block size (64, 128, 256) with each neighbour
- * strategy (the tiled one with several tile shapes), restores the state it advanced,
+ * strategy (the tiled one with several tile shapes, the lane-split ones with 2 and 4
+ * lanes per particle), restores the state it advanced,
  * and keeps the fastest setting; outputs (any may be null) the chosen block, strategy and
  * ms per sub-step (sphx_mp_get_tuning gives the tile shape). */
 int sphx_mp_autotune(sphx_mp mp, int reps, int *best_block, int *best_strategy, double *best_ms);

@@ -579,6 +579,40 @@ __global__ void __launch_bounds__(256) k_mp_second_persistent(size_t n, MPConst 
     warp_max_to(adv_slot, amax);
 }
 
+// ---------------------------------------------------------------- lanes per particle (strategies 5, 6)
+// The stored lists of strategy 0 with LANES (2 or 4) consecutive lanes on each particle,
+// 32 / LANES particles per warp: the lanes split the list slots (lane s takes slots s,
+// s + LANES, ...), so a warp walks lists LANES times shorter and the lanes of a warp wait
+// on fewer ragged list lengths.  Each lane keeps its own compensated sums, combined by warp
+// shuffles at the end: a different summation order from strategy 0, so the results agree
+// to FP32 rounding, not bit for bit.
+template <int D, int LANES>
+__global__ void __launch_bounds__(256, 4) k_mp_first_lanes(size_t n, MPConst k, MPFluid f, MPWall w, MPLists in,
+                                                           MPLists wl, double dt, unsigned long long *ac_slot)
+{
+    const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    double vmax = -1.0e300;
+    if (t / LANES < n) // whole groups: blocks hold a multiple of LANES threads
+        vmax = first_particle<D, true, 0, LANES>(t / LANES, n, k.p, Visit{k.m, 0u, nullptr, nullptr}, dt, f, w, in,
+                                                 wl);
+    warp_max_to(ac_slot, vmax);
+}
+
+template <int D, int LANES>
+__global__ void k_mp_second_lanes(size_t n, MPConst k, MPFluid f, MPWall w, MPLists in, MPLists wl, double dt,
+                                  unsigned long long *adv_slot)
+{
+    const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    double amax = -1.0e300;
+    if (t / LANES < n)
+        amax = second_particle<D, true, 0, LANES>(t / LANES, n, k.p, Visit{k.m, 0u, nullptr, nullptr}, dt, f, w,
+                                                  in, wl);
+    warp_max_to(adv_slot, amax);
+}
+
+// Lanes per particle of strategies 5 and 6 (0 for the others).
+inline int strategy_lanes(int strategy) { return strategy == 5 ? 2 : (strategy == 6 ? 4 : 0); }
+
 template <int D, bool LISTS, bool ORDER>
 __global__ void __launch_bounds__(256, 4) k_mp_first(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
                const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, double dt,
@@ -1266,6 +1300,32 @@ void launch_second(sphx_mp mp, unsigned blk, double dt)
         n, mp->k, mp->a, mp->f_offset, mp->w, mp->w_offset, mp->in, mp->wl, dt, mp->slots + 1, mp->order);
 }
 
+template <int D>
+void launch_first_lanes(sphx_mp mp, unsigned blk, double dt)
+{
+    const size_t n = mp->n;
+    cudaStream_t s = mp->ctx->stream;
+    if (strategy_lanes(mp->strategy) == 2)
+        k_mp_first_lanes<D, 2><<<grid_for(2 * n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->w, mp->in, mp->wl, dt,
+                                                                    mp->slots);
+    else
+        k_mp_first_lanes<D, 4><<<grid_for(4 * n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->w, mp->in, mp->wl, dt,
+                                                                    mp->slots);
+}
+
+template <int D>
+void launch_second_lanes(sphx_mp mp, unsigned blk, double dt)
+{
+    const size_t n = mp->n;
+    cudaStream_t s = mp->ctx->stream;
+    if (strategy_lanes(mp->strategy) == 2)
+        k_mp_second_lanes<D, 2><<<grid_for(2 * n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->w, mp->in, mp->wl, dt,
+                                                                     mp->slots + 1);
+    else
+        k_mp_second_lanes<D, 4><<<grid_for(4 * n, blk), blk, 0, s>>>(n, mp->k, mp->a, mp->w, mp->in, mp->wl, dt,
+                                                                     mp->slots + 1);
+}
+
 // Grid of the resident capacity for a persistent kernel (blocks per SM from the occupancy
 // calculator, times the SMs), the chunk counters cleared before each launch.
 template <class K>
@@ -1384,6 +1444,8 @@ int substep(sphx_mp mp, double dt)
         SPHX_TRY(launch_first_async<D>(mp, blk, dt));
     else if (mp->strategy == 4)
         SPHX_TRY(launch_first_persistent<D>(mp, blk, dt));
+    else if (strategy_lanes(mp->strategy))
+        launch_first_lanes<D>(mp, blk, dt);
     else if (mp->strategy != 1)
         mp->order_active ? launch_first<D, true, true>(mp, blk, dt) : launch_first<D, true, false>(mp, blk, dt);
     else
@@ -1406,6 +1468,8 @@ int substep(sphx_mp mp, double dt)
         SPHX_TRY(launch_second_async<D>(mp, blk, dt));
     else if (mp->strategy == 4)
         SPHX_TRY(launch_second_persistent<D>(mp, blk, dt));
+    else if (strategy_lanes(mp->strategy))
+        launch_second_lanes<D>(mp, blk, dt);
     else if (mp->strategy != 1)
         mp->order_active ? launch_second<D, true, true>(mp, blk, dt) : launch_second<D, true, false>(mp, blk, dt);
     else
@@ -2092,8 +2156,8 @@ extern "C" int sphx_mp_autotune(sphx_mp mp, int reps, int *best_block, int *best
     std::vector<Setting> settings = {{0, {0, 0, 0}}, {1, {0, 0, 0}}};
     if (!mp->k.periodic)
     {
-        settings.push_back(Setting{3, {0, 0, 0}});
-        settings.push_back(Setting{4, {0, 0, 0}});
+        for (int st : {3, 4, 5, 6})
+            settings.push_back(Setting{st, {0, 0, 0}});
         if (mp->dim == 3)
             for (const Setting &t : {Setting{2, {4, 4, 4}}, Setting{2, {4, 4, 8}}})
                 settings.push_back(t);
@@ -2176,8 +2240,8 @@ extern "C" int sphx_mp_autotune(sphx_mp mp, int reps, int *best_block, int *best
 
 extern "C" int sphx_mp_set_tuning(sphx_mp mp, int block, int strategy)
 {
-    if (!mp || block < 64 || block > 256 || block % 32 != 0 || strategy < 0 || strategy > 4)
-        return fail(SPHX_ERR_INVALID_ARG, "block must be 64..256 in steps of 32, strategy 0 to 4");
+    if (!mp || block < 64 || block > 256 || block % 32 != 0 || strategy < 0 || strategy > 6)
+        return fail(SPHX_ERR_INVALID_ARG, "block must be 64..256 in steps of 32, strategy 0 to 6");
     if (strategy >= 3 && mp->k.periodic)
         return fail(SPHX_ERR_INVALID_ARG, "strategies 3 and 4 serve the dam-break solver only");
     if (strategy == 2 && mp->k.periodic)

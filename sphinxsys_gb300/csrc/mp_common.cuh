@@ -494,25 +494,52 @@ struct Visit
     const uint32_t *f_offset, *w_offset;
 };
 
+// This lane's place in its group of LANES consecutive lanes (0 when LANES is 1).
+template <int LANES>
+__device__ __forceinline__ unsigned lane_in_group()
+{
+    return LANES == 1 ? 0u : (threadIdx.x & unsigned(LANES - 1));
+}
+
+// Sum of v over the LANES lanes of this lane's group (consecutive lanes, LANES a power of
+// two dividing 32); every lane of the group gets the sum.
+template <int LANES>
+__device__ __forceinline__ float group_sum(float v)
+{
+    if (LANES > 1)
+    {
+        const unsigned lane = threadIdx.x & 31u;
+        const unsigned mask = ((1u << LANES) - 1u) << (lane & ~unsigned(LANES - 1));
+#pragma unroll
+        for (int o = LANES / 2; o > 0; o >>= 1)
+            v += __shfl_xor_sync(mask, v, o);
+    }
+    return v;
+}
+
 // Calls pair(x) for every stored neighbour of i, with U neighbour records loaded
 // before the arithmetic, and flush() after every kGroup neighbours; load(j) fetches what
 // pair() consumes.  PREFETCH also loads the next U list entries before the current
 // records are used (one list read in flight behind the record gathers); it pays where the
 // records are small (1st half), not where the extra registers cost occupancy (2nd half).
-template <bool PREFETCH, int U, class Load, class Pair, class Flush>
+// With LANES > 1 the lanes of a group share the particle: lane `sub` visits the list slots
+// sub, sub + LANES, sub + 2 LANES, ... (its own compensated sums, combined afterwards).
+template <bool PREFETCH, int U, int LANES = 1, class Load, class Pair, class Flush>
 __device__ __forceinline__ void list_sweep(size_t i, size_t n, const MPNeighbors &l, Load &&load, Pair &&pair,
-                                           Flush &&flush)
+                                           Flush &&flush, unsigned sub = 0)
 {
     static_assert(kGroup % U == 0, "groups hold whole unrolled batches");
-    const unsigned c = min(l.count[i], l.cap);
-    const uint32_t *J = l.J + i;
+    const unsigned call = min(l.count[i], l.cap);
+    const unsigned c = LANES == 1 ? call : (call > sub ? (call - sub + LANES - 1) / LANES : 0u);
+    const uint32_t *J = l.J + i + size_t(LANES == 1 ? 0u : sub) * n;
+    const size_t stride = size_t(LANES) * n;
     unsigned s = 0;
     uint32_t jn[U];
     if (PREFETCH && c >= U)
     {
 #pragma unroll
         for (int u = 0; u < U; ++u)
-            jn[u] = __ldg(&J[size_t(u) * n]);
+            jn[u] = __ldg(&J[size_t(u) * stride]);
     }
     for (; s + kGroup <= c; s += kGroup)
     {
@@ -530,14 +557,14 @@ __device__ __forceinline__ void list_sweep(size_t i, size_t n, const MPNeighbors
                 {
 #pragma unroll
                     for (int u = 0; u < U; ++u)
-                        jn[u] = __ldg(&J[size_t(nx + u) * n]);
+                        jn[u] = __ldg(&J[size_t(nx + u) * stride]);
                 }
             }
             else
             {
 #pragma unroll
                 for (int u = 0; u < U; ++u)
-                    jj[u] = __ldg(&J[size_t(s + h + u) * n]);
+                    jj[u] = __ldg(&J[size_t(s + h + u) * stride]);
             }
             decltype(load(0u)) rec[U];
 #pragma unroll
@@ -550,7 +577,7 @@ __device__ __forceinline__ void list_sweep(size_t i, size_t n, const MPNeighbors
         flush();
     }
     for (; s < c; ++s)
-        pair(load(__ldg(&J[size_t(s) * n])));
+        pair(load(__ldg(&J[size_t(s) * stride])));
     flush();
 }
 
@@ -673,7 +700,10 @@ struct SecondRec
 // acoustic-time-step candidate c0 + |v|.
 // DEPTH > 0: the stored lists with the neighbour records gathered through an AsyncRing of
 // that depth (ring: slots for geo0 in a, the pressure in c).
-template <int D, bool LISTS, int DEPTH = 0>
+// LANES > 1: the stored lists, LANES consecutive lanes on particle i (list slots strided
+// over the lanes, sums combined by shuffles); the first lane of the group writes the state
+// and returns the candidate, the others return -1e300.
+template <int D, bool LISTS, int DEPTH = 0, int LANES = 1>
 __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPParams &k, const Visit &v, double dt,
                                                  const MPState &f, const MPWallData &w, const MPNeighbors &in,
                                                  const MPNeighbors &wl, const AsyncRing<DEPTH> *ring = nullptr)
@@ -718,7 +748,7 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
         list_sweep_async<DEPTH>(i, n, in, rg, issue, read, pair, flush);
     }
     else if (LISTS)
-        list_sweep<true, kUnrollFirst>(i, n, in, load, pair, flush);
+        list_sweep<true, kUnrollFirst, LANES>(i, n, in, load, pair, flush, lane_in_group<LANES>());
     else
         cell_sweep<D, true>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, i, f.geo0, load, pair, flush);
 
@@ -745,19 +775,29 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
     };
     auto wload = [&](uint32_t j) { return __ldg(&w.geo[j]); };
     if (LISTS || DEPTH > 0)
-        list_sweep<true, kUnrollFirst>(i, n, wl, wload, wpair, wflush);
+        list_sweep<true, kUnrollFirst, LANES>(i, n, wl, wload, wpair, wflush, lane_in_group<LANES>());
     else
         cell_sweep<D, false>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, ~size_t(0), w.geo, wload,
                              wpair, wflush);
 
-    f.drho_dt[i] = (rdis.value() * k.inv_z) * rho_i + (wrdis.value() * k.inv_z) * rho_i;
+    float fsum[3], wfsum[3];
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        fsum[d] = group_sum<LANES>(force[d].value());
+        wfsum[d] = group_sum<LANES>(wforce[d].value());
+    }
+    const float rsum = group_sum<LANES>(rdis.value()), wrsum = group_sum<LANES>(wrdis.value());
+    if (lane_in_group<LANES>() != 0)
+        return -1.0e300;
+    f.drho_dt[i] = (rsum * k.inv_z) * rho_i + (wrsum * k.inv_z) * rho_i;
     float v2 = 0.f;
     float vn[3] = {di.x, di.y, di.z};
     const float dt_f = float(dt);
 #pragma unroll
     for (int d = 0; d < D; ++d)
     {
-        float F = f.force[d * n + i] + force[d].value() * k.Vol + wforce[d].value() * k.Vol;
+        float F = f.force[d * n + i] + fsum[d] * k.Vol + wfsum[d] * k.Vol;
         f.force[d * n + i] = F;
         float vo = vn[d];
         // position half-step in FP64 (initialisation of the 1st half, old velocity)
@@ -774,8 +814,8 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
 // dissipation against fluid and wall neighbours, density update.  Returns the
 // advection-time-step candidate max(|v|^2, 4 h |F + F_prior| / m).
 // DEPTH > 0: the stored lists with the neighbour records gathered through an AsyncRing of
-// that depth (ring: slots for geo0 in a, dyn in b).
-template <int D, bool LISTS, int DEPTH = 0>
+// that depth (ring: slots for geo0 in a, dyn in b).  LANES as first_particle.
+template <int D, bool LISTS, int DEPTH = 0, int LANES = 1>
 __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPParams &k, const Visit &v, double dt,
                                                   const MPState &f, const MPWallData &w, const MPNeighbors &in,
                                                   const MPNeighbors &wl, const AsyncRing<DEPTH> *ring = nullptr)
@@ -822,7 +862,7 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
         list_sweep_async<DEPTH>(i, n, in, rg, issue, read, pair, flush);
     }
     else if (LISTS)
-        list_sweep<false, kUnrollSecond>(i, n, in, load, pair, flush);
+        list_sweep<false, kUnrollSecond, LANES>(i, n, in, load, pair, flush, lane_in_group<LANES>());
     else
         cell_sweep<D, true>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, i, f.geo0, load, pair, flush);
 
@@ -851,19 +891,29 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
     };
     auto wload = [&](uint32_t j) { return SecondRec{__ldg(&w.geo[j]), __ldg(&w.n[j])}; };
     if (LISTS || DEPTH > 0)
-        list_sweep<false, kUnrollSecond>(i, n, wl, wload, wpair, wflush);
+        list_sweep<false, kUnrollSecond, LANES>(i, n, wl, wload, wpair, wflush, lane_in_group<LANES>());
     else
         cell_sweep<D, false>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, ~size_t(0), w.geo, wload,
                              wpair, wflush);
 
-    float drho_dt = f.drho_dt[i] + rate.value() * rho_i + wrate.value() * rho_i;
+    float psum[3], wpsum[3];
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        psum[d] = group_sum<LANES>(pdis[d].value());
+        wpsum[d] = group_sum<LANES>(wdis[d].value());
+    }
+    const float ratesum = group_sum<LANES>(rate.value()), wratesum = group_sum<LANES>(wrate.value());
+    if (lane_in_group<LANES>() != 0)
+        return -1.0e300;
+    float drho_dt = f.drho_dt[i] + ratesum * rho_i + wratesum * rho_i;
     f.drho_dt[i] = drho_dt;
     f.drho[i] = f.drho[i] + drho_dt * float(0.5 * dt);
     float v2 = 0.f, a2 = 0.f;
 #pragma unroll
     for (int d = 0; d < D; ++d)
     {
-        float F = pdis[d].value() * k.Vol + wdis[d].value() * k.Vol;
+        float F = psum[d] * k.Vol + wpsum[d] * k.Vol;
         f.force[d * n + i] = F;
         half_step(f, n, i, d, dt, vi[d]);
         v2 += vi[d] * vi[d];

@@ -535,7 +535,7 @@ if __name__ == "__main__":
                     help="only advance one solver to t_end and report its throughput")
     ap.add_argument("--out", default=None)
     ap.add_argument("--block", type=int, default=128, help="mixed solver: sweep block size")
-    ap.add_argument("--strategy", type=int, default=0, help="mixed solver: neighbour strategy 0-3")
+    ap.add_argument("--strategy", type=int, default=0, help="mixed solver: neighbour strategy 0-6")
     ap.add_argument("--tile", type=int, nargs=3, default=None, help="mixed solver: tile shape (sub-cells)")
     a = ap.parse_args()
     c = dambreak_3d(a.dp) if a.dim == 3 else dambreak_2d(a.dp)

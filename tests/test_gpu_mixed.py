@@ -96,6 +96,33 @@ def test_tiled_and_async_strategies_bitwise_equal(case, tiles):
             assert np.array_equal(a, b), (block, strategy, tile)
 
 
+@pytest.mark.parametrize("case", [cases.dambreak_2d(), cases.dambreak_3d(0.04)], ids=lambda c: c.name)
+def test_lane_split_strategies_agree_with_stored_lists(case):
+    """Strategies 5 and 6 put 2 and 4 lanes on each particle (each lane takes every 2nd /
+    4th slot of the stored lists; the lanes' compensated sums are combined by warp
+    shuffles): the same pairs summed in another order.  After 5 advection steps the state
+    agrees with strategy 0 to the rounding of a re-ordered FP32 sum (1e-5 relative, the
+    bound of the re-imported state, whose cells order their particles differently), with
+    the same sub-step counts; each lane count gives the same bits for every block size."""
+    def run(block, strategy):
+        mp = MixedPrecisionDamBreak(case, block=block, strategy=strategy)
+        subs = [mp.advection_step()[0] for _ in range(5)]
+        mp.sync_fp64()
+        return subs, [mp.fp64.water_block.download(n) for n in ("Position", "Velocity", "Density")]
+
+    ref_subs, ref = run(128, 0)
+    for strategy in (5, 6):
+        subs, out = run(128, strategy)
+        assert subs == ref_subs, strategy
+        errs = [rel_err(o, r) for o, r in zip(out, ref)]
+        print(case.name, strategy, errs)
+        assert max(errs) < 1e-5, (strategy, errs)
+        subs2, out2 = run(64, strategy)
+        assert subs2 == subs
+        for a, b in zip(out, out2):
+            assert np.array_equal(a, b), strategy
+
+
 def test_tiled_strategy_rejects_large_tiles():
     from sphinxsys_gb300.native import SphxError
     mp = MixedPrecisionDamBreak(cases.dambreak_2d(), strategy=2)
