@@ -35,6 +35,7 @@ extern "C" {
 #define SPHX_ERR_TIMEOUT 6      /* a bounded device wait gave up */
 #define SPHX_ERR_NUMERIC 7      /* non-finite value detected by a checked entry point */
 #define SPHX_ERR_NO_DEVICE 8
+#define SPHX_ERR_BOUNDS 9       /* an index test of the bounds-checked build failed */
 
 typedef struct sphx_ctx_s *sphx_ctx;
 typedef struct sphx_body_s *sphx_body;
@@ -47,6 +48,16 @@ typedef enum { SPHX_F64 = 0, SPHX_U32 = 1, SPHX_F32 = 2, SPHX_I32 = 3 } sphx_dty
 const char *sphx_last_error(void);
 /* Library version string. */
 const char *sphx_version(void);
+/* 1 when the library was built with -DSPHX_CHECK (bounds-checked build), else 0. */
+int sphx_checked_build(void);
+/* Bounds-checked build: the kernels test the neighbour-list entries, cell-list ranges and
+ * cell indices they read through, count each failed test, skip its access and keep the
+ * first one (site in the high 16 bits: 1 list entry, 2 cell range, 3 cell index; the
+ * offending value in the low 48).  Synchronises the device, outputs (may be null) the
+ * count and the first record since the last reset, clears them when reset != 0, and
+ * returns SPHX_ERR_BOUNDS when the count is non-zero.  In other builds the count is 0.
+ * The reference indexes its containers unchecked (no counterpart). */
+int sphx_check_violations(uint64_t *count, uint64_t *first, int reset);
 
 /* ------------------------------------------------------------------ context
  * Replaces the SYCL device queue singleton and USM helpers

@@ -1,5 +1,7 @@
 """In-tree build of libsphx_cuda.so for sm_103a (nvcc, one translation unit per source,
-compiled in parallel, linked with -shared).  Output: sphinxsys_gb300/_build/."""
+compiled in parallel, linked with -shared).  Output: sphinxsys_gb300/_build/; the
+bounds-checked build (-DSPHX_CHECK: index tests in the kernels, read with
+sphx_check_violations) goes to sphinxsys_gb300/_build_check/."""
 from __future__ import annotations
 
 import concurrent.futures as cf
@@ -13,6 +15,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libsphx_cuda.so")
+OUT_DIR_CHECK = os.path.join(HERE, "_build_check")
+LIB_CHECK = os.path.join(OUT_DIR_CHECK, "libsphx_cuda.so")
 SOURCES = ["sphx_core.cu", "cell_list.cu", "relation.cu", "fluid.cu", "mixed.cu", "batch.cu", "ck.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
@@ -32,8 +36,8 @@ def _headers_mtime() -> float:
     return max(os.path.getmtime(p) for p in paths)
 
 
-def _compile(src: str, extra: list) -> str:
-    obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
+def _compile(src: str, extra: list, out_dir: str = OUT_DIR) -> str:
+    obj = os.path.join(out_dir, os.path.splitext(src)[0] + ".o")
     s = os.path.join(CSRC, src)
     if os.path.exists(obj) and os.path.getmtime(obj) > max(os.path.getmtime(s), _headers_mtime()):
         return obj
@@ -44,20 +48,22 @@ def _compile(src: str, extra: list) -> str:
     return obj
 
 
-def build(verbose: bool = False, extra: list = None) -> str:
-    os.makedirs(OUT_DIR, exist_ok=True)
-    extra = list(extra or [])
+def build(verbose: bool = False, extra: list = None, checked: bool = False) -> str:
+    out_dir, lib = (OUT_DIR_CHECK, LIB_CHECK) if checked else (OUT_DIR, LIB)
+    os.makedirs(out_dir, exist_ok=True)
+    extra = list(extra or []) + (["-DSPHX_CHECK"] if checked else [])
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra), SOURCES))
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs
+        objs = list(ex.map(lambda s: _compile(s, extra, out_dir), SOURCES))
+    if not os.path.exists(lib) or os.path.getmtime(lib) < max(os.path.getmtime(o) for o in objs):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", lib] + objs
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     if verbose:
-        print(LIB)
-    return LIB
+        print(lib)
+    return lib
 
 
 if __name__ == "__main__":
-    build(verbose=True, extra=sys.argv[1:])
+    args = sys.argv[1:]
+    build(verbose=True, extra=[a for a in args if a != "--checked"], checked="--checked" in args)

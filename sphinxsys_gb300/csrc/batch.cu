@@ -515,6 +515,7 @@ int b_alloc_lists(sphx_batch bt, MPNeighbors &l, unsigned cap)
     if (!l.J)
         return fail(SPHX_ERR_OUT_OF_MEMORY, "batch neighbour list allocation failed (%u slots)", cap);
     l.cap = cap;
+    l.limit = uint32_t(&l == &bt->wl ? bt->nw : bt->n); // records the entries index
     bt->invalidate_graphs(); // the graphs hold the old list pointer
     return SPHX_OK;
 }

@@ -149,8 +149,11 @@ __global__ void k_scatter(size_t n, const uint32_t *__restrict__ cell_of, const 
                           const uint32_t *__restrict__ offset, uint32_t *__restrict__ particle_index)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i < n)
-        particle_index[offset[cell_of[i]] + rank[i]] = uint32_t(i);
+    if (i >= n)
+        return;
+    const uint32_t slot = offset[cell_of[i]] + rank[i];
+    if (SPHX_CHECKED(slot < n, kCheckCellRange, slot))
+        particle_index[slot] = uint32_t(i);
 }
 
 // Puts each cell's particles in ascending index order (insertion sort of a short segment).

@@ -89,7 +89,14 @@ struct Lists
     const uint32_t *count, *J;
     size_t n_src;
     unsigned cap;
+    uint32_t limit; // target particles the entries index (tested by the checked build)
 };
+
+// Entry j indexes a target particle (always true unless built with SPHX_CHECK).
+__device__ __forceinline__ bool entry_ok(const Lists &l, uint32_t j)
+{
+    return SPHX_CHECKED(j < l.limit, kCheckListEntry, j);
+}
 
 Lists lists_of(sphx_relation r)
 {
@@ -100,6 +107,7 @@ Lists lists_of(sphx_relation r)
     l.J = r->j;
     l.n_src = r->n_src;
     l.cap = unsigned(r->cap);
+    l.limit = uint32_t(r->tgt ? r->tgt->n : 0);
     return l;
 }
 
@@ -195,6 +203,8 @@ __device__ __forceinline__ void ck_summation(size_t n, const CKFluid &f, const C
     for (unsigned s = 0; s < c; ++s)
     {
         uint32_t j = in.J[size_t(s) * n + i];
+        if (!entry_ok(in, j))
+            continue;
         double len = geometry<D>(f.pos, n, i, f.pos, n, j, r, e);
         sum += tW(t, len) * f.Vol_ref[j];
     }
@@ -204,6 +214,8 @@ __device__ __forceinline__ void ck_summation(size_t n, const CKFluid &f, const C
         for (unsigned s = 0; s < c; ++s)
         {
             uint32_t j = wl.J[size_t(s) * n + i];
+            if (!entry_ok(wl, j))
+                continue;
             double len = geometry<D>(f.pos, n, i, w.pos, w.nw, j, r, e);
             sum += tW(t, len) * w.Vol_ref[j];
         }
@@ -314,6 +326,8 @@ __global__ void k_ck_correction(size_t n, CKFluid f, CKWall w, Lists in, Lists w
     for (unsigned s = 0; s < c; ++s)
     {
         uint32_t j = in.J[size_t(s) * n + i];
+        if (!entry_ok(in, j))
+            continue;
         add(geometry<D>(f.pos, n, i, f.pos, n, j, r, e), f.Vol[j]);
     }
     if (wl.J)
@@ -322,6 +336,8 @@ __global__ void k_ck_correction(size_t n, CKFluid f, CKWall w, Lists in, Lists w
         for (unsigned s = 0; s < c; ++s)
         {
             uint32_t j = wl.J[size_t(s) * n + i];
+            if (!entry_ok(wl, j))
+                continue;
             add(geometry<D>(f.pos, n, i, w.pos, w.nw, j, r, e), w.Vol[j]);
         }
     }
@@ -378,6 +394,8 @@ __global__ void __launch_bounds__(kBlock) k_ck_interact1(size_t n, CKFluid f, CK
     for (unsigned s = 0; s < c; ++s)
     {
         uint32_t j = in.J[size_t(s) * n + i];
+        if (!entry_ok(in, j))
+            continue;
         double len = geometry<D>(f.pos, n, i, f.pos, n, j, r, e);
         double dWV = tdW(t, len) * f.Vol[j];
         matvec<D>(f.B, n, j, e, bj);
@@ -399,6 +417,8 @@ __global__ void __launch_bounds__(kBlock) k_ck_interact1(size_t n, CKFluid f, CK
         for (unsigned s = 0; s < c; ++s)
         {
             uint32_t j = wl.J[size_t(s) * n + i];
+            if (!entry_ok(wl, j))
+                continue;
             double len = geometry<D>(f.pos, n, i, w.pos, w.nw, j, r, e);
             double dWV = tdW(t, len) * w.Vol[j];
             double acc[3];
@@ -440,6 +460,8 @@ __global__ void __launch_bounds__(kBlock) k_ck_second(size_t n, CKFluid f, CKWal
     for (unsigned s = 0; s < c; ++s)
     {
         uint32_t j = in.J[size_t(s) * n + i];
+        if (!entry_ok(in, j))
+            continue;
         double len = geometry<D>(f.pos, n, i, f.pos, n, j, r, e);
         double dWV = tdW(t, len) * f.Vol[j];
         matvec<D>(f.B, n, i, e, be);
@@ -468,6 +490,8 @@ __global__ void __launch_bounds__(kBlock) k_ck_second(size_t n, CKFluid f, CKWal
         for (unsigned s = 0; s < c; ++s)
         {
             uint32_t j = wl.J[size_t(s) * n + i];
+            if (!entry_ok(wl, j))
+                continue;
             double len = geometry<D>(f.pos, n, i, w.pos, w.nw, j, r, e);
             double dWV = tdW(t, len) * w.Vol[j];
             double vel_diff[3], nj[3];
@@ -530,6 +554,8 @@ __global__ void k_ck_indication_inner(size_t n, CKFluid f, Lists in, TabK t, con
     for (unsigned s = 0; s < c; ++s)
     {
         uint32_t j = in.J[size_t(s) * n + i];
+        if (!entry_ok(in, j))
+            continue;
         double len = geometry<D>(f.pos, n, i, f.pos, n, j, r, e);
         pd -= tdW(t, len) * f.Vol[j] * len;
     }
@@ -555,6 +581,8 @@ __global__ void k_ck_indication_contact(size_t n, CKFluid f, CKWall w, Lists wl,
     for (unsigned s = 0; s < c; ++s)
     {
         uint32_t j = wl.J[size_t(s) * n + i];
+        if (!entry_ok(wl, j))
+            continue;
         double len = geometry<D>(f.pos, n, i, w.pos, w.nw, j, r, e);
         pd -= tdW(t, len) * w.Vol[j] * len;
     }
@@ -577,6 +605,8 @@ __global__ void k_ck_indication_update(size_t n, CKFluid f, Lists in, const doub
         for (unsigned s = 0; s < c && !very_near; ++s)
         {
             uint32_t j = in.J[size_t(s) * n + i];
+            if (!entry_ok(in, j))
+                continue;
             double len = geometry<D>(f.pos, n, i, f.pos, n, j, r, e);
             very_near = pos_div[j] < thr && len < h;
         }

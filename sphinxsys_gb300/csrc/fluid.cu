@@ -54,7 +54,14 @@ struct Neighbors
     const double *DW, *E, *R;
     size_t stride; // cap * n_src
     unsigned cap;  // slots per particle; loops never read past it
+    uint32_t limit; // target particles the entries index (tested by the checked build)
 };
+
+// Entry j indexes a target particle (always true unless built with SPHX_CHECK).
+__device__ __forceinline__ bool entry_ok(const Neighbors &nb, uint32_t j)
+{
+    return SPHX_CHECKED(j < nb.limit, kCheckListEntry, j);
+}
 
 Neighbors neighbors_of(sphx_relation r)
 {
@@ -66,6 +73,7 @@ Neighbors neighbors_of(sphx_relation r)
     nb.R = r->r;
     nb.stride = size_t(r->cap) * r->n_src;
     nb.cap = unsigned(r->cap);
+    nb.limit = uint32_t(r->tgt ? r->tgt->n : 0);
     return nb;
 }
 
@@ -128,6 +136,8 @@ __global__ void __launch_bounds__(kBlock)
     {
         size_t slot = size_t(s) * n + i;
         uint32_t j = in.J[slot];
+        if (!entry_ok(in, j))
+            continue;
         double dWV = in.DW[slot] * f.Vol[j];
         double p_j = f.p[j];
         double sc = (p_i + p_j) * dWV;
@@ -154,6 +164,8 @@ __global__ void __launch_bounds__(kBlock)
         {
             size_t slot = size_t(s) * n + i;
             uint32_t j = wn.J[slot];
+            if (!entry_ok(wn, j))
+                continue;
             double dWV = wn.DW[slot] * w.Vol[j];
             double r_ij = wn.R[slot];
             double e[3];
@@ -207,6 +219,8 @@ __global__ void __launch_bounds__(kBlock)
     {
         size_t slot = size_t(s) * n + i;
         uint32_t j = in.J[slot];
+        if (!entry_ok(in, j))
+            continue;
         double dWV = in.DW[slot] * f.Vol[j];
         double e[3];
         double u_jump = 0;
@@ -236,6 +250,8 @@ __global__ void __launch_bounds__(kBlock)
         {
             size_t slot = size_t(s) * n + i;
             uint32_t j = wn.J[slot];
+            if (!entry_ok(wn, j))
+                continue;
             double dWV = wn.DW[slot] * w.Vol[j];
             double e[3], nj[3], va[3];
             double en = 0;
@@ -363,7 +379,7 @@ __global__ void k_gravity(size_t n, int dim, const double *__restrict__ mass, do
 }
 
 // Interpolation at observer points: one warp per observer, fixed-order combine.
-__global__ void k_observe(size_t n_obs, unsigned cap, const uint32_t *__restrict__ count, const uint32_t *__restrict__ J,
+__global__ void k_observe(size_t n_obs, size_t n_tgt, unsigned cap, const uint32_t *__restrict__ count, const uint32_t *__restrict__ J,
                           const double *__restrict__ W, const double *__restrict__ Vol, const double *__restrict__ q,
                           double *__restrict__ out)
 {
@@ -375,8 +391,11 @@ __global__ void k_observe(size_t n_obs, unsigned cap, const uint32_t *__restrict
     for (unsigned s = 0; s < cnt; ++s)
     {
         size_t slot = size_t(s) * n_obs + i;
-        double w = W[slot] * Vol[J[slot]];
-        num += w * q[J[slot]];
+        const uint32_t j = J[slot];
+        if (!SPHX_CHECKED(j < n_tgt, kCheckListEntry, j))
+            continue;
+        double w = W[slot] * Vol[j];
+        num += w * q[j];
         ttl += w;
     }
     out[i] = num / (ttl + kTinyReal);
@@ -533,6 +552,8 @@ __global__ void __launch_bounds__(kBlock) k_viscous_inner(size_t n, Neighbors in
     {
         size_t slot = size_t(s) * n + i;
         uint32_t j = in.J[slot];
+        if (!entry_ok(in, j))
+            continue;
         double e[3] = {0, 0, 0};
 #pragma unroll
         for (int a = 0; a < D; ++a)
@@ -578,6 +599,8 @@ __global__ void __launch_bounds__(kBlock) k_tvc_inner(size_t n, Neighbors in, co
     {
         size_t slot = size_t(s) * n + i;
         uint32_t j = in.J[slot];
+        if (!entry_ok(in, j))
+            continue;
         double w = (1.0 + 1.0) * in.DW[slot] * Vol[j];
 #pragma unroll
         for (int a = 0; a < D; ++a)
@@ -765,7 +788,7 @@ extern "C" int sphx_observe_quantity(sphx_relation rel, const char *name, double
     sphx_ctx ctx = rel->ctx;
     SPHX_TRY(ctx->ensure_scratch(n * sizeof(double)));
     double *d_out = static_cast<double *>(ctx->d_scratch);
-    k_observe<<<unsigned(n), 32, 0, ctx->stream>>>(n, unsigned(rel->cap), rel->count, rel->j, rel->W,
+    k_observe<<<unsigned(n), 32, 0, ctx->stream>>>(n, tgt->n, unsigned(rel->cap), rel->count, rel->j, rel->W,
                                                    static_cast<const double *>(Vol->dev),
                                                    static_cast<const double *>(q->dev), d_out);
     SPHX_LAUNCHED(ctx);

@@ -408,6 +408,8 @@ __global__ void __launch_bounds__(256) k_mp_first_tiled(size_t n, MPConst k, MPF
         sw.wa = wa;
         sw.wb = wb;
         __syncthreads();
+        in.limit = t.total[0]; // the entries index the staged records
+        wl.limit = t.total[1];
         const uint32_t tile = g.tiles[blockIdx.x];
         const uint32_t te = g.tile_offset[tile + 1];
         for (uint32_t q = g.tile_offset[tile] + threadIdx.x; q < te; q += blockDim.x)
@@ -456,6 +458,8 @@ __global__ void __launch_bounds__(256) k_mp_second_tiled(size_t n, MPConst k, MP
         sw.wb = wb;
         sw.wc = wc;
         __syncthreads();
+        in.limit = t.total[0];
+        wl.limit = t.total[1];
         const uint32_t tile = g.tiles[blockIdx.x];
         const uint32_t te = g.tile_offset[tile + 1];
         for (uint32_t q = g.tile_offset[tile] + threadIdx.x; q < te; q += blockDim.x)
@@ -1060,6 +1064,8 @@ int alloc_lists(sphx_mp mp, MPLists &l, unsigned cap)
     if (!l.J)
         return fail(SPHX_ERR_OUT_OF_MEMORY, "neighbour list allocation failed (%u slots)", cap);
     l.cap = cap;
+    l.limit = uint32_t(&l == &mp->wl ? mp->nw : mp->n); // records the entries index
+    l.mask = mp->k.periodic ? kIndexMask : 0xffffffffu;
     return SPHX_OK;
 }
 

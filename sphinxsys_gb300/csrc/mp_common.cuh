@@ -267,7 +267,15 @@ struct MPNeighbors
 {
     uint32_t *count, *J; // slot-major: slot s of particle i at J[s * n + i]
     unsigned cap;
+    uint32_t limit = 0xffffffffu; // records the entries index (tested by the checked build)
+    uint32_t mask = 0xffffffffu;  // index bits of an entry (periodic entries carry image codes)
 };
+
+// Entry e of list l indexes one of its records (always true unless built with SPHX_CHECK).
+__device__ __forceinline__ bool entry_ok(uint32_t e, const MPNeighbors &l)
+{
+    return SPHX_CHECKED((e & l.mask) < l.limit, kCheckListEntry, e);
+}
 
 struct Kahan
 {
@@ -400,6 +408,26 @@ __device__ __forceinline__ void axis_reach(float o, float inv_gs, float r, int &
     lo = max(0, min(kReach, int(ceilf((r - o) * inv_gs))));
 }
 
+// Sub-cell c inside the mesh, and its indices packed 16 bits per axis (for the check record).
+template <int D>
+__device__ __forceinline__ bool cell_in_mesh(const MeshDev &m, const int *c)
+{
+    bool in = true;
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+        in = in && c[a] >= 0 && c[a] < m.all_cells[a];
+    return in;
+}
+template <int D>
+__device__ __forceinline__ uint64_t packed_cell(const int *c)
+{
+    uint64_t p = 0;
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+        p |= uint64_t(uint16_t(c[a])) << (16 * a);
+    return p;
+}
+
 // Candidate runs of the pruned (2 kReach + 1)^D window around sub-cell c: run(x, y, b, e)
 // for every column (x, y) of the window (x alone in 2D) with the candidate particles
 // [b, e) of its cells along the last axis; the cells of one instance start at cell_base
@@ -408,6 +436,13 @@ template <int D, bool PRUNE, class R>
 __device__ __forceinline__ void for_each_candidate_run(const MeshDev &m, uint32_t cell_base, const uint32_t *offset,
                                                        const int *c, const Reach &q, R &&run)
 {
+    // checked builds: the sub-cell lies in the mesh and every range is ordered
+    if (!SPHX_CHECKED(cell_in_mesh<D>(m, c), kCheckCellIndex, packed_cell<D>(c)))
+        return;
+    auto span = [&](int x, int y, uint32_t b, uint32_t e) {
+        if (SPHX_CHECKED(b <= e, kCheckCellRange, (uint64_t(b) << 32) | e))
+            run(x, y, b, e);
+    };
     if (!PRUNE)
     {
         const int lo0 = max(c[0] - kReach, 0), hi0 = min(c[0] + kReach, m.all_cells[0] - 1);
@@ -417,7 +452,7 @@ __device__ __forceinline__ void for_each_candidate_run(const MeshDev &m, uint32_
             for (int x = lo0; x <= hi0; ++x)
             {
                 uint32_t a = cell_base + uint32_t(x) * uint32_t(m.all_cells[1]);
-                run(x, 0, offset[a + uint32_t(lo1)], offset[a + uint32_t(hi1) + 1]);
+                span(x, 0, offset[a + uint32_t(lo1)], offset[a + uint32_t(hi1) + 1]);
             }
         }
         else
@@ -428,7 +463,7 @@ __device__ __forceinline__ void for_each_candidate_run(const MeshDev &m, uint32_
                 {
                     uint32_t a = cell_base +
                                  (uint32_t(x) * uint32_t(m.all_cells[1]) + uint32_t(y)) * uint32_t(m.all_cells[2]);
-                    run(x, y, offset[a + uint32_t(lo2)], offset[a + uint32_t(hi2) + 1]);
+                    span(x, y, offset[a + uint32_t(lo2)], offset[a + uint32_t(hi2) + 1]);
                 }
         }
         return;
@@ -446,7 +481,7 @@ __device__ __forceinline__ void for_each_candidate_run(const MeshDev &m, uint32_
             axis_reach(q.o[1], q.inv_gs, sqrtf(fmaxf(r2 - gx * gx, 0.0f)), l1, h1);
             const int lo1 = max(c[1] - l1, 0), hi1 = min(c[1] + h1, m.all_cells[1] - 1);
             uint32_t a = cell_base + uint32_t(x) * uint32_t(m.all_cells[1]);
-            run(x, 0, offset[a + uint32_t(lo1)], offset[a + uint32_t(hi1) + 1]);
+            span(x, 0, offset[a + uint32_t(lo1)], offset[a + uint32_t(hi1) + 1]);
         }
     }
     else
@@ -468,7 +503,7 @@ __device__ __forceinline__ void for_each_candidate_run(const MeshDev &m, uint32_
                 const int lo2 = max(c[2] - l2, 0), hi2 = min(c[2] + h2, m.all_cells[2] - 1);
                 uint32_t a = cell_base +
                              (uint32_t(x) * uint32_t(m.all_cells[1]) + uint32_t(y)) * uint32_t(m.all_cells[2]);
-                run(x, y, offset[a + uint32_t(lo2)], offset[a + uint32_t(hi2) + 1]);
+                span(x, y, offset[a + uint32_t(lo2)], offset[a + uint32_t(hi2) + 1]);
             }
         }
     }
@@ -567,17 +602,26 @@ __device__ __forceinline__ void list_sweep(size_t i, size_t n, const MPNeighbors
                     jj[u] = __ldg(&J[size_t(s + h + u) * stride]);
             }
             decltype(load(0u)) rec[U];
+            bool ok[U];
 #pragma unroll
             for (int u = 0; u < U; ++u)
-                rec[u] = load(jj[u]);
+                ok[u] = entry_ok(jj[u], l);
 #pragma unroll
             for (int u = 0; u < U; ++u)
-                pair(rec[u]);
+                rec[u] = ok[u] ? load(jj[u]) : decltype(load(0u)){};
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (ok[u])
+                    pair(rec[u]);
         }
         flush();
     }
     for (; s < c; ++s)
-        pair(load(__ldg(&J[size_t(s) * stride])));
+    {
+        const uint32_t j = __ldg(&J[size_t(s) * stride]);
+        if (entry_ok(j, l))
+            pair(load(j));
+    }
     flush();
 }
 
@@ -627,11 +671,16 @@ __device__ __forceinline__ void list_sweep_async(size_t i, size_t n, const MPNei
 {
     const unsigned c = min(l.count[i], l.cap);
     const uint32_t *J = l.J + i;
+    // a bad entry (checked builds) is not copied: its pair reads the slot's stale record
+    auto issue_entry = [&](uint32_t j, unsigned slot) {
+        if (entry_ok(j, l))
+            issue(j, slot);
+    };
 #pragma unroll
     for (int u = 0; u < DEPTH; ++u)
     {
         if (unsigned(u) < c)
-            issue(__ldg(&J[size_t(u) * n]), unsigned(u));
+            issue_entry(__ldg(&J[size_t(u) * n]), unsigned(u));
         if (unsigned(u + DEPTH) < c)
             cp_async4(&ring.idx[ring.at(u)], &J[size_t(u + DEPTH) * n]);
         cp_async_commit();
@@ -645,7 +694,7 @@ __device__ __forceinline__ void list_sweep_async(size_t i, size_t n, const MPNei
         const unsigned nx = s + DEPTH;
         if (nx < c)
         {
-            issue(ring.idx[ring.at(slot)], slot);
+            issue_entry(ring.idx[ring.at(slot)], slot);
             if (nx + DEPTH < c)
                 cp_async4(&ring.idx[ring.at(slot)], &J[size_t(nx + DEPTH) * n]);
         }

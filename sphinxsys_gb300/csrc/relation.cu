@@ -88,6 +88,8 @@ __global__ void __launch_bounds__(kBlock) k_build(BuildArgs a)
                 float o2 = D == 3 ? float(xi[2] - cell_corner(a.m, 2, cc[2])) : 0.0f;
                 uint32_t lc = linear_cell<D>(a.m, cc);
                 uint32_t kb = a.cell_offset[lc], ke = a.cell_offset[lc + 1];
+                if (!SPHX_CHECKED(kb <= ke && ke <= a.n_tgt, kCheckCellRange, (uint64_t(kb) << 32) | ke))
+                    ke = kb;
                 for (uint32_t kk = kb; kk < ke; ++kk)
                 {
                     float f0 = o0 - a.soff[kk], f1 = o1 - a.soff[a.n_tgt + kk];
@@ -117,6 +119,8 @@ __global__ void __launch_bounds__(kBlock) k_build(BuildArgs a)
     for (unsigned s = 0; s < stored; ++s)
     {
         const uint32_t kk = a.J[size_t(s) * a.n_src + i];
+        if (!SPHX_CHECKED(kk < a.n_tgt && a.pidx[kk] < a.n_tgt, kCheckListEntry, kk))
+            continue;
         double dx[3] = {0, 0, 0};
 #pragma unroll
         for (int d = 0; d < D; ++d)

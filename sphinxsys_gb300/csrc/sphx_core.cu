@@ -109,6 +109,53 @@ int sphx_body_s::need(const char *name, sphx_dtype dtype, int nc, Field **out)
 extern "C" const char *sphx_last_error(void) { return g_err; }
 extern "C" const char *sphx_version(void) { return "sphx-gb300 0.1 (sm_103a)"; }
 
+namespace sphx
+{
+static std::vector<CheckReader> &check_readers()
+{
+    static std::vector<CheckReader> readers;
+    return readers;
+}
+
+int check_register(CheckReader reader)
+{
+    check_readers().push_back(reader);
+    return int(check_readers().size());
+}
+} // namespace sphx
+
+extern "C" int sphx_checked_build(void)
+{
+#ifdef SPHX_CHECK
+    return 1;
+#else
+    return 0;
+#endif
+}
+
+extern "C" int sphx_check_violations(uint64_t *count, uint64_t *first, int reset)
+{
+    SPHX_CUDA(cudaDeviceSynchronize());
+    unsigned long long total = 0, first_seen = 0;
+    for (CheckReader read : check_readers())
+    {
+        unsigned long long c = 0, f = 0;
+        if (read(&c, &f, reset != 0) != 0)
+            return fail(SPHX_ERR_CUDA, "reading the bounds-check record failed");
+        if (c && !total)
+            first_seen = f;
+        total += c;
+    }
+    if (count)
+        *count = total;
+    if (first)
+        *first = first_seen;
+    if (total)
+        return fail(SPHX_ERR_BOUNDS, "%llu failed index tests; first: site %llu, value %llu", total,
+                    first_seen >> 48, first_seen & 0xffffffffffffull);
+    return SPHX_OK;
+}
+
 extern "C" int sphx_ctx_create(int device, void *stream, sphx_ctx *out)
 {
     if (!out)

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/sphx/sphx.h"
+#include "sphx_check.cuh"
 
 namespace sphx
 {

@@ -1,7 +1,8 @@
 """ctypes binding of libsphx_cuda.so (the C ABI declared in include/sphx/sphx.h).
 
 The library is built in-tree by sphinxsys_gb300/build.py.  Loading fails loudly when it
-is missing: there is no CPU fallback.
+is missing: there is no CPU fallback.  With SPHX_CHECKED_BUILD=1 in the environment the
+bounds-checked build (build.py --checked) is loaded instead.
 """
 from __future__ import annotations
 
@@ -13,7 +14,8 @@ from . import build as _build
 
 SPHX_OK = 0
 ERRORS = {1: "SPHX_ERR_INVALID_ARG", 2: "SPHX_ERR_CUDA", 3: "SPHX_ERR_CAPACITY", 4: "SPHX_ERR_OUT_OF_MEMORY",
-          5: "SPHX_ERR_NOT_FOUND", 6: "SPHX_ERR_TIMEOUT", 7: "SPHX_ERR_NUMERIC", 8: "SPHX_ERR_NO_DEVICE"}
+          5: "SPHX_ERR_NOT_FOUND", 6: "SPHX_ERR_TIMEOUT", 7: "SPHX_ERR_NUMERIC", 8: "SPHX_ERR_NO_DEVICE",
+          9: "SPHX_ERR_BOUNDS"}
 F64, U32, F32, I32 = 0, 1, 2, 3
 
 
@@ -41,6 +43,8 @@ _pvp = C.POINTER(C.c_void_p)
 SIGNATURES = {
     "sphx_last_error": (C.c_char_p, []),
     "sphx_version": (C.c_char_p, []),
+    "sphx_checked_build": (C.c_int, []),
+    "sphx_check_violations": (C.c_int, [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.c_int]),
     "sphx_ctx_create": (_i, [_i, _vp, _pvp]),
     "sphx_ctx_destroy": (_i, [_vp]),
     "sphx_ctx_synchronize": (_i, [_vp]),
@@ -131,8 +135,12 @@ SIGNATURES = {
 _lib: Optional[C.CDLL] = None
 
 
+def checked_requested() -> bool:
+    return os.environ.get("SPHX_CHECKED_BUILD", "0") not in ("", "0")
+
+
 def library_path() -> str:
-    return _build.LIB
+    return _build.LIB_CHECK if checked_requested() else _build.LIB
 
 
 def load(build_if_missing: bool = False) -> C.CDLL:
@@ -140,12 +148,12 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     global _lib
     if _lib is not None:
         return _lib
-    path = _build.LIB
+    path = library_path()
     if not os.path.exists(path):
         if not build_if_missing:
             raise RuntimeError(f"{path} is missing: build it with sphinxsys_gb300/build.py "
                                "(there is no CPU fallback)")
-        _build.build()
+        _build.build(checked=checked_requested())
     lib = C.CDLL(path)
     for name, (res, args) in SIGNATURES.items():
         fn = getattr(lib, name)
@@ -163,3 +171,13 @@ def check(status: int) -> None:
 
 def call(name: str, *args) -> None:
     check(getattr(load(), name)(*args))
+
+
+def check_violations(reset: bool = True) -> tuple:
+    """(count, site, value) of the bounds-checked build's failed index tests since the last
+    reset, the site and value of the first one (count 0 in other builds); synchronises."""
+    c, f = C.c_uint64(), C.c_uint64()
+    st = load().sphx_check_violations(C.byref(c), C.byref(f), int(reset))
+    if st not in (SPHX_OK, 9):
+        check(st)
+    return c.value, f.value >> 48, f.value & ((1 << 48) - 1)

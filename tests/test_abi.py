@@ -46,3 +46,15 @@ def test_errors_are_returned_not_fatal():
     st = lib.sphx_mesh_from_bounds(4, None, None, 0.1, 2, None)
     assert st == 1
     assert b"invalid" in lib.sphx_last_error()
+
+
+def test_checked_build_builds_and_reports_itself():
+    """The bounds-checked build (-DSPHX_CHECK) compiles, exports the same entry points and
+    reports itself; the default build does not."""
+    path = build.build(checked=True)
+    assert path != build.LIB
+    lib = ctypes.CDLL(path)
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+    assert lib.sphx_checked_build() == 1
+    assert native.load().sphx_checked_build() == 0

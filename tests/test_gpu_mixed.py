@@ -226,11 +226,14 @@ def test_host_rows_load_and_store_like_the_body_path(case):
 
 
 def test_autotune_keeps_state():
+    """The autotuner restores the state it advanced (whichever of the strategies 0-6 it
+    keeps: on this 3,200-particle case the lane-split ones can win, their extra lanes
+    filling more of the GPU)."""
     case = cases.dambreak_2d()
     a = MixedPrecisionDamBreak(case)
     b = MixedPrecisionDamBreak(case)
     block, strategy, ms = b.autotune(reps=1)
-    assert block in (64, 128, 256) and strategy in (0, 1) and ms > 0
+    assert block in (64, 128, 256) and strategy in range(7) and ms > 0
     b.set_tuning(128, 0)
     for _ in range(3):
         a.advection_step()
