@@ -156,24 +156,12 @@ __global__ void k_scatter(size_t n, const uint32_t *__restrict__ cell_of, const 
         particle_index[slot] = uint32_t(i);
 }
 
-// Puts each cell's particles in ascending index order (insertion sort of a short segment).
+// Puts each cell's particles in ascending index order.
 __global__ void k_sort_segments(size_t nseg, const uint32_t *__restrict__ offset, uint32_t *__restrict__ idx)
 {
     size_t c = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (c >= nseg)
-        return;
-    uint32_t b = offset[c], e = offset[c + 1];
-    for (uint32_t k = b + 1; k < e; ++k)
-    {
-        uint32_t v = idx[k];
-        uint32_t m = k;
-        while (m > b && idx[m - 1] > v)
-        {
-            idx[m] = idx[m - 1];
-            --m;
-        }
-        idx[m] = v;
-    }
+    if (c < nseg)
+        sort_segment(idx, offset[c], offset[c + 1]);
 }
 
 // Cell-ordered copies of the positions: exact FP64 and the FP32 offset from the lower

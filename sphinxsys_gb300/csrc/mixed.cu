@@ -144,20 +144,8 @@ __global__ void k_mp_scatter(size_t n, const uint32_t *__restrict__ key, const u
 __global__ void k_mp_sort_segments(size_t nseg, const uint32_t *__restrict__ offset, uint32_t *__restrict__ idx)
 {
     size_t c = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (c >= nseg)
-        return;
-    uint32_t b = offset[c], e = offset[c + 1];
-    for (uint32_t k = b + 1; k < e; ++k)
-    {
-        uint32_t v = idx[k];
-        uint32_t q = k;
-        while (q > b && idx[q - 1] > v)
-        {
-            idx[q] = idx[q - 1];
-            --q;
-        }
-        idx[q] = v;
-    }
+    if (c < nseg)
+        sort_segment(idx, offset[c], offset[c + 1]);
 }
 
 __global__ void k_mp_set_total(uint32_t *offset, size_t ncells, uint32_t total) { offset[ncells] = total; }

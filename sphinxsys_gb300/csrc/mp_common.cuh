@@ -1016,8 +1016,8 @@ __device__ __forceinline__ void build_particle(size_t i, size_t n, const MPParam
     });
     in.count[i] = cnt;
     wl.count[i] = wc;
-    atomicMax(&max_counts[0], cnt);
-    atomicMax(&max_counts[1], wc);
+    warp_atomic_max(&max_counts[0], cnt);
+    warp_atomic_max(&max_counts[1], wc);
     // rho_sum - rho0 = rho0 (W0 + sum W - sigma0) / sigma0 + wall term
     double dsig = (double(sigma.s) - k.sigma0) - double(sigma.c) + double(k.fW);
     f.drho_sum[i] = float(dsig) * k.rho0_over_sigma0 + wsig.value() * k.wall_factor;
@@ -1308,7 +1308,7 @@ __device__ __forceinline__ void build_particle_periodic(size_t i, size_t n, cons
         ++cnt;
     });
     in.count[i] = cnt;
-    atomicMax(&max_counts[0], cnt);
+    warp_atomic_max(&max_counts[0], cnt);
     // Two phases: the candidate loop above only tests and stores (the lanes of a warp
     // accept different candidates, and a warp runs the accepting branch whenever any lane
     // takes it); each lane now runs the kernel sums over its own stored entries, in the

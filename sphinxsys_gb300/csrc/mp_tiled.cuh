@@ -260,8 +260,8 @@ __device__ __forceinline__ void build_particle_tiled(size_t t, size_t i, size_t 
                                      });
     in.count[t] = cnt;
     wl.count[t] = wcnt;
-    atomicMax(&max_counts[0], cnt);
-    atomicMax(&max_counts[1], wcnt);
+    warp_atomic_max(&max_counts[0], cnt);
+    warp_atomic_max(&max_counts[1], wcnt);
     double dsig = (double(sigma.s) - k.sigma0) - double(sigma.c) + double(k.fW);
     f.drho_sum[i] = float(dsig) * k.rho0_over_sigma0 + wsig.value() * k.wall_factor;
 }

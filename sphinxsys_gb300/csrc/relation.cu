@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(kBlock) k_build(BuildArgs a)
     }
     a.count[i] = cnt;
     a.wsum[i] = ws;
-    atomicMax(a.max_count, cand);
+    warp_atomic_max(a.max_count, cand);
 }
 } // namespace
 

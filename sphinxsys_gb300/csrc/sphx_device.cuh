@@ -85,4 +85,69 @@ __host__ __device__ __forceinline__ double from_ordered_bits(unsigned long long 
     memcpy(&d, &r, sizeof(d));
     return d;
 }
+
+// atomicMax of v over the lanes that reach this call together: one atomic per group of
+// converged lanes instead of one per lane on a single contended address.
+__device__ __forceinline__ void warp_atomic_max(unsigned int *addr, unsigned int v)
+{
+    const unsigned mask = __activemask();
+    const unsigned m = __reduce_max_sync(mask, v);
+    if ((threadIdx.x & 31u) == unsigned(__ffs(mask) - 1))
+        atomicMax(addr, m);
+}
+
+// Sorts the len distinct entries idx[b, b + len) held in R registers: all loads issued
+// before any compare (one memory latency), R rounds of odd-even transposition, stores.
+template <int R>
+__device__ __forceinline__ void sort_in_registers(uint32_t *idx, uint32_t b, uint32_t len)
+{
+    uint32_t v[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q)
+        v[q] = uint32_t(q) < len ? idx[b + q] : 0xffffffffu;
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+    {
+#pragma unroll
+        for (int q = r & 1; q + 1 < R; q += 2)
+        {
+            const uint32_t lo = min(v[q], v[q + 1]), hi = max(v[q], v[q + 1]);
+            v[q] = lo;
+            v[q + 1] = hi;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < R; ++q)
+        if (uint32_t(q) < len)
+            idx[b + q] = v[q];
+}
+
+// Puts the entries of one cell segment idx[b, e) (distinct particle indices, in the order
+// of the atomic ranks) in ascending order, so the cell order does not depend on the order
+// in which the atomics ran.  Segments of up to 16 entries are sorted in registers; an
+// insertion sort in memory, whose dependent loads cost a latency each, takes the rest.
+__device__ __forceinline__ void sort_segment(uint32_t *idx, uint32_t b, uint32_t e)
+{
+    const uint32_t len = e - b;
+    if (len < 2)
+        return;
+    if (len <= 4)
+        sort_in_registers<4>(idx, b, len);
+    else if (len <= 8)
+        sort_in_registers<8>(idx, b, len);
+    else if (len <= 16)
+        sort_in_registers<16>(idx, b, len);
+    else
+        for (uint32_t k = b + 1; k < e; ++k)
+        {
+            const uint32_t v = idx[k];
+            uint32_t q = k;
+            while (q > b && idx[q - 1] > v)
+            {
+                idx[q] = idx[q - 1];
+                --q;
+            }
+            idx[q] = v;
+        }
+}
 } // namespace sphx
