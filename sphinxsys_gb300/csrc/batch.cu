@@ -272,7 +272,7 @@ __global__ void k_b_begin(int count, const BInst *__restrict__ inst, BRun *run)
 // ---------------------------------------------------------------- acoustic sub-step
 __global__ void k_b_init1(size_t n, const uint32_t *__restrict__ starts, int count,
                           const BInst *__restrict__ inst, const BRun *__restrict__ run, float *__restrict__ drho,
-                          const float *__restrict__ drho_dt, float4 *__restrict__ dyn)
+                          const float *__restrict__ drho_dt, float4 *__restrict__ dyn, float *__restrict__ pres)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -282,7 +282,9 @@ __global__ void k_b_init1(size_t n, const uint32_t *__restrict__ starts, int cou
         return;
     float r = drho[i] + drho_dt[i] * float(0.5 * run[b].dt);
     drho[i] = r;
-    reinterpret_cast<float *>(dyn)[4 * i + 3] = inst[b].p.p0_over_rho0 * r;
+    const float p = inst[b].p.p0_over_rho0 * r;
+    reinterpret_cast<float *>(dyn)[4 * i + 3] = p;
+    pres[i] = p;
 }
 
 // at most 64 registers: 4 blocks of 256 threads per SM
@@ -485,8 +487,10 @@ int b_alloc_state(sphx_batch bt, MPState &s)
     s.drho = bt->alloc<float>(n);
     s.drho_dt = bt->alloc<float>(n);
     s.drho_sum = bt->alloc<float>(n);
+    s.pres = bt->alloc<float>(n);
     s.id = bt->alloc<uint32_t>(n);
-    if (!s.geo0 || !s.dyn || !s.off || !s.off_lo || !s.force || !s.drho || !s.drho_dt || !s.drho_sum || !s.id)
+    if (!s.geo0 || !s.dyn || !s.off || !s.off_lo || !s.force || !s.drho || !s.drho_dt || !s.drho_sum || !s.pres ||
+        !s.id)
         return fail(SPHX_ERR_OUT_OF_MEMORY, "batch state allocation failed");
     return SPHX_OK;
 }
@@ -599,7 +603,7 @@ int b_enqueue_substep(sphx_batch bt, cudaStream_t s, const MPState &cur, int use
     size_t n = bt->n;
     unsigned blk = unsigned(bt->block);
     k_b_init1<<<grid_for(n, 256), 256, 0, s>>>(n, bt->starts, bt->count, bt->inst, bt->run, cur.drho, cur.drho_dt,
-                                               cur.dyn);
+                                               cur.dyn, cur.pres);
     SPHX_CUDA(cudaGetLastError());
     k_b_first<D><<<grid_for(n, blk), blk, 0, s>>>(n, bt->starts, bt->count, bt->inst, bt->run, cur, bt->w, bt->in,
                                                   bt->wl);

@@ -247,14 +247,16 @@ __global__ void k_mp_density(size_t n, const float *__restrict__ drho_sum, float
 
 // ---------------------------------------------------------------- acoustic sub-step
 __global__ void k_mp_init1(size_t n, float *__restrict__ drho, const float *__restrict__ drho_dt,
-                           float4 *__restrict__ dyn, float p0_over_rho0, float half_dt)
+                           float4 *__restrict__ dyn, float *__restrict__ pres, float p0_over_rho0, float half_dt)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
     float r = drho[i] + drho_dt[i] * half_dt;
     drho[i] = r;
-    reinterpret_cast<float *>(dyn)[4 * i + 3] = p0_over_rho0 * r;
+    const float p = p0_over_rho0 * r;
+    reinterpret_cast<float *>(dyn)[4 * i + 3] = p;
+    pres[i] = p;
 }
 
 // at most 64 registers: 4 blocks of 256 threads per SM
@@ -383,7 +385,7 @@ __global__ void __launch_bounds__(256) k_mp_first_tiled(size_t n, MPConst k, MPF
         const Window<D> &win = sw.w;
         for_each_staged<D>(win, t.fbeg, t.fbase, [&](uint32_t j, uint32_t s) {
             const float4 gj = f.geo0[j];
-            fa[s] = make_float4(gj.x, gj.y, gj.z, __ldg(&f.dyn[j].w));
+            fa[s] = make_float4(gj.x, gj.y, gj.z, __ldg(&f.pres[j]));
             fb[s] = window_cell<D>(win, __float_as_uint(gj.w));
         });
         for_each_staged<D>(win, t.wbeg, t.wbase, [&](uint32_t j, uint32_t s) {
@@ -605,8 +607,23 @@ __global__ void k_mp_second_lanes(size_t n, MPConst k, MPFluid f, MPWall w, MPLi
 // Lanes per particle of strategies 5 and 6 (0 for the others).
 inline int strategy_lanes(int strategy) { return strategy == 5 ? 2 : (strategy == 6 ? 4 : 0); }
 
+// Blocks of 256 threads per SM the stored-list / cell sweeps are compiled to fit (the
+// register cap follows: 4 -> 64, 5 -> 48 registers; 0 leaves the 2nd half unbounded, ~64
+// registers): build-time tuning parameters.
+#ifndef SPHX_FIRST_MINB
+#define SPHX_FIRST_MINB 4
+#endif
+#ifndef SPHX_SECOND_MINB
+#define SPHX_SECOND_MINB 0
+#endif
+#if SPHX_SECOND_MINB > 0
+#define SPHX_SECOND_BOUNDS __launch_bounds__(256, SPHX_SECOND_MINB)
+#else
+#define SPHX_SECOND_BOUNDS
+#endif
+
 template <int D, bool LISTS, bool ORDER>
-__global__ void __launch_bounds__(256, 4) k_mp_first(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
+__global__ void __launch_bounds__(256, SPHX_FIRST_MINB) k_mp_first(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
                const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, double dt,
                unsigned long long *ac_slot, const uint32_t *__restrict__ order)
 {
@@ -619,7 +636,7 @@ __global__ void __launch_bounds__(256, 4) k_mp_first(size_t n, MPConst k, MPFlui
 }
 
 template <int D, bool LISTS, bool ORDER>
-__global__ void k_mp_second(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
+__global__ void SPHX_SECOND_BOUNDS k_mp_second(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
                 const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, double dt,
                 unsigned long long *adv_slot, const uint32_t *__restrict__ order)
 {
@@ -1028,8 +1045,10 @@ int alloc_state(sphx_mp mp, MPFluid &s)
     s.drho = mp->alloc<float>(n);
     s.drho_dt = mp->alloc<float>(n);
     s.drho_sum = mp->alloc<float>(n);
+    s.pres = mp->alloc<float>(n);
     s.id = mp->alloc<uint32_t>(n);
-    if (!s.geo0 || !s.dyn || !s.off || !s.off_lo || !s.force || !s.drho || !s.drho_dt || !s.drho_sum || !s.id)
+    if (!s.geo0 || !s.dyn || !s.off || !s.off_lo || !s.force || !s.drho || !s.drho_dt || !s.drho_sum || !s.pres ||
+        !s.id)
         return fail(SPHX_ERR_OUT_OF_MEMORY, "mixed-precision state allocation failed");
     if (mp->k.periodic)
     {
@@ -1410,8 +1429,8 @@ int substep(sphx_mp mp, double dt)
     if (!mp->k.periodic && (mp->strategy == 2) != (mp->lists_strategy == 2))
         SPHX_TRY(launch_build<D>(mp));
     unsigned blk = unsigned(mp->block);
-    k_mp_init1<<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.drho, mp->a.drho_dt, mp->a.dyn, mp->k.p.p0_over_rho0,
-                                                float(0.5 * dt));
+    k_mp_init1<<<grid_for(n, 256), 256, 0, s>>>(n, mp->a.drho, mp->a.drho_dt, mp->a.dyn, mp->a.pres,
+                                                mp->k.p.p0_over_rho0, float(0.5 * dt));
     SPHX_LAUNCHED(ctx);
     SPHX_CUDA(cudaMemsetAsync(mp->slots, 0, 2 * sizeof(unsigned long long), s));
     cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};

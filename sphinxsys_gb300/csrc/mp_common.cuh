@@ -25,7 +25,13 @@ constexpr int kGroup = 8;             // neighbours per plain partial sum
 // small (geo0 + pressure), the 2nd half's carry the velocity and use more registers
 // (measured: 8 / 4 is 8% faster in the 1st half than 4 / 4 and 7% faster in the 2nd half
 // than 8 / 8, 3D dam break dp = 0.006)
-constexpr int kUnrollFirst = 8, kUnrollSecond = 4;
+#ifndef SPHX_UNROLL_FIRST
+#define SPHX_UNROLL_FIRST 8
+#endif
+#ifndef SPHX_UNROLL_SECOND
+#define SPHX_UNROLL_SECOND 4
+#endif
+constexpr int kUnrollFirst = SPHX_UNROLL_FIRST, kUnrollSecond = SPHX_UNROLL_SECOND;
 constexpr int kCellBias = 4;          // |c_i - c_j| per axis handled by the packed difference
 constexpr int kReach = 2;             // neighbour search reach in sub-cells (cut-off = 2 sub-cells)
 
@@ -228,6 +234,7 @@ struct MPState
     // FP32 (what the pair arithmetic reads), off_lo = the FP32 rounding of its residual, so
     // the position integration carries the FP64 offset from step to step
     float *off, *off_lo, *force, *drho, *drho_dt, *drho_sum;
+    float *pres; // the pressure of dyn.w as a dense array (the 1st half's gathers read 4 B)
     uint32_t *id;
     float *fprior, *shift; // periodic flow only: prior (viscous) force, transport-velocity shift
 };
@@ -785,13 +792,13 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
             force[d].flush();
         rdis.flush();
     };
-    auto load = [&](uint32_t j) { return FirstRec{__ldg(&f.geo0[j]), __ldg(&f.dyn[j].w)}; };
+    auto load = [&](uint32_t j) { return FirstRec{__ldg(&f.geo0[j]), __ldg(&f.pres[j])}; };
     if constexpr (DEPTH > 0)
     {
         const AsyncRing<DEPTH> &rg = *ring;
         auto issue = [&](uint32_t j, unsigned slot) {
             cp_async16(&rg.a[rg.at(slot)], &f.geo0[j]);
-            cp_async4(&rg.c[rg.at(slot)], &f.dyn[j].w);
+            cp_async4(&rg.c[rg.at(slot)], &f.pres[j]);
         };
         auto read = [&](unsigned slot) { return FirstRec{rg.a[rg.at(slot)], rg.c[rg.at(slot)]}; };
         list_sweep_async<DEPTH>(i, n, in, rg, issue, read, pair, flush);
@@ -1185,7 +1192,7 @@ __device__ __forceinline__ double first_particle_periodic(size_t i, size_t n, co
     };
     auto load = [&](uint32_t e) {
         const uint32_t j = e & kIndexMask;
-        return FirstRecP{__ldg(&f.geo0[j]), __ldg(&f.dyn[j].w), wrap_corr<D>(k, e)};
+        return FirstRecP{__ldg(&f.geo0[j]), __ldg(&f.pres[j]), wrap_corr<D>(k, e)};
     };
     if (LISTS)
         list_sweep<true, kUnrollFirst>(i, n, in, load, pair, flush);
