@@ -343,6 +343,37 @@ __device__ __forceinline__ void geo_dx(float gs, uint32_t pib, const float *oi, 
     }
 }
 
+// geo_dx for the candidates of one run of for_each_candidate_run: the run's column fixes
+// the cell differences of all axes but the last, so only the last lane is decoded per
+// candidate.  Every difference is the same exact integer geo_dx forms, so dx is the same
+// bit for bit.
+template <int D>
+struct RunDx
+{
+    float gs, kl; // kl = 2^23 + c_i of the last axis (exact)
+    int c0, c1;
+    const float *oi;
+    __device__ __forceinline__ RunDx(float gs_, const int *ci, const float *oi_)
+        : gs(gs_), kl(8388608.0f + float(ci[D - 1])), c0(ci[0]), c1(ci[1]), oi(oi_)
+    {
+    }
+    __device__ __forceinline__ float column(int x) const { return float(c0 - x); }
+    __device__ __forceinline__ float column_y(int y) const { return D == 3 ? float(c1 - y) : 0.0f; }
+    __device__ __forceinline__ void dx(float dcx, float dcy, float4 gj, float *d) const
+    {
+        const uint32_t lane = (__float_as_uint(gj.w) >> ((D - 1) * CellLanes<D>::bits)) & CellLanes<D>::mask;
+        const float dcl = kl - __uint_as_float(0x4B000000u | lane);
+        d[0] = fmaf(dcx, gs, oi[0] - gj.x);
+        if (D == 3)
+        {
+            d[1] = fmaf(dcy, gs, oi[1] - gj.y);
+            d[2] = fmaf(dcl, gs, oi[2] - gj.z);
+        }
+        else
+            d[1] = fmaf(dcl, gs, oi[1] - gj.y);
+    }
+};
+
 template <int D>
 __device__ __forceinline__ float sq(const float *dx)
 {
@@ -995,32 +1026,43 @@ __device__ __forceinline__ void build_particle(size_t i, size_t n, const MPParam
     const float oi[3] = {gi.x, gi.y, gi.z};
     Kahan sigma;
     unsigned cnt = 0;
-    for_each_candidate<D, true>(v.m, v.cell_base, v.f_offset, ci, Reach(oi, k.gs_f, k.rc_reach), [&](uint32_t j) {
-        if (j == uint32_t(i))
-            return;
-        float dx[3];
-        geo_dx<D>(k.gs_f, pib, oi, f.geo0[j], dx);
-        float r2 = sq<D>(dx);
-        if (!(r2 < k.rc_sqr))
-            return;
-        if (cnt < in.cap)
-            in.J[size_t(cnt) * n + i] = j;
-        ++cnt;
-        sigma.add(wc2_W(k.fW, k.inv_h, sqrtf(r2)));
-    });
+    const RunDx<D> rd(k.gs_f, ci, oi);
+    for_each_candidate_run<D, true>(v.m, v.cell_base, v.f_offset, ci, Reach(oi, k.gs_f, k.rc_reach),
+                                    [&](int x, int y, uint32_t b, uint32_t e) {
+                                        const float dcx = rd.column(x), dcy = rd.column_y(y);
+                                        for (uint32_t j = b; j < e; ++j)
+                                        {
+                                            if (j == uint32_t(i))
+                                                continue;
+                                            float dx[3];
+                                            rd.dx(dcx, dcy, f.geo0[j], dx);
+                                            float r2 = sq<D>(dx);
+                                            if (!(r2 < k.rc_sqr))
+                                                continue;
+                                            if (cnt < in.cap)
+                                                in.J[size_t(cnt) * n + i] = j;
+                                            ++cnt;
+                                            sigma.add(wc2_W(k.fW, k.inv_h, sqrtf(r2)));
+                                        }
+                                    });
     Kahan wsig;
     unsigned wc = 0;
-    for_each_candidate<D, false>(v.m, v.cell_base, v.w_offset, ci, Reach(oi, k.gs_f, k.rc_reach), [&](uint32_t j) {
-        float dx[3];
-        geo_dx<D>(k.gs_f, pib, oi, w.geo[j], dx);
-        float r2 = sq<D>(dx);
-        if (!(r2 < k.rc_sqr))
-            return;
-        if (wc < wl.cap)
-            wl.J[size_t(wc) * n + i] = j;
-        ++wc;
-        wsig.add(wc2_W(k.fW, k.inv_h, sqrtf(r2)));
-    });
+    for_each_candidate_run<D, false>(v.m, v.cell_base, v.w_offset, ci, Reach(oi, k.gs_f, k.rc_reach),
+                                     [&](int x, int y, uint32_t b, uint32_t e) {
+                                         const float dcx = rd.column(x), dcy = rd.column_y(y);
+                                         for (uint32_t j = b; j < e; ++j)
+                                         {
+                                             float dx[3];
+                                             rd.dx(dcx, dcy, w.geo[j], dx);
+                                             float r2 = sq<D>(dx);
+                                             if (!(r2 < k.rc_sqr))
+                                                 continue;
+                                             if (wc < wl.cap)
+                                                 wl.J[size_t(wc) * n + i] = j;
+                                             ++wc;
+                                             wsig.add(wc2_W(k.fW, k.inv_h, sqrtf(r2)));
+                                         }
+                                     });
     in.count[i] = cnt;
     wl.count[i] = wc;
     warp_atomic_max(&max_counts[0], cnt);
