@@ -353,6 +353,15 @@ int sphx_mp_upload_host(sphx_mp mp, const double *position, const double *veloci
 /* Position and velocity (n x dim), density and pressure (n) rows in the body's particle
  * order, the values sphx_mp_download writes into the body (synchronises). */
 int sphx_mp_download_host(sphx_mp mp, double *position, double *velocity, double *density, double *pressure);
+/* Host rows (body order, the layout of sphx_mp_download_host) that every later
+ * sphx_mp_advection_step fills with the state it ends on: the velocity and pressure rows
+ * are copied while the last sub-step's 2nd half still runs (it changes neither), the
+ * position and density rows after it; the step returns once they are in host memory.  The
+ * same values as sphx_mp_download_host after the step.  Four nulls unregister.  Pinned
+ * rows (cudaHostAlloc) copy at the link's rate.  No counterpart in the reference, whose
+ * state lives in host memory: the device-to-host half of a caller that keeps its state in
+ * its own arrays (with sphx_mp_upload_host). */
+int sphx_mp_set_host_rows(sphx_mp mp, double *position, double *velocity, double *density, double *pressure);
 /* FP64 conservation sums: out[0] total mass, out[1..3] momentum, out[4] mechanical energy
  * (kinetic + potential with gravity and zero reference at the origin). */
 int sphx_mp_conservation(sphx_mp mp, double *out);

@@ -791,8 +791,11 @@ __global__ void k_mp_download(size_t n, MPConst k, MPFluid f, double *__restrict
 }
 
 // Host-row export (sphx_mp_download_host): position, velocity, density and pressure rows
-// in the body's particle order, the values k_mp_download writes.
-template <int D>
+// in the body's particle order, the values k_mp_download writes.  ROWS selects them:
+// kRowsAll, kRowsVelocity (velocity and pressure, final once the last 1st half has run)
+// or kRowsPosition (position and density, final after the 2nd half).
+constexpr int kRowsAll = 3, kRowsVelocity = 1, kRowsPosition = 2;
+template <int D, int ROWS>
 __global__ void k_mp_export_rows(size_t n, MPConst k, MPFluid f, double *__restrict__ pos, double *__restrict__ vel,
                                  double *__restrict__ rho, double *__restrict__ p)
 {
@@ -800,18 +803,24 @@ __global__ void k_mp_export_rows(size_t n, MPConst k, MPFluid f, double *__restr
     if (i >= n)
         return;
     uint32_t o = f.id[i];
-    int c[3];
-    unpack_cell<D>(__float_as_uint(f.geo0[i].w), c);
-    float4 di = f.dyn[i];
-    const float v[3] = {di.x, di.y, di.z};
-#pragma unroll
-    for (int d = 0; d < D; ++d)
+    if (ROWS & kRowsPosition)
     {
-        pos[size_t(o) * D + d] = position(k, f, n, i, d, c);
-        vel[size_t(o) * D + d] = v[d];
+        int c[3];
+        unpack_cell<D>(__float_as_uint(f.geo0[i].w), c);
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            pos[size_t(o) * D + d] = position(k, f, n, i, d, c);
+        rho[o] = double(k.p.rho0) + double(f.drho[i]);
     }
-    rho[o] = double(k.p.rho0) + double(f.drho[i]);
-    p[o] = di.w;
+    if (ROWS & kRowsVelocity)
+    {
+        float4 di = f.dyn[i];
+        const float v[3] = {di.x, di.y, di.z};
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            vel[size_t(o) * D + d] = v[d];
+        p[o] = di.w;
+    }
 }
 
 template <int D>
@@ -988,6 +997,10 @@ struct sphx_mp_s
     double *stage = nullptr;
     cudaStream_t side = nullptr;
     cudaEvent_t ev_pos = nullptr, ev_rest = nullptr;
+    // host rows every advection step delivers (sphx_mp_set_host_rows), and the event that
+    // releases the velocity rows after the last sub-step's 1st half
+    double *host_pos = nullptr, *host_vel = nullptr, *host_rho = nullptr, *host_p = nullptr;
+    cudaEvent_t ev_half = nullptr;
     int block = 128, strategy = 0;
     // tile-grouped traversal (TileShape): tile[0] == 0 keeps the cell order; `order` holds
     // the particles grouped by tile, recomputed at every configuration update
@@ -1416,8 +1429,39 @@ int launch_second_tiled(sphx_mp mp, unsigned blk, double dt)
     return SPHX_OK;
 }
 
+// Export of registered host rows from the last sub-step: velocity and pressure (final
+// after its 1st half) on the side stream, concurrent with the 2nd half; position and
+// density on the context's stream after the 2nd half.
 template <int D>
-int substep(sphx_mp mp, double dt)
+int deliver_rows(sphx_mp mp, int rows)
+{
+    const size_t n = mp->n;
+    cudaStream_t s = mp->ctx->stream;
+    double *spos = mp->stage, *svel = spos + n * D, *srho = svel + n * D, *sp = srho + n;
+    const size_t vec = n * D * sizeof(double), sca = n * sizeof(double);
+    if (rows == kRowsVelocity)
+    {
+        SPHX_CUDA(cudaEventRecord(mp->ev_half, s));
+        SPHX_CUDA(cudaStreamWaitEvent(mp->side, mp->ev_half, 0));
+        k_mp_export_rows<D, kRowsVelocity><<<grid_for(n, 256), 256, 0, mp->side>>>(n, mp->k, mp->a, spos, svel,
+                                                                                    srho, sp);
+        SPHX_LAUNCHED(mp->ctx);
+        SPHX_CUDA(cudaMemcpyAsync(mp->host_vel, svel, vec, cudaMemcpyDeviceToHost, mp->side));
+        SPHX_CUDA(cudaMemcpyAsync(mp->host_p, sp, sca, cudaMemcpyDeviceToHost, mp->side));
+    }
+    else
+    {
+        k_mp_export_rows<D, kRowsPosition><<<grid_for(n, 256), 256, 0, s>>>(n, mp->k, mp->a, spos, svel, srho, sp);
+        SPHX_LAUNCHED(mp->ctx);
+        SPHX_CUDA(cudaMemcpyAsync(mp->host_pos, spos, vec, cudaMemcpyDeviceToHost, s));
+        SPHX_CUDA(cudaMemcpyAsync(mp->host_rho, srho, sca, cudaMemcpyDeviceToHost, s));
+    }
+    return SPHX_OK;
+}
+
+// One acoustic sub-step; deliver: the last of an advection step with host rows registered.
+template <int D>
+int substep(sphx_mp mp, double dt, bool deliver = false)
 {
     sphx_ctx ctx = mp->ctx;
     cudaStream_t s = ctx->stream;
@@ -1464,6 +1508,8 @@ int substep(sphx_mp mp, double dt)
     else
         mp->order_active ? launch_first<D, false, true>(mp, blk, dt) : launch_first<D, false, false>(mp, blk, dt);
     SPHX_LAUNCHED(ctx);
+    if (deliver)
+        SPHX_TRY(deliver_rows<D>(mp, kRowsVelocity));
     if (e[1])
         SPHX_CUDA(cudaEventRecord(e[1], s));
     if (e[2])
@@ -1488,6 +1534,8 @@ int substep(sphx_mp mp, double dt)
     else
         mp->order_active ? launch_second<D, false, true>(mp, blk, dt) : launch_second<D, false, false>(mp, blk, dt);
     SPHX_LAUNCHED(ctx);
+    if (deliver)
+        SPHX_TRY(deliver_rows<D>(mp, kRowsPosition));
     if (e[3])
         SPHX_CUDA(cudaEventRecord(e[3], s));
     return SPHX_OK;
@@ -1510,6 +1558,7 @@ int advection_step(sphx_mp mp, int loop_style, int *substeps, double *adv_dt)
     }
     double relaxation = 0, dt = mp->acoustic_dt;
     int count = 0;
+    bool delivered = false;
     while (relaxation < Dt)
     {
         double ac;
@@ -1520,7 +1569,10 @@ int advection_step(sphx_mp mp, int loop_style, int *substeps, double *adv_dt)
             if (mp->k.periodic) // dt = SMIN(acoustic dt, Dt) (taylor_green.cpp:146)
                 dt = std::min(dt, Dt);
         }
-        SPHX_TRY(substep<D>(mp, dt));
+        // the last sub-step (relaxation reaches Dt) delivers the registered host rows
+        const bool deliver = mp->host_pos && relaxation + dt >= Dt;
+        SPHX_TRY(substep<D>(mp, dt, deliver));
+        delivered = delivered || deliver;
         if (loop_style == 1) // after it (test_3d_dambreak/dambreak.cpp:197)
         {
             SPHX_TRY(read_slot(mp, 0, &ac));
@@ -1532,6 +1584,11 @@ int advection_step(sphx_mp mp, int loop_style, int *substeps, double *adv_dt)
     }
     mp->acoustic_dt = dt;
     mp->moved = true;
+    if (delivered) // the rows are in host memory when the step returns
+    {
+        SPHX_CUDA(cudaStreamSynchronize(mp->side));
+        SPHX_CUDA(cudaStreamSynchronize(mp->ctx->stream));
+    }
     if (substeps)
         *substeps = count;
     if (adv_dt)
@@ -1917,6 +1974,8 @@ int ensure_host_io(sphx_mp mp)
         SPHX_CUDA(cudaEventCreateWithFlags(&mp->ev_pos, cudaEventDisableTiming));
     if (!mp->ev_rest)
         SPHX_CUDA(cudaEventCreateWithFlags(&mp->ev_rest, cudaEventDisableTiming));
+    if (!mp->ev_half)
+        SPHX_CUDA(cudaEventCreateWithFlags(&mp->ev_half, cudaEventDisableTiming));
     return SPHX_OK;
 }
 
@@ -1990,7 +2049,7 @@ int download_host(sphx_mp mp, double *pos, double *vel, double *rho, double *p)
     double *spos = mp->stage, *svel = spos + n * D, *srho = svel + n * D, *sp = srho + n;
     if (n > 0)
     {
-        k_mp_export_rows<D><<<grid_for(n, 256), 256, 0, s>>>(n, mp->k, mp->a, spos, svel, srho, sp);
+        k_mp_export_rows<D, kRowsAll><<<grid_for(n, 256), 256, 0, s>>>(n, mp->k, mp->a, spos, svel, srho, sp);
         SPHX_LAUNCHED(mp->ctx);
         const size_t vec = n * D * sizeof(double), sca = n * sizeof(double);
         SPHX_CUDA(cudaMemcpyAsync(pos, spos, vec, cudaMemcpyDeviceToHost, s));
@@ -2021,6 +2080,24 @@ extern "C" int sphx_mp_download_host(sphx_mp mp, double *position, double *veloc
         return fail(SPHX_ERR_INVALID_ARG, "sphx_mp_download_host needs the four host rows");
     return mp->dim == 2 ? download_host<2>(mp, position, velocity, density, pressure)
                         : download_host<3>(mp, position, velocity, density, pressure);
+}
+
+extern "C" int sphx_mp_set_host_rows(sphx_mp mp, double *position, double *velocity, double *density,
+                                     double *pressure)
+{
+    if (!mp)
+        return fail(SPHX_ERR_INVALID_ARG, "null solver");
+    const bool none = !position && !velocity && !density && !pressure;
+    if (!none && mp->n > 0 && (!position || !velocity || !density || !pressure))
+        return fail(SPHX_ERR_INVALID_ARG, "sphx_mp_set_host_rows takes the four host rows, or none");
+    if (!none)
+        SPHX_TRY(ensure_host_io(mp));
+    SPHX_CUDA(cudaStreamSynchronize(mp->ctx->stream));
+    mp->host_pos = none ? nullptr : position;
+    mp->host_vel = none ? nullptr : velocity;
+    mp->host_rho = none ? nullptr : density;
+    mp->host_p = none ? nullptr : pressure;
+    return SPHX_OK;
 }
 
 extern "C" int sphx_mp_upload(sphx_mp mp, sphx_body fb)
@@ -2102,6 +2179,8 @@ extern "C" int sphx_mp_destroy(sphx_mp mp)
         cudaEventDestroy(mp->ev_pos);
     if (mp->ev_rest)
         cudaEventDestroy(mp->ev_rest);
+    if (mp->ev_half)
+        cudaEventDestroy(mp->ev_half);
     for (void *p : mp->owned)
         cudaFree(p);
     if (mp->h_slots)

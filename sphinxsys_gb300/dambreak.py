@@ -232,6 +232,23 @@ class MixedPrecisionDamBreak:
         C = self._C
         self._N.call("sphx_mp_download_host", self.handle, *[C.c_void_p(a.ctypes.data) for a in rows])
 
+    def set_host_rows(self, position=None, velocity=None, density=None, pressure=None) -> None:
+        """Registers host rows (the layout of download_host) that every later advection
+        step fills with its final state (sphx_mp_set_host_rows); no arguments unregister.
+        The arrays are kept referenced while registered."""
+        rows = [position, velocity, density, pressure]
+        C = self._C
+        if all(a is None for a in rows):
+            self._N.call("sphx_mp_set_host_rows", self.handle, None, None, None, None)
+            self._host_rows = None
+            return
+        for a, nc in zip(rows, (self.case.dim, self.case.dim, 1, 1)):
+            if (a is None or a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]
+                    or a.size != self.n_fluid * nc):
+                raise ValueError("host rows must be C-contiguous float64 of the fluid's size")
+        self._N.call("sphx_mp_set_host_rows", self.handle, *[C.c_void_p(a.ctypes.data) for a in rows])
+        self._host_rows = rows
+
     def sync_fp64(self) -> None:
         sim = self.fp64
         self._N.call("sphx_mp_download", self.handle, sim.water_block.handle)

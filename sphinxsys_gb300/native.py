@@ -112,6 +112,7 @@ SIGNATURES = {
     "sphx_mp_upload": (_i, [_vp, _vp]),
     "sphx_mp_upload_host": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "sphx_mp_download_host": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "sphx_mp_set_host_rows": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "sphx_mp_conservation": (_i, [_vp, _pd]),
     "sphx_mp_upper_front": (_i, [_vp, _i, _pd, _pd, _pd]),
     "sphx_mp_check_state": (_i, [_vp, _pu64, _pu64]),

@@ -225,6 +225,33 @@ def test_host_rows_load_and_store_like_the_body_path(case):
         assert np.array_equal(v, a.fp64.water_block.download(name)), name
 
 
+@pytest.mark.parametrize("case", [cases.dambreak_2d(), cases.dambreak_3d(0.04)], ids=lambda c: c.name)
+def test_registered_host_rows_hold_each_step_result(case):
+    """Rows registered with sphx_mp_set_host_rows hold, after every advection step, what
+    sphx_mp_download_host returns after it, bit for bit (velocity and pressure copied
+    during the last 2nd half, position and density after it); the run itself is the
+    same as without rows; unregistered, the rows stay as the last step left them."""
+    a = MixedPrecisionDamBreak(case)
+    b = MixedPrecisionDamBreak(case)
+    n, d = a.n_fluid, case.dim
+    rows = {"Position": np.zeros((n, d)), "Velocity": np.zeros((n, d)), "Density": np.zeros(n),
+            "Pressure": np.zeros(n)}
+    b.set_host_rows(rows["Position"], rows["Velocity"], rows["Density"], rows["Pressure"])
+    for _ in range(3):
+        assert a.advection_step() == b.advection_step()
+        ref = {k: np.zeros_like(v) for k, v in rows.items()}
+        a.download_host(ref["Position"], ref["Velocity"], ref["Density"], ref["Pressure"])
+        for name, v in rows.items():
+            assert np.array_equal(v, ref[name]), name
+    kept = {k: v.copy() for k, v in rows.items()}
+    b.set_host_rows()
+    b.advection_step()
+    for name, v in rows.items():
+        assert np.array_equal(v, kept[name]), name
+    with pytest.raises(ValueError):
+        b.set_host_rows(rows["Position"], None, rows["Density"], rows["Pressure"])
+
+
 def test_autotune_keeps_state():
     """The autotuner restores the state it advanced (whichever of the strategies 0-6 it
     keeps: on this 3,200-particle case the lane-split ones can win, their extra lanes
