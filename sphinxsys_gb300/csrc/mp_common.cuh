@@ -1096,24 +1096,24 @@ __device__ __forceinline__ uint32_t wrap_corr(const MPParams &k, uint32_t e)
     return c;
 }
 
-// Candidates of the wrapped window around sub-cell c, pruned as for_each_candidate does:
-// f(j, code) with code the per-axis image shifts (two bits per axis, two's complement) of
-// the cell j was found in.
-template <int D, class F>
-__device__ __forceinline__ void for_each_candidate_periodic(const MeshDev &m, const uint32_t *offset, const int *c,
-                                                            const Reach &q, F &&f)
+// Candidate runs of the wrapped window around sub-cell c, pruned as for_each_candidate
+// does: run(ax, by, sl, code, b, e) for the candidates [b, e) of one segment of a column,
+// with ax, by the column's offset from c before wrapping (c_i - c_j + s N = -ax along x,
+// -by along y), sl the image shift along the last axis, and code the per-axis image shifts
+// (two bits per axis, two's complement) of the cells the segment's candidates lie in.
+template <int D, class R>
+__device__ __forceinline__ void for_each_run_periodic(const MeshDev &m, const uint32_t *offset, const int *c,
+                                                      const Reach &q, R &&run)
 {
     const int NL = m.all_cells[D - 1];
     const float r2 = q.r * q.r;
-    auto last_axis = [&](uint32_t base, uint32_t code, float rl) {
+    auto last_axis = [&](uint32_t base, uint32_t code, float rl, int ax, int by) {
         int l, h;
         axis_reach(q.o[D - 1], q.inv_gs, rl, l, h);
         const int lo = c[D - 1] - l, hi = c[D - 1] + h;
         auto seg = [&](int z0, int z1, int s) {
             const uint32_t cd = code | ((uint32_t(s) & 3u) << (2 * (D - 1)));
-            const uint32_t b = offset[base + uint32_t(z0)], e = offset[base + uint32_t(z1) + 1];
-            for (uint32_t j = b; j < e; ++j)
-                f(j, cd);
+            run(ax, by, s, cd, offset[base + uint32_t(z0)], offset[base + uint32_t(z1) + 1]);
         };
         if (lo < 0)
         {
@@ -1138,7 +1138,7 @@ __device__ __forceinline__ void for_each_candidate_periodic(const MeshDev &m, co
         x += sx * m.all_cells[0];
         const uint32_t cx = uint32_t(sx) & 3u;
         if (D == 2)
-            last_axis(uint32_t(x) * uint32_t(m.all_cells[1]), cx, sqrtf(fmaxf(r2 - gx * gx, 0.0f)));
+            last_axis(uint32_t(x) * uint32_t(m.all_cells[1]), cx, sqrtf(fmaxf(r2 - gx * gx, 0.0f)), a, 0);
         else
         {
             int l1, h1;
@@ -1153,10 +1153,21 @@ __device__ __forceinline__ void for_each_candidate_periodic(const MeshDev &m, co
                 const int sy = y < 0 ? 1 : (y >= m.all_cells[1] ? -1 : 0);
                 y += sy * m.all_cells[1];
                 last_axis((uint32_t(x) * uint32_t(m.all_cells[1]) + uint32_t(y)) * uint32_t(m.all_cells[2]),
-                          cx | ((uint32_t(sy) & 3u) << 2), sqrtf(r2 - g2));
+                          cx | ((uint32_t(sy) & 3u) << 2), sqrtf(r2 - g2), a, b);
             }
         }
     }
+}
+
+// Candidates of the wrapped window one by one: f(j, code) in run order.
+template <int D, class F>
+__device__ __forceinline__ void for_each_candidate_periodic(const MeshDev &m, const uint32_t *offset, const int *c,
+                                                            const Reach &q, F &&f)
+{
+    for_each_run_periodic<D>(m, offset, c, q, [&](int, int, int, uint32_t code, uint32_t b, uint32_t e) {
+        for (uint32_t j = b; j < e; ++j)
+            f(j, code);
+    });
 }
 
 // Same visits as the stored periodic lists, by a sweep of the wrapped window.
@@ -1344,18 +1355,39 @@ __device__ __forceinline__ void build_particle_periodic(size_t i, size_t n, cons
     unpack_cell<D>(__float_as_uint(gi.w), ci);
     const float oi[3] = {gi.x, gi.y, gi.z};
     unsigned cnt = 0;
-    for_each_candidate_periodic<D>(m, f_offset, ci, Reach(oi, k.gs_f, k.rc_reach), [&](uint32_t j, uint32_t code) {
-        if (j == uint32_t(i) && code == 0)
-            return;
-        const uint32_t e = j | (code << kCodeShift);
-        float dx[3];
-        geo_dx<D>(k.gs_f, pib + wrap_corr<D>(k, e), oi, f.geo0[j], dx);
-        if (!(sq<D>(dx) < k.rc_sqr))
-            return;
-        if (cnt < in.cap)
-            in.J[size_t(cnt) * n + i] = e;
-        ++cnt;
-    });
+    // per segment the cell differences of the column axes are -ax, -by and the last axis's
+    // is c_i + sl N - c_j: only the last lane is decoded per candidate (the exact integer
+    // differences geo_dx forms from the shifted lanes, so the same dx bit for bit)
+    const int NL = m.all_cells[D - 1];
+    for_each_run_periodic<D>(m, f_offset, ci, Reach(oi, k.gs_f, k.rc_reach),
+                             [&](int ax, int by, int sl, uint32_t code, uint32_t b, uint32_t e) {
+                                 const float dcx = float(-ax), dcy = float(-by);
+                                 const float kl = 8388608.0f + float(ci[D - 1] + sl * NL);
+                                 const uint32_t hi = code << kCodeShift;
+                                 for (uint32_t j = b; j < e; ++j)
+                                 {
+                                     if (j == uint32_t(i) && code == 0)
+                                         continue;
+                                     const float4 gj = f.geo0[j];
+                                     const uint32_t lane = (__float_as_uint(gj.w) >> ((D - 1) * CellLanes<D>::bits)) &
+                                                           CellLanes<D>::mask;
+                                     const float dcl = kl - __uint_as_float(0x4B000000u | lane);
+                                     float dx[3];
+                                     dx[0] = fmaf(dcx, k.gs_f, oi[0] - gj.x);
+                                     if (D == 3)
+                                     {
+                                         dx[1] = fmaf(dcy, k.gs_f, oi[1] - gj.y);
+                                         dx[2] = fmaf(dcl, k.gs_f, oi[2] - gj.z);
+                                     }
+                                     else
+                                         dx[1] = fmaf(dcl, k.gs_f, oi[1] - gj.y);
+                                     if (!(sq<D>(dx) < k.rc_sqr))
+                                         continue;
+                                     if (cnt < in.cap)
+                                         in.J[size_t(cnt) * n + i] = j | hi;
+                                     ++cnt;
+                                 }
+                             });
     in.count[i] = cnt;
     warp_atomic_max(&max_counts[0], cnt);
     // Two phases: the candidate loop above only tests and stores (the lanes of a warp
