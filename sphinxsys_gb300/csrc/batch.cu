@@ -305,8 +305,10 @@ __global__ void __launch_bounds__(256, 4) k_b_first(size_t n, const uint32_t *__
     instance_max(run, b, active, vmax, false);
 }
 
+// held to 64 registers like the single-case 2nd half (its packed x / y arithmetic would
+// otherwise take more, and fewer warps fit)
 template <int D>
-__global__ void k_b_second(size_t n, const uint32_t *__restrict__ starts, int count, const BInst *__restrict__ inst, BRun *run,
+__global__ void __launch_bounds__(256, 4) k_b_second(size_t n, const uint32_t *__restrict__ starts, int count, const BInst *__restrict__ inst, BRun *run,
                MPState f, MPWallData w, MPNeighbors in, MPNeighbors wl)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;

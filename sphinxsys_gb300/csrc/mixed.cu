@@ -608,13 +608,13 @@ __global__ void k_mp_second_lanes(size_t n, MPConst k, MPFluid f, MPWall w, MPLi
 inline int strategy_lanes(int strategy) { return strategy == 5 ? 2 : (strategy == 6 ? 4 : 0); }
 
 // Blocks of 256 threads per SM the stored-list / cell sweeps are compiled to fit (the
-// register cap follows: 4 -> 64, 5 -> 48 registers; 0 leaves the 2nd half unbounded, ~64
-// registers): build-time tuning parameters.
+// register cap follows: 4 -> 64, 5 -> 48 registers; 0 leaves the 2nd half unbounded: with
+// the packed x / y arithmetic it would take 66): build-time tuning parameters.
 #ifndef SPHX_FIRST_MINB
 #define SPHX_FIRST_MINB 4
 #endif
 #ifndef SPHX_SECOND_MINB
-#define SPHX_SECOND_MINB 0
+#define SPHX_SECOND_MINB 4
 #endif
 #if SPHX_SECOND_MINB > 0
 #define SPHX_SECOND_BOUNDS __launch_bounds__(256, SPHX_SECOND_MINB)
