@@ -894,6 +894,8 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
     const float p_i = di.w;
     const float rho_i = k.rho0 + f.drho[i];
     // the x and y components in packed arithmetic (the same operations as the scalar z)
+    // (measured slower here: the z force paired with the dissipation in a second packed
+    // accumulator, 60 B of spills; p_i + p_j and p_i - p_j as one packed add, 12 B)
     const float2 oi01 = make_float2(gi.x, gi.y);
     Acc2 force01;
     Acc force2, rdis;
@@ -960,6 +962,7 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
                              wpair, wflush);
 
     const float fv[3] = {force01.x(), force01.y(), force2.value()};
+    const float rv = rdis.value();
     float fsum[3], wfsum[3];
 #pragma unroll
     for (int d = 0; d < D; ++d)
@@ -967,7 +970,7 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
         fsum[d] = group_sum<LANES>(fv[d]);
         wfsum[d] = group_sum<LANES>(wforce[d].value());
     }
-    const float rsum = group_sum<LANES>(rdis.value()), wrsum = group_sum<LANES>(wrdis.value());
+    const float rsum = group_sum<LANES>(rv), wrsum = group_sum<LANES>(wrdis.value());
     if (lane_in_group<LANES>() != 0)
         return -1.0e300;
     f.drho_dt[i] = (rsum * k.inv_z) * rho_i + (wrsum * k.inv_z) * rho_i;
@@ -1013,8 +1016,8 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
     // operations): measured 8 % faster when the kernel is held to 64 registers, slower
     // when it takes the 66 it would otherwise use
     const float2 oi01 = make_float2(gi.x, gi.y), vi01 = make_float2(di.x, di.y);
-    Acc rate, pdis2, pdis[3];
-    Acc2 pdis01;
+    Acc rate, pdis[3];
+    Acc2 pdis01, zr;
     auto pair = [&](const SecondRec &r) {
         float dx[3];
         if (SPHX_PACKED_SECOND)
@@ -1038,31 +1041,39 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
         }
         dv[2] = vi[2] - r.v.z;
         float u = dot<D>(dv, dx) * inv;
-        rate.add(u * dWV);
         float sc = p_jump(k, u) * (dWV * inv);
         if (SPHX_PACKED_SECOND)
         {
             pdis01.fma(make_float2(sc, sc), make_float2(dx[0], dx[1]));
-            if (D == 3)
-                pdis2.add(sc * dx[2]);
+            if (D == 3) // the z dissipation and the density rate share a packed pair
+                zr.fma(make_float2(sc, u), make_float2(dx[2], dWV));
+            else
+                rate.add(u * dWV);
         }
         else
+        {
+            rate.add(u * dWV);
 #pragma unroll
             for (int d = 0; d < D; ++d)
                 pdis[d].add(sc * dx[d]);
+        }
     };
     auto flush = [&]() {
-        rate.flush();
         if (SPHX_PACKED_SECOND)
         {
             pdis01.flush();
             if (D == 3)
-                pdis2.flush();
+                zr.flush();
+            else
+                rate.flush();
         }
         else
+        {
+            rate.flush();
 #pragma unroll
             for (int d = 0; d < D; ++d)
                 pdis[d].flush();
+        }
     };
     auto load = [&](uint32_t j) { return SecondRec{__ldg(&f.geo0[j]), __ldg(&f.dyn[j])}; };
     if constexpr (DEPTH > 0)
@@ -1110,9 +1121,11 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
         cell_sweep<D, false>(v, v.w_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, ~size_t(0), w.geo, wload,
                              wpair, wflush);
 
+    const bool zr_rate = SPHX_PACKED_SECOND && D == 3;
     const float pv[3] = {SPHX_PACKED_SECOND ? pdis01.x() : pdis[0].value(),
                          SPHX_PACKED_SECOND ? pdis01.y() : pdis[1].value(),
-                         SPHX_PACKED_SECOND ? pdis2.value() : pdis[2].value()};
+                         SPHX_PACKED_SECOND ? zr.x() : pdis[2].value()};
+    const float rate_v = zr_rate ? zr.y() : rate.value();
     float psum[3], wpsum[3];
 #pragma unroll
     for (int d = 0; d < D; ++d)
@@ -1120,7 +1133,7 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
         psum[d] = group_sum<LANES>(pv[d]);
         wpsum[d] = group_sum<LANES>(wdis[d].value());
     }
-    const float ratesum = group_sum<LANES>(rate.value()), wratesum = group_sum<LANES>(wrate.value());
+    const float ratesum = group_sum<LANES>(rate_v), wratesum = group_sum<LANES>(wrate.value());
     if (lane_in_group<LANES>() != 0)
         return -1.0e300;
     float drho_dt = f.drho_dt[i] + ratesum * rho_i + wratesum * rho_i;
