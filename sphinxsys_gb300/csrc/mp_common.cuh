@@ -32,6 +32,11 @@ constexpr int kGroup = 8;             // neighbours per plain partial sum
 #define SPHX_UNROLL_SECOND 4
 #endif
 constexpr int kUnrollFirst = SPHX_UNROLL_FIRST, kUnrollSecond = SPHX_UNROLL_SECOND;
+// the 2nd half's list entries loaded one batch ahead (see list_sweep)
+#ifndef SPHX_PREFETCH_SECOND
+#define SPHX_PREFETCH_SECOND 0
+#endif
+constexpr bool kPrefetchSecond = SPHX_PREFETCH_SECOND != 0;
 constexpr int kCellBias = 4;          // |c_i - c_j| per axis handled by the packed difference
 constexpr int kReach = 2;             // neighbour search reach in sub-cells (cut-off = 2 sub-cells)
 
@@ -1087,7 +1092,7 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
         list_sweep_async<DEPTH>(i, n, in, rg, issue, read, pair, flush);
     }
     else if (LISTS)
-        list_sweep<false, kUnrollSecond, LANES>(i, n, in, load, pair, flush, lane_in_group<LANES>());
+        list_sweep<kPrefetchSecond, kUnrollSecond, LANES>(i, n, in, load, pair, flush, lane_in_group<LANES>());
     else
         cell_sweep<D, true>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, i, f.geo0, load, pair, flush);
 
