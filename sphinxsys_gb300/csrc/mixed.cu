@@ -672,8 +672,19 @@ __global__ void __launch_bounds__(256, 4) k_mp_first_periodic(size_t n, MPConst 
     warp_max_to(ac_slot, vmax);
 }
 
+// Blocks of 256 per SM the periodic 2nd half is compiled to fit (5: 48 registers; 0: no
+// bound).
+#ifndef SPHX_PERIODIC_SECOND_MINB
+#define SPHX_PERIODIC_SECOND_MINB 5
+#endif
+#if SPHX_PERIODIC_SECOND_MINB > 0
+#define SPHX_PERIODIC_SECOND_BOUNDS __launch_bounds__(256, SPHX_PERIODIC_SECOND_MINB)
+#else
+#define SPHX_PERIODIC_SECOND_BOUNDS
+#endif
+
 template <int D, bool LISTS, bool RIEMANN>
-__global__ void k_mp_second_periodic(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset,
+__global__ void SPHX_PERIODIC_SECOND_BOUNDS k_mp_second_periodic(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset,
                                      MPLists in, double dt, unsigned long long *adv_slot)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;

@@ -311,6 +311,9 @@ struct Kahan
 #ifndef SPHX_PACKED_SECOND
 #define SPHX_PACKED_SECOND 1
 #endif
+#ifndef SPHX_PACKED_PERIODIC_SECOND
+#define SPHX_PACKED_PERIODIC_SECOND 1
+#endif
 __device__ __forceinline__ float2 f2_add(float2 a, float2 b)
 {
 #if SPHX_PACKED_F32X2
@@ -1439,15 +1442,31 @@ __device__ __forceinline__ double second_particle_periodic(size_t i, size_t n, c
     const float4 di = f.dyn[i];
     const float vi[3] = {di.x, di.y, di.z};
     const float rho_i = k.rho0 + f.drho[i];
-    // (scalar: the packed x / y arithmetic of first_particle measured 10 % slower here)
+    // SPHX_PACKED_PERIODIC_SECOND: x and y of the geometry and the velocity difference in
+    // packed arithmetic; held to 48 registers 3 % faster than the scalar form (unbounded,
+    // at 52 registers, 10 % slower)
+    const float2 oi01 = make_float2(gi.x, gi.y), vi01 = make_float2(di.x, di.y);
     Acc rate, pdis[3];
     auto pair = [&](const SecondRecP &r) {
         float dx[3];
-        geo_dx<D>(k.gs_f, pib + r.corr, oi, r.g, dx);
+        float dv[3];
+        if (SPHX_PACKED_PERIODIC_SECOND)
+        {
+            geo_dx2<D>(k.gs_f, pib + r.corr, oi01, oi[2], r.g, dx);
+            const float2 dv01 = f2_sub(vi01, make_float2(r.v.x, r.v.y));
+            dv[0] = dv01.x;
+            dv[1] = dv01.y;
+        }
+        else
+        {
+            geo_dx<D>(k.gs_f, pib + r.corr, oi, r.g, dx);
+            dv[0] = vi[0] - r.v.x;
+            dv[1] = vi[1] - r.v.y;
+        }
+        dv[2] = vi[2] - r.v.z;
         float r2 = sq<D>(dx);
         float inv = inv_dist(r2);
         float dWV = wc2_dWV(k.cW, k.inv_h, r2 * inv);
-        const float dv[3] = {vi[0] - r.v.x, vi[1] - r.v.y, vi[2] - r.v.z};
         float u = dot<D>(dv, dx) * inv;
         rate.add(u * dWV);
         if (RIEMANN)
