@@ -287,9 +287,13 @@ __global__ void k_b_init1(size_t n, const uint32_t *__restrict__ starts, int cou
     pres[i] = p;
 }
 
-// at most 64 registers: 4 blocks of 256 threads per SM
+// Blocks of 256 threads per SM the batch's 1st half is compiled to fit (4: 64 registers
+// with spills; 3, at 80 registers without, measured 2 % slower).
+#ifndef SPHX_BATCH_FIRST_MINB
+#define SPHX_BATCH_FIRST_MINB 4
+#endif
 template <int D>
-__global__ void __launch_bounds__(256, 4) k_b_first(size_t n, const uint32_t *__restrict__ starts, int count, const BInst *__restrict__ inst, BRun *run,
+__global__ void __launch_bounds__(256, SPHX_BATCH_FIRST_MINB) k_b_first(size_t n, const uint32_t *__restrict__ starts, int count, const BInst *__restrict__ inst, BRun *run,
               MPState f, MPWallData w, MPNeighbors in, MPNeighbors wl)
 {
     size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
