@@ -633,9 +633,26 @@ inline int strategy_lanes(int strategy) { return strategy == 5 ? 2 : (strategy =
 #else
 #define SPHX_SECOND_BOUNDS
 #endif
+// Register caps of the sweeps independent of the block size (0: from the bounds above).
+#ifndef SPHX_FIRST_MAXNREG
+#define SPHX_FIRST_MAXNREG 0
+#endif
+#ifndef SPHX_SECOND_MAXNREG
+#define SPHX_SECOND_MAXNREG 0
+#endif
+#if SPHX_FIRST_MAXNREG > 0
+#define SPHX_FIRST_ATTR __maxnreg__(SPHX_FIRST_MAXNREG)
+#else
+#define SPHX_FIRST_ATTR __launch_bounds__(256, SPHX_FIRST_MINB)
+#endif
+#if SPHX_SECOND_MAXNREG > 0
+#define SPHX_SECOND_ATTR __maxnreg__(SPHX_SECOND_MAXNREG)
+#else
+#define SPHX_SECOND_ATTR SPHX_SECOND_BOUNDS
+#endif
 
 template <int D, bool LISTS, bool ORDER>
-__global__ void __launch_bounds__(256, SPHX_FIRST_MINB) k_mp_first(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
+__global__ void SPHX_FIRST_ATTR k_mp_first(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
                const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, double dt,
                unsigned long long *ac_slot, const uint32_t *__restrict__ order)
 {
@@ -648,7 +665,7 @@ __global__ void __launch_bounds__(256, SPHX_FIRST_MINB) k_mp_first(size_t n, MPC
 }
 
 template <int D, bool LISTS, bool ORDER>
-__global__ void SPHX_SECOND_BOUNDS k_mp_second(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
+__global__ void SPHX_SECOND_ATTR k_mp_second(size_t n, MPConst k, MPFluid f, const uint32_t *__restrict__ f_offset, MPWall w,
                 const uint32_t *__restrict__ w_offset, MPLists in, MPLists wl, double dt,
                 unsigned long long *adv_slot, const uint32_t *__restrict__ order)
 {
