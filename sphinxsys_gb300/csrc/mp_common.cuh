@@ -941,25 +941,26 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
     else
         cell_sweep<D, true>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, i, f.geo0, load, pair, flush);
 
-    Acc wforce[3], wrdis;
+    Acc2 wforce01; // x and y packed, as the fluid pairs
+    Acc wforce2, wrdis;
     auto wpair = [&](const float4 &gj) {
         float dx[3];
-        geo_dx<D>(k.gs_f, pib, oi, gj, dx);
+        geo_dx2<D>(k.gs_f, pib, oi01, oi[2], gj, dx);
         float r2 = sq<D>(dx);
         float inv = inv_dist(r2);
         float dWV = wc2_dWV(k.cWw, k.inv_h, r2 * inv);
         // wall pressure p_i + rho_i r max(0, (F_prior / m - a_wall) . (-e)), static wall
         float p_w = p_i + rho_i * fmaxf(0.0f, -dot<D>(k.g, dx));
         float sc = (p_i + p_w) * (dWV * inv);
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-            wforce[d].add(-sc * dx[d]);
+        wforce01.fma(make_float2(-sc, -sc), make_float2(dx[0], dx[1]));
+        if (D == 3)
+            wforce2.add(-sc * dx[2]);
         wrdis.add((p_i - p_w) * dWV);
     };
     auto wflush = [&]() {
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-            wforce[d].flush();
+        wforce01.flush();
+        if (D == 3)
+            wforce2.flush();
         wrdis.flush();
     };
     auto wload = [&](uint32_t j) { return __ldg(&w.geo[j]); };
@@ -970,13 +971,14 @@ __device__ __forceinline__ double first_particle(size_t i, size_t n, const MPPar
                              wpair, wflush);
 
     const float fv[3] = {force01.x(), force01.y(), force2.value()};
+    const float wv[3] = {wforce01.x(), wforce01.y(), wforce2.value()};
     const float rv = rdis.value();
     float fsum[3], wfsum[3];
 #pragma unroll
     for (int d = 0; d < D; ++d)
     {
         fsum[d] = group_sum<LANES>(fv[d]);
-        wfsum[d] = group_sum<LANES>(wforce[d].value());
+        wfsum[d] = group_sum<LANES>(wv[d]);
     }
     const float rsum = group_sum<LANES>(rv), wrsum = group_sum<LANES>(wrdis.value());
     if (lane_in_group<LANES>() != 0)
@@ -1099,10 +1101,11 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
     else
         cell_sweep<D, true>(v, v.f_offset, ci, k.gs_f, pib, oi, k.rc_sqr, k.rc_reach, i, f.geo0, load, pair, flush);
 
-    Acc wrate, wdis[3];
+    Acc wrate, wdis2;
+    Acc2 wdis01; // x and y packed, as the fluid pairs
     auto wpair = [&](const SecondRec &r) {
         float dx[3];
-        geo_dx<D>(k.gs_f, pib, oi, r.g, dx);
+        geo_dx2<D>(k.gs_f, pib, oi01, oi[2], r.g, dx);
         float r2 = sq<D>(dx);
         float inv = inv_dist(r2);
         float dWV = wc2_dWV(k.cWw, k.inv_h, r2 * inv);
@@ -1112,15 +1115,15 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
         // (v_i - (2 v_wall - v_i)) . e with a static wall; face velocity jump along n
         wrate.add(2.0f * (dot<D>(vi, dx) * inv) * dWV);
         float sc = p_jump(k, 2.0f * sgn * dot<D>(vi, nj)) * dWV * sgn;
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-            wdis[d].add(sc * nj[d]);
+        wdis01.fma(make_float2(sc, sc), make_float2(nj[0], nj[1]));
+        if (D == 3)
+            wdis2.add(sc * nj[2]);
     };
     auto wflush = [&]() {
         wrate.flush();
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-            wdis[d].flush();
+        wdis01.flush();
+        if (D == 3)
+            wdis2.flush();
     };
     auto wload = [&](uint32_t j) { return SecondRec{__ldg(&w.geo[j]), __ldg(&w.n[j])}; };
     if (LISTS || DEPTH > 0)
@@ -1134,12 +1137,13 @@ __device__ __forceinline__ double second_particle(size_t i, size_t n, const MPPa
                          SPHX_PACKED_SECOND ? pdis01.y() : pdis[1].value(),
                          SPHX_PACKED_SECOND ? zr.x() : pdis[2].value()};
     const float rate_v = zr_rate ? zr.y() : rate.value();
+    const float wv[3] = {wdis01.x(), wdis01.y(), wdis2.value()};
     float psum[3], wpsum[3];
 #pragma unroll
     for (int d = 0; d < D; ++d)
     {
         psum[d] = group_sum<LANES>(pv[d]);
-        wpsum[d] = group_sum<LANES>(wdis[d].value());
+        wpsum[d] = group_sum<LANES>(wv[d]);
     }
     const float ratesum = group_sum<LANES>(rate_v), wratesum = group_sum<LANES>(wrate.value());
     if (lane_in_group<LANES>() != 0)
