@@ -57,12 +57,14 @@ struct MPWall : MPWallData
 // From FP64 positions: component d of particle i at pos[d * comp_stride + i * row_stride]
 // (the body's SoA layout, or host rows).
 template <int D>
-__global__ void k_mp_from_fp64(size_t n, const double *__restrict__ pos, size_t comp_stride, size_t row_stride,
-                               MPConst k, uint32_t *__restrict__ ncell, float *__restrict__ noff,
-                               uint32_t *__restrict__ key, uint32_t *__restrict__ rank, uint32_t *__restrict__ count)
+// Particles [first, end) of n (a chunk of the rows, or all of them).
+__global__ void k_mp_from_fp64(size_t n, size_t first, size_t end, const double *__restrict__ pos,
+                               size_t comp_stride, size_t row_stride, MPConst k, uint32_t *__restrict__ ncell,
+                               float *__restrict__ noff, uint32_t *__restrict__ key, uint32_t *__restrict__ rank,
+                               uint32_t *__restrict__ count)
 {
-    size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n)
+    size_t i = first + size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= end)
         return;
     const MeshDev &m = k.m;
     double x[3] = {0, 0, 0};
@@ -1010,6 +1012,9 @@ T *dalloc(size_t n)
 }
 } // namespace
 
+// Chunks of the position rows sphx_mp_upload_host copies and hashes in a pipeline.
+constexpr int kUploadChunks = 4;
+
 struct sphx_mp_s
 {
     sphx_ctx ctx = nullptr;
@@ -1041,6 +1046,7 @@ struct sphx_mp_s
     // releases the velocity rows after the last sub-step's 1st half
     double *host_pos = nullptr, *host_vel = nullptr, *host_rho = nullptr, *host_p = nullptr;
     cudaEvent_t ev_half = nullptr;
+    cudaEvent_t ev_chunk[kUploadChunks] = {}; // position chunks of sphx_mp_upload_host
     int block = 128, strategy = 0;
     // tile-grouped traversal (TileShape): tile[0] == 0 keeps the cell order; `order` holds
     // the particles grouped by tile, recomputed at every configuration update
@@ -1706,10 +1712,10 @@ int import_fluid(sphx_mp mp, sphx_body fb, double rho0, double c0)
     if (n > 0)
     {
         if (D == 2)
-            k_mp_from_fp64<2><<<grid_for(n, 256), 256, 0, s>>>(n, (const double *)pos->dev, n, 1, mp->k, mp->ncell,
+            k_mp_from_fp64<2><<<grid_for(n, 256), 256, 0, s>>>(n, 0, n, (const double *)pos->dev, n, 1, mp->k, mp->ncell,
                                                                mp->noff, mp->key, mp->rank, mp->count);
         else
-            k_mp_from_fp64<3><<<grid_for(n, 256), 256, 0, s>>>(n, (const double *)pos->dev, n, 1, mp->k, mp->ncell,
+            k_mp_from_fp64<3><<<grid_for(n, 256), 256, 0, s>>>(n, 0, n, (const double *)pos->dev, n, 1, mp->k, mp->ncell,
                                                                mp->noff, mp->key, mp->rank, mp->count);
         ctx->launches++;
     }
@@ -2016,6 +2022,9 @@ int ensure_host_io(sphx_mp mp)
         SPHX_CUDA(cudaEventCreateWithFlags(&mp->ev_rest, cudaEventDisableTiming));
     if (!mp->ev_half)
         SPHX_CUDA(cudaEventCreateWithFlags(&mp->ev_half, cudaEventDisableTiming));
+    for (cudaEvent_t &e : mp->ev_chunk)
+        if (!e)
+            SPHX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     return SPHX_OK;
 }
 
@@ -2035,23 +2044,32 @@ int upload_host(sphx_mp mp, const double *pos, const double *vel, const double *
     double *spos = mp->stage, *svel = spos + n * D, *sforce = svel + n * D, *srho = sforce + n * D,
            *sdrho = srho + n;
     const size_t vec = n * D * sizeof(double), sca = n * sizeof(double);
+    SPHX_CUDA(cudaMemsetAsync(mp->count, 0, mp->ncells * sizeof(uint32_t), s));
+    SPHX_CUDA(cudaEventRecord(mp->ev_pos, s));
     if (n > 0)
     {
-        SPHX_CUDA(cudaMemcpyAsync(spos, pos, vec, cudaMemcpyHostToDevice, s));
-        SPHX_CUDA(cudaEventRecord(mp->ev_pos, s));
+        // the position rows in chunks on the side stream, each hashed on the context's
+        // stream as soon as it has arrived (the hash of one chunk overlaps the copy of the
+        // next); then the other rows
         SPHX_CUDA(cudaStreamWaitEvent(mp->side, mp->ev_pos, 0));
+        for (int c = 0; c < kUploadChunks; ++c)
+        {
+            const size_t b0 = n * size_t(c) / kUploadChunks, b1 = n * size_t(c + 1) / kUploadChunks;
+            if (b1 == b0)
+                continue;
+            SPHX_CUDA(cudaMemcpyAsync(spos + b0 * D, pos + b0 * D, (b1 - b0) * D * sizeof(double),
+                                      cudaMemcpyHostToDevice, mp->side));
+            SPHX_CUDA(cudaEventRecord(mp->ev_chunk[c], mp->side));
+            SPHX_CUDA(cudaStreamWaitEvent(s, mp->ev_chunk[c], 0));
+            k_mp_from_fp64<D><<<grid_for(b1 - b0, 256), 256, 0, s>>>(n, b0, b1, spos, 1, D, mp->k, mp->ncell,
+                                                                     mp->noff, mp->key, mp->rank, mp->count);
+            SPHX_LAUNCHED(ctx);
+        }
         SPHX_CUDA(cudaMemcpyAsync(svel, vel, vec, cudaMemcpyHostToDevice, mp->side));
         SPHX_CUDA(cudaMemcpyAsync(sforce, force, vec, cudaMemcpyHostToDevice, mp->side));
         SPHX_CUDA(cudaMemcpyAsync(srho, rho, sca, cudaMemcpyHostToDevice, mp->side));
         SPHX_CUDA(cudaMemcpyAsync(sdrho, drho_dt, sca, cudaMemcpyHostToDevice, mp->side));
         SPHX_CUDA(cudaEventRecord(mp->ev_rest, mp->side));
-    }
-    SPHX_CUDA(cudaMemsetAsync(mp->count, 0, mp->ncells * sizeof(uint32_t), s));
-    if (n > 0)
-    {
-        k_mp_from_fp64<D><<<grid_for(n, 256), 256, 0, s>>>(n, spos, 1, D, mp->k, mp->ncell, mp->noff, mp->key,
-                                                           mp->rank, mp->count);
-        SPHX_LAUNCHED(ctx);
     }
     SPHX_TRY(sort_keys(mp, n, mp->f_offset));
     if (n > 0)
@@ -2221,6 +2239,9 @@ extern "C" int sphx_mp_destroy(sphx_mp mp)
         cudaEventDestroy(mp->ev_rest);
     if (mp->ev_half)
         cudaEventDestroy(mp->ev_half);
+    for (cudaEvent_t e : mp->ev_chunk)
+        if (e)
+            cudaEventDestroy(e);
     for (void *p : mp->owned)
         cudaFree(p);
     if (mp->h_slots)
