@@ -128,15 +128,8 @@ __global__ void k_b_rehash(size_t n, MPState f, const uint32_t *__restrict__ sta
     const BInst &k = inst[find_instance(starts, count, uint32_t(i))];
     int c0[3];
     unpack_cell<D>(__float_as_uint(f.geo0[i].w), c0);
-    double o[3] = {0.0, 0.0, 0.0}, no[3];
-#pragma unroll
-    for (int d = 0; d < D; ++d)
-        o[d] = offset_of(f, n, i, d);
     int c[3] = {0, 0, 0};
-    rehash_relative<D>(k.m, k.inv_gs, false, c0, o, c, no);
-#pragma unroll
-    for (int d = 0; d < D; ++d)
-        stage_offset(noff, n, i, d, no[d]);
+    rehash_particle<D>(k.m, k.inv_gs, k.p.gs_f, false, f, n, i, c0, c, noff);
     store_hash<D>(k, c, ncell, i, key, rank, cnt);
 }
 

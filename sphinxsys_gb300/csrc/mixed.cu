@@ -120,15 +120,8 @@ __global__ void k_mp_rehash(size_t n, MPFluid f, MPConst k, uint32_t *__restrict
     const MeshDev &m = k.m;
     int c0[3];
     unpack_cell<D>(__float_as_uint(f.geo0[i].w), c0);
-    double o[3] = {0.0, 0.0, 0.0}, no[3];
-#pragma unroll
-    for (int d = 0; d < D; ++d)
-        o[d] = offset_of(f, n, i, d);
     int c[3] = {0, 0, 0};
-    rehash_relative<D>(m, k.inv_gs, k.periodic != 0, c0, o, c, no);
-#pragma unroll
-    for (int d = 0; d < D; ++d)
-        stage_offset(noff, n, i, d, no[d]);
+    rehash_particle<D>(m, k.inv_gs, k.p.gs_f, k.periodic != 0, f, n, i, c0, c, noff);
     ncell[i] = pack_cell<D>(c);
     uint32_t lc = linear_cell<D>(m, c);
     key[i] = lc;

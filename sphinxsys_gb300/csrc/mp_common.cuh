@@ -264,6 +264,44 @@ __device__ __forceinline__ void stage_offset(float *noff, size_t n, size_t i, in
     noff[(3 + d) * n + i] = float(x - double(hi));
 }
 
+// Re-hash of particle i (cell c0 at the last configuration): its new sub-cell c and the
+// staged offset pair.  A particle whose FP32 offset lies inside its sub-cell on every axis,
+// away from the faces by a margin far above the residual, keeps its cell and its offset
+// pair as they are, with no FP64 arithmetic (rehash_relative would give the same cell and
+// the same offset); the others are re-based in FP64 by rehash_relative.
+template <int D>
+__device__ __forceinline__ void rehash_particle(const MeshDev &m, double inv_gs, float gs_f, bool periodic,
+                                                const MPState &f, size_t n, size_t i, const int *c0, int *c,
+                                                float *noff)
+{
+    bool inside = true;
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+    {
+        const float o = f.off[d * n + i];
+        inside = inside && o > 0.0f && o < gs_f * (1.0f - 1.0f / 65536.0f);
+    }
+    if (inside)
+    {
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+        {
+            c[d] = c0[d];
+            noff[d * n + i] = f.off[d * n + i];
+            noff[(3 + d) * n + i] = f.off_lo[d * n + i];
+        }
+        return;
+    }
+    double o[3] = {0.0, 0.0, 0.0}, no[3];
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        o[d] = offset_of(f, n, i, d);
+    rehash_relative<D>(m, inv_gs, periodic, c0, o, c, no);
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+        stage_offset(noff, n, i, d, no[d]);
+}
+
 // Position half-step x += dt / 2 v in FP64 on the stored pair.
 __device__ __forceinline__ void half_step(const MPState &f, size_t n, size_t i, int d, double dt, float v)
 {
